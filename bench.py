@@ -1,0 +1,373 @@
+#!/usr/bin/env python
+"""Benchmark of the DEMON RK4 / shielded-Coulomb hot path on GB300.
+
+One "step" is one RK4 step (four fused pair-force + stage launches) of the
+workload's cloud.  Metric: pair-interactions/s = 4 * N(N-1) * steps / time
+(ordered pairs i != j, four force evaluations per RK4 step), whole job.
+
+    python bench.py [--steps K] [--warmup W] [--workload disk16k]
+                    [--precision fp32c] [--impl gb300|reference]
+
+Multi-GPU (torchrun, one rank per GPU): every rank integrates its own
+replica of the workload (independent clouds, no collective on the data path,
+weak scaling); the time is the max over ranks.
+
+Prints ONE JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from demon_simulation_code_gb300 import workloads as W  # noqa: E402
+
+METRIC = "pair-interactions/s/GPU: FP32-compensated vs FP64 at <=1e-6 rel force err"
+UNIT = "pair-interactions/s"
+FLOPS_PER_PAIR = 23  # algorithmic FP32 flops per ordered pair
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="disk16k", choices=sorted(W.WORKLOADS))
+    ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def workload(name):
+    if name == "disk16k":
+        return W.disk16k(thermal=True)
+    return W.WORKLOADS[name]()
+
+
+def config_of(w, args, extra=None):
+    c = w.clouds[0]
+    cfg = {
+        "workload": w.name,
+        "description": w.description,
+        "clouds": len(w.clouds),
+        "n": int(c.n) if len(w.clouds) == 1 else [int(x.n) for x in w.clouds][:4] + ["..."],
+        "dt": w.dt,
+        "pairs_per_force_eval": w.pairs_per_eval,
+        "force_evals_per_step": 4,
+        "precision": args.precision,
+        "l2": "flushed between timed steps (256 MiB write)",
+        "parallelism": f"replicas x{args.gpus}",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(self.NAMES, parts[2:]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_rk4_rate(w, nsteps, nthreads):
+    """The oracle (restatement of the reference's algorithm, OpenMP, per-block
+    locks like the reference) on `nsteps` RK4 steps of the first cloud."""
+    import oracle
+
+    oracle.build()
+    o = oracle.Oracle()
+    c = w.clouds[0]
+    p = oracle.make_params(**c.params())
+    t0 = time.perf_counter()
+    o.rk4_fixed(c.x, c.y, c.vx, c.vy, c.q, c.m, p, w.dt, nsteps, 0, nthreads)
+    el = time.perf_counter() - t0
+    pairs = 4.0 * c.n * (c.n - 1) * nsteps
+    return pairs / el, el
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU algorithm (oracle port: the reference sources need
+    x86 SSE4.2 and do not build on the Arm host) on this host's cores."""
+    if rank != 0:
+        return 0
+    w = workload(args.workload)
+    threads = cpu_threads()
+    nst = max(1, min(args.steps, 10))
+    if args.warmup > 0:
+        cpu_rk4_rate(w, 1, threads)
+    rate, el = cpu_rk4_rate(w, nst, threads)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": nst, "warmup": min(args.warmup, 1), "ms_per_step": el / nst * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator, demon_simulation_code_gb300/workloads.py)",
+        "config": config_of(w, args, {"precision": "fp64 (CPU)"}),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{nst} RK4 steps of {w.name} (oracle/demon_oracle.c, OpenMP "
+                                   f"per-block locks as in ShieldedCoulombForce.cpp), "
+                                   f"{threads} threads, {el:.2f} s"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device")
+    torch.cuda.set_device(local)
+    from demon_simulation_code_gb300 import Context, DeviceCloud
+
+    w = workload(args.workload)
+    c0 = w.clouds[0]
+    n = c0.n
+    pairs_step = 4.0 * n * (n - 1)
+    stream = torch.cuda.current_stream()
+    ctx = Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    cloud = DeviceCloud.from_cloud(ctx, c0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def timed_steps(prec, k):
+        evs = []
+        for _ in range(k):
+            flush.fill_(1.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            cloud.step(1, w.dt, prec)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+    # warm-up (untimed)
+    cloud.step(max(args.warmup, 3), w.dt, args.precision)
+    torch.cuda.synchronize()
+
+    # timed region: K steps, pair kernels bracketed by events inside the library
+    ctx.profile(True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        elapsed = timed_steps(args.precision, args.steps)
+    pair_ms, launches, pairs_prof = ctx.profile_read()
+    ctx.profile(False)
+    t_max = elapsed
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = pairs_step * args.steps * world / t_max
+
+    # FP64 kernel on the same workload (the 5x comparison)
+    fp64_value = None
+    if args.precision == "fp32c" and args.fp64_steps > 0:
+        c64 = DeviceCloud.from_cloud(ctx, c0)
+        c64.step(1, w.dt, "fp64")
+        torch.cuda.synchronize()
+        cloud_saved = cloud
+        cloud = c64
+        e64 = timed_steps("fp64", args.fp64_steps)
+        cloud = cloud_saved
+        fp64_value = pairs_step * args.fp64_steps / e64
+        c64.close()
+
+    # end to end through the public API with host buffers: pinned H2D of the
+    # state, one RK4 step, D2H of the state, every step
+    pin = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(4)]
+    hx = [p.numpy() for p in pin]
+    st = cloud.download()
+    for dst, src in zip(hx, st):
+        dst[:] = src
+    e2e_cloud = DeviceCloud.from_cloud(ctx, c0)
+    e2e_cloud.upload(*hx)
+    e2e_cloud.step(1, w.dt, args.precision)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_cloud.upload(*hx)
+        e2e_cloud.step(1, w.dt, args.precision)
+        out = e2e_cloud.download()
+        for dst, src in zip(hx, out):
+            dst[:] = src
+    torch.cuda.synchronize()
+    e2e_el = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_el], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_el = float(t.item())
+    e2e_value = pairs_step * args.e2e_steps * world / e2e_el
+
+    # roofline of the dominant kernel (fused pair + stage, FP32 pipe bound)
+    peak = ctx.probe_peak("fp32")
+    avg_launch_s = pair_ms / 1e3 / max(launches, 1)
+    achieved = FLOPS_PER_PAIR * n * (n - 1) / avg_launch_s / 1e12
+    kname = "pair_stage_fp32c" if args.precision == "fp32c" else "pair_stage_fp64"
+    traffic = traffic_from_profiles(kname, w.name)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and args.cpu_steps > 0:
+        threads = cpu_threads()
+        rate, el = cpu_rk4_rate(w, args.cpu_steps, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_steps} RK4 steps of {w.name} (oracle/demon_oracle.c, "
+                         f"OpenMP per-block locks as in the reference), {threads} threads, "
+                         f"{el:.2f} s"}
+
+    if rank == 0:
+        res = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32c" else "f64",
+            "data": "synthetic (seeded generator, demon_simulation_code_gb300/workloads.py)",
+            "config": config_of(w, args),
+            "fp64_value": fp64_value,
+            "fp32c_over_fp64": (value / world / fp64_value) if fp64_value else None,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * n,
+                    "d2h_bytes_per_step": 4 * 8 * n, "steps": args.e2e_steps},
+            "gpu_launches": 4 * args.steps,
+            "roofline": {"bound": "fp32-pipe", "kernel": kname, "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": traffic,
+                         "flops_per_pair": FLOPS_PER_PAIR,
+                         "avg_launch_us": avg_launch_s * 1e6,
+                         "peak_source": "in-run FP32 FMA probe (dm_probe_peak); "
+                                        "MEASURED_PEAKS.json has no FP32 figure"},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(res))
+    return 0
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args)
+    args.gpus = world if world > 1 else args.gpus
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank)
+        return run_gb300(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

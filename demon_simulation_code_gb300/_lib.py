@@ -1,0 +1,116 @@
+"""ctypes binding of libdemon_gb300.so (the C ABI in include/demon_gb300.h).
+
+There is no CPU fallback: if the library is missing or the GPU is not an
+sm_103a device, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB
+
+DM_OK = 0
+DM_FP64 = 0
+DM_FP32C = 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_lib = None
+
+
+class DemonError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[dm status {code}] {message}")
+        self.code = code
+
+
+class ForceParams(ctypes.Structure):
+    """dm_force_params."""
+
+    _fields_ = [
+        ("flags", ctypes.c_longlong),
+        ("shielding", ctypes.c_double),
+        ("confine", ctypes.c_double),
+        ("confine_x", ctypes.c_double),
+        ("confine_y", ctypes.c_double),
+        ("gamma", ctypes.c_double),
+        ("heat", ctypes.c_double),
+        ("thermal_mode", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+def force_params(flags, shielding=2e4, confine=0.0, confine_x=0.0, confine_y=0.0, gamma=0.0,
+                 heat=0.0, thermal_mode=1, seed=0) -> ForceParams:
+    return ForceParams(int(flags), shielding, confine, confine_x, confine_y, gamma, heat,
+                       int(thermal_mode), 0, int(seed))
+
+
+# (name, restype, argtypes) of every exported symbol
+SIGNATURES = {
+    "dm_version": (ctypes.c_int, []),
+    "dm_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "dm_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dm_ctx_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dm_ctx_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "dm_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "dm_ctx_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dm_ctx_profile_read": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_longlong), _dp]),
+    "dm_probe_peak": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "dm_cloud_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp,
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "dm_cloud_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dm_cloud_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "dm_cloud_upload": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+    "dm_cloud_download": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+    "dm_cloud_set_charge_mass": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    "dm_cloud_set_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForceParams)]),
+    "dm_cloud_eval_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
+    "dm_cloud_eval_forces_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                   ctypes.c_void_p]),
+    "dm_cloud_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]),
+    "dm_cloud_move_particles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_int, ctypes.c_int, _dp,
+                                               ctypes.POINTER(ctypes.c_int)]),
+    "dm_cloud_modify_timestep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
+                                                ctypes.POINTER(ctypes.c_float), _dp]),
+    "dm_cloud_diagnostics": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "dm_cloud_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "dm_cloud_get_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+}
+
+
+def load(path: str = LIB) -> ctypes.CDLL:
+    """Loads the library (no build, no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error(ctx) -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().dm_last_error(ctx, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, ctx=None) -> None:
+    if rc != DM_OK:
+        raise DemonError(rc, last_error(ctx))
+
+
+def ptr(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(_dp)

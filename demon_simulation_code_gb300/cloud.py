@@ -1,0 +1,167 @@
+"""Object API over the C ABI: a GPU context and a device-resident cloud.
+
+Method names follow the reference's classes where one exists:
+``eval_forces`` is the sum of ``Force::force1`` over the ForceArray
+(Runge_Kutta2.cpp:90-93); ``move_particles`` is
+``Runge_Kutta4::moveParticles`` (Runge_Kutta4.cpp:23-137); ``step`` is the
+same for an explicit step count with a fixed dt.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import DM_FP32C, DM_FP64, check, ptr
+
+PRECISIONS = {"fp64": DM_FP64, "fp32c": DM_FP32C, DM_FP64: DM_FP64, DM_FP32C: DM_FP32C}
+
+
+def _prec(p) -> int:
+    try:
+        return PRECISIONS[p]
+    except KeyError:
+        raise ValueError(f"unknown precision {p!r}") from None
+
+
+class Context:
+    """One GPU + one CUDA stream (dm_ctx)."""
+
+    def __init__(self, device: int = 0):
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(lib.dm_ctx_create(device, ctypes.byref(h)), None)
+        self.lib = lib
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.dm_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        check(self.lib.dm_ctx_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)), self.h)
+
+    def synchronize(self):
+        check(self.lib.dm_ctx_synchronize(self.h), self.h)
+
+    def profile(self, enable: bool):
+        check(self.lib.dm_ctx_profile_enable(self.h, int(enable)), self.h)
+
+    def profile_read(self):
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        pairs = ctypes.c_double()
+        check(self.lib.dm_ctx_profile_read(self.h, ctypes.byref(ms), ctypes.byref(n),
+                                           ctypes.byref(pairs)), self.h)
+        return ms.value, n.value, pairs.value
+
+    def probe_peak(self, kind: str = "fp32") -> float:
+        v = ctypes.c_double()
+        check(self.lib.dm_probe_peak(self.h, 0 if kind == "fp32" else 1, ctypes.byref(v)), self.h)
+        return v.value
+
+
+class DeviceCloud:
+    """A device-resident cloud (dm_cloud)."""
+
+    def __init__(self, ctx: Context, x, y, vx, vy, q, m, params=None):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, vx, vy, q, m)]
+        n = len(arrs[0])
+        if any(len(a) != n for a in arrs):
+            raise ValueError("arrays differ in length")
+        h = ctypes.c_void_p()
+        check(self.lib.dm_cloud_create(ctx.h, n, *(ptr(a) for a in arrs), ctypes.byref(h)), ctx.h)
+        self.h = h
+        self.n = n
+        if params is not None:
+            self.set_forces(params)
+
+    @classmethod
+    def from_cloud(cls, ctx: Context, c) -> "DeviceCloud":
+        """From a workloads.Cloud."""
+        return cls(ctx, c.x, c.y, c.vx, c.vy, c.q, c.m, _lib.force_params(**c.params()))
+
+    def close(self):
+        if self.h:
+            self.lib.dm_cloud_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        check(rc, self.ctx.h)
+
+    def set_forces(self, params):
+        if isinstance(params, dict):
+            params = _lib.force_params(**params)
+        self._chk(self.lib.dm_cloud_set_forces(self.h, ctypes.byref(params)))
+
+    def upload(self, x, y, vx, vy):
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, vx, vy)]
+        self._chk(self.lib.dm_cloud_upload(self.h, *(ptr(v) for v in a)))
+
+    def download(self):
+        out = [np.empty(self.n) for _ in range(4)]
+        self._chk(self.lib.dm_cloud_download(self.h, *(ptr(v) for v in out)))
+        return tuple(out)
+
+    def set_charge_mass(self, q=None, m=None):
+        qa = None if q is None else np.ascontiguousarray(q, dtype=np.float64)
+        ma = None if m is None else np.ascontiguousarray(m, dtype=np.float64)
+        self._chk(self.lib.dm_cloud_set_charge_mass(self.h, None if qa is None else ptr(qa),
+                                                    None if ma is None else ptr(ma)))
+
+    def eval_forces(self, precision="fp64"):
+        fx = np.empty(self.n)
+        fy = np.empty(self.n)
+        self._chk(self.lib.dm_cloud_eval_forces(self.h, _prec(precision), ptr(fx), ptr(fy)))
+        return fx, fy
+
+    def step(self, nsteps: int, dt: float, precision="fp32c", t: float | None = None):
+        tt = ctypes.c_double(t or 0.0)
+        self._chk(self.lib.dm_cloud_step(self.h, int(nsteps), float(dt), _prec(precision),
+                                         ctypes.byref(tt)))
+        return tt.value
+
+    def move_particles(self, end_time: float, dt: float, t: float, precision="fp64",
+                       adaptive: bool = False):
+        tt = ctypes.c_double(t)
+        steps = ctypes.c_int()
+        self._chk(self.lib.dm_cloud_move_particles(self.h, float(end_time), float(dt),
+                                                   _prec(precision), int(adaptive),
+                                                   ctypes.byref(tt), ctypes.byref(steps)))
+        return tt.value, steps.value
+
+    def modify_timestep(self, init_dt: float):
+        dmin = ctypes.c_float()
+        dt = ctypes.c_double()
+        self._chk(self.lib.dm_cloud_modify_timestep(self.h, float(init_dt), ctypes.byref(dmin),
+                                                    ctypes.byref(dt)))
+        return dmin.value, dt.value
+
+    def diagnostics(self):
+        out = np.zeros(5)
+        self._chk(self.lib.dm_cloud_diagnostics(self.h, ptr(out)))
+        return out
+
+    def set_step_counter(self, step: int):
+        self._chk(self.lib.dm_cloud_set_step_counter(self.h, int(step)))
+
+    def get_step_counter(self) -> int:
+        v = ctypes.c_uint64()
+        self._chk(self.lib.dm_cloud_get_step_counter(self.h, ctypes.byref(v)))
+        return v.value

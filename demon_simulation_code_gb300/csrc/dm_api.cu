@@ -1,0 +1,708 @@
+// dm_api.cu -- host side of the C ABI declared in include/demon_gb300.h.
+//
+// One dm_ctx = one GPU + one stream.  One dm_cloud = one device-resident
+// particle cloud (layout in dm_device.cuh).  Per RK4 step the library issues
+// four launches of the fused pair+stage kernel (dm_pair.cuh); fixed-dt step
+// sequences are captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/demon_gb300.h"
+#include "dm_misc.cuh"
+#include "dm_pair.cuh"
+
+using namespace dm;
+
+static_assert(sizeof(dm_force_params) == sizeof(ForceParams), "force params layout");
+
+namespace {
+
+std::string g_create_error;
+
+constexpr int kNT32 = 128, kILP32 = 4, kJT32 = 512;
+constexpr int kNT64 = 128, kILP64 = 2, kJT64 = 256;
+constexpr int kGraphSteps = 16;
+
+}  // namespace
+
+struct dm_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    std::string err;
+    bool prof = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
+    size_t prof_used = 0;
+    double prof_pairs = 0.0;
+    long long prof_launches = 0;
+
+    int fail(int code, const char *fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+};
+
+struct GraphKey {
+    int precision;
+    int nsteps;
+    double dt;
+    bool operator<(const GraphKey &o) const {
+        if (precision != o.precision) return precision < o.precision;
+        if (nsteps != o.nsteps) return nsteps < o.nsteps;
+        return dt < o.dt;
+    }
+};
+
+struct dm_cloud {
+    dm_ctx *ctx = nullptr;
+    int n = 0, n_pad = 0;
+    void *block = nullptr;
+    CloudDev d{};
+    ForceParams f{};
+    double coulomb = 0.0;
+    double *d_fx = nullptr, *d_fy = nullptr;
+    double *d_dt = nullptr;
+    unsigned int *d_min = nullptr;
+    float *d_dmin = nullptr;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    cudaStream_t graph_stream = nullptr;  // stream the graphs were built for
+
+    void drop_graphs() {
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
+};
+
+#define DM_CUDA(ctx, call)                                                                   \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return (ctx)->fail(DM_ERR_CUDA, "%s failed: %s (%s:%d)", #call,                 \
+                               cudaGetErrorString(e_), __FILE__, __LINE__);                 \
+    } while (0)
+
+namespace {
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+int check_device_errors(dm_ctx *ctx, dm_cloud *c) {
+    int h = 0;
+    DM_CUDA(ctx, cudaMemcpyAsync(&h, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h) {
+        DM_CUDA(ctx, cudaMemsetAsync(c->d.err, 0, sizeof(int), ctx->stream));
+        if (h & 2) return ctx->fail(DM_ERR_NUMERIC, "zero particle separation in the adaptive time step test");
+        return ctx->fail(DM_ERR_NUMERIC, "non-finite particle position after a stage (error bits 0x%x)", h);
+    }
+    return DM_OK;
+}
+
+ExpConsts make_exp_consts() {
+    ExpConsts E;
+    const double l2e = 1.4426950408889634;
+    E.l2e_hi = (float)l2e;
+    E.l2e_lo = (float)(l2e - (double)E.l2e_hi);
+    const double ln2 = 0.69314718055994530942;
+    double fact = 1.0, pw = 1.0;
+    for (int k = 0; k < 8; k++) {
+        if (k > 0) { fact *= k; pw *= -ln2; }
+        E.c[k] = (float)(pw / fact);
+    }
+    return E;
+}
+
+const ExpConsts &exp_consts() {
+    static const ExpConsts E = make_exp_consts();
+    return E;
+}
+
+StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const double *dt_dev) {
+    StageParams P{};
+    P.c = c->d;
+    P.f = c->f;
+    P.stage = stage;
+    P.mode = mode;
+    P.dt = dt;
+    P.dt_dev = dt_dev;
+    P.coulomb = c->coulomb;
+    P.fx_out = c->d_fx;
+    P.fy_out = c->d_fy;
+    const double kappa = c->f.shielding;
+    P.rc2 = (kappa > 0.0) ? (10.0 / kappa) * (10.0 / kappa) : INFINITY;
+    // FP32 r^2 is within ~6 ulp of the FP64 value; outside this band the
+    // FP32 decision cannot differ from the reference's FP64 one
+    P.rc2_lo = (float)(P.rc2 * (1.0 - 4e-6));
+    P.rc2_hi = (float)(P.rc2 * (1.0 + 4e-6));
+    P.kappa_f = (float)kappa;
+    return P;
+}
+
+// Cluster size (j split) for a cloud: aim for ~4 CTAs per SM.
+int pick_split(int n_pad, int tile, int num_sms) {
+    const int ntiles = (n_pad + tile - 1) / tile;
+    int s = 1;
+    while (s < 16 && ntiles * s < num_sms * 4 && (n_pad / (s * 2)) >= 256) s *= 2;
+    return s;
+}
+
+template <typename K>
+int launch_cluster(dm_ctx *ctx, K kernel, int ntiles, int S, int nt, size_t smem,
+                   const StageParams &P) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ntiles * S, 1, 1);
+    cfg.blockDim = dim3(nt, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, kernel, P));
+    return DM_OK;
+}
+
+template <typename K>
+int launch_cluster32(dm_ctx *ctx, K kernel, int ntiles, int S, int nt, size_t smem,
+                     const StageParams &P, const ExpConsts &E) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ntiles * S, 1, 1);
+    cfg.blockDim = dim3(nt, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, kernel, P, E));
+    return DM_OK;
+}
+
+int ensure_kernel_attrs(dm_ctx *ctx) {
+    static bool done[64] = {false};
+    int dev = ctx->device;
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (done[dev]) return DM_OK;
+    DM_CUDA(ctx, cudaFuncSetAttribute(pair_stage_fp32c<kNT32, kILP32, kJT32>,
+                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    DM_CUDA(ctx, cudaFuncSetAttribute(pair_stage_fp64<kNT64, kILP64, kJT64>,
+                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    done[dev] = true;
+    return DM_OK;
+}
+
+// One launch of the fused pair + stage kernel.
+int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, const double *dt_dev) {
+    dm_ctx *ctx = c->ctx;
+    int rc = ensure_kernel_attrs(ctx);
+    if (rc) return rc;
+    const StageParams P = make_stage_params(c, stage, mode, dt, dt_dev);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ctx->prof) {
+        if (ctx->prof_used == ctx->prof_events.size()) {
+            cudaEvent_t a, b;
+            DM_CUDA(ctx, cudaEventCreate(&a));
+            DM_CUDA(ctx, cudaEventCreate(&b));
+            ctx->prof_events.push_back({a, b});
+        }
+        e0 = ctx->prof_events[ctx->prof_used].first;
+        e1 = ctx->prof_events[ctx->prof_used].second;
+        ctx->prof_used++;
+        DM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+    }
+    if (precision == DM_FP32C) {
+        const int tile = kNT32 * kILP32;
+        const int S = pick_split(c->n_pad, tile, ctx->num_sms);
+        const int ntiles = (c->n + tile - 1) / tile;
+        const size_t smem = (size_t)kJT32 * 2 * sizeof(float4) + (size_t)kILP32 * kNT32 * sizeof(float4);
+        rc = launch_cluster32(ctx, pair_stage_fp32c<kNT32, kILP32, kJT32>, ntiles, S, kNT32, smem, P,
+                              exp_consts());
+    } else {
+        const int tile = kNT64 * kILP64;
+        const int S = pick_split(c->n_pad, tile, ctx->num_sms);
+        const int ntiles = (c->n + tile - 1) / tile;
+        const size_t smem = (size_t)kJT64 * sizeof(JD) + (size_t)kILP64 * kNT64 * sizeof(double2);
+        rc = launch_cluster(ctx, pair_stage_fp64<kNT64, kILP64, kJT64>, ntiles, S, kNT64, smem, P);
+    }
+    if (rc) return rc;
+    if (ctx->prof) {
+        DM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        ctx->prof_launches++;
+        ctx->prof_pairs += (double)c->n * (double)(c->n - 1);
+    }
+    return DM_OK;
+}
+
+int enqueue_steps(dm_cloud *c, int nsteps, double dt, int precision) {
+    for (int s = 0; s < nsteps; s++)
+        for (int st = 1; st <= 4; st++) {
+            int rc = launch_stage(c, precision, st, kModeStep, dt, nullptr);
+            if (rc) return rc;
+        }
+    return DM_OK;
+}
+
+int run_steps(dm_cloud *c, int nsteps, double dt, int precision) {
+    dm_ctx *ctx = c->ctx;
+    if (ctx->prof || nsteps < kGraphSteps) return enqueue_steps(c, nsteps, dt, precision);
+    if (c->graph_stream != ctx->stream) {
+        c->drop_graphs();
+        c->graph_stream = ctx->stream;
+    }
+    const GraphKey key{precision, kGraphSteps, dt};
+    auto it = c->graphs.find(key);
+    if (it == c->graphs.end()) {
+        cudaGraph_t g = nullptr;
+        DM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_steps(c, kGraphSteps, dt, precision);
+        cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ec != cudaSuccess) return ctx->fail(DM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+        cudaGraphExec_t ge = nullptr;
+        ec = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ec != cudaSuccess) return ctx->fail(DM_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ec));
+        it = c->graphs.emplace(key, ge).first;
+    }
+    const int reps = nsteps / kGraphSteps;
+    for (int r = 0; r < reps; r++) DM_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
+    return enqueue_steps(c, nsteps - reps * kGraphSteps, dt, precision);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int dm_version(void) { return DM_ABI_VERSION; }
+
+int dm_ctx_create(int device, dm_ctx **out) {
+    if (!out) {
+        g_create_error = "dm_ctx_create: out is NULL";
+        return DM_ERR_ARG;
+    }
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || device < 0 || device >= count) {
+        g_create_error = std::string("dm_ctx_create: no CUDA device ") + std::to_string(device) +
+                         (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : std::string());
+        return e != cudaSuccess ? DM_ERR_CUDA : DM_ERR_ARG;
+    }
+    dm_ctx *ctx = new dm_ctx();
+    ctx->device = device;
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    int major = 0, minor = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("dm_ctx_create: ") + cudaGetErrorString(e);
+        delete ctx;
+        return DM_ERR_CUDA;
+    }
+    if (major * 10 + minor != 103) {
+        g_create_error = "dm_ctx_create: this build targets sm_103a (GB300); device is sm_" +
+                         std::to_string(major) + std::to_string(minor);
+        cudaStreamDestroy(ctx->own_stream);
+        delete ctx;
+        return DM_ERR_UNSUPPORTED;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return DM_OK;
+}
+
+int dm_ctx_destroy(dm_ctx *ctx) {
+    if (!ctx) return DM_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &p : ctx->prof_events) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return DM_OK;
+}
+
+int dm_ctx_set_stream(dm_ctx *ctx, void *stream) {
+    if (!ctx) return DM_ERR_ARG;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return DM_OK;
+}
+
+int dm_ctx_synchronize(dm_ctx *ctx) {
+    if (!ctx) return DM_ERR_ARG;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DM_OK;
+}
+
+int dm_last_error(const dm_ctx *ctx, char *buf, size_t len) {
+    if (!buf || len == 0) return DM_ERR_ARG;
+    const std::string &s = ctx ? ctx->err : g_create_error;
+    snprintf(buf, len, "%s", s.c_str());
+    return DM_OK;
+}
+
+int dm_ctx_profile_enable(dm_ctx *ctx, int enable) {
+    if (!ctx) return DM_ERR_ARG;
+    ctx->prof = enable != 0;
+    ctx->prof_used = 0;
+    ctx->prof_pairs = 0.0;
+    ctx->prof_launches = 0;
+    return DM_OK;
+}
+
+int dm_ctx_profile_read(dm_ctx *ctx, double *total_ms, long long *launches, double *pairs) {
+    if (!ctx) return DM_ERR_ARG;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double tot = 0.0;
+    for (size_t k = 0; k < ctx->prof_used; k++) {
+        float ms = 0.0f;
+        DM_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->prof_events[k].first, ctx->prof_events[k].second));
+        tot += ms;
+    }
+    if (total_ms) *total_ms = tot;
+    if (launches) *launches = ctx->prof_launches;
+    if (pairs) *pairs = ctx->prof_pairs;
+    ctx->prof_used = 0;
+    ctx->prof_pairs = 0.0;
+    ctx->prof_launches = 0;
+    return DM_OK;
+}
+
+int dm_probe_peak(dm_ctx *ctx, int kind, double *tflops) {
+    if (!ctx || !tflops || (kind != 0 && kind != 1)) return DM_ERR_ARG;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    void *out = nullptr;
+    DM_CUDA(ctx, cudaMalloc(&out, 16));
+    cudaEvent_t a, b;
+    DM_CUDA(ctx, cudaEventCreate(&a));
+    DM_CUDA(ctx, cudaEventCreate(&b));
+    const int threads = 256, blocks = ctx->num_sms * 8;
+    const int iters = (kind == 0) ? 8192 : 256;
+    double best = 0.0;
+    for (int rep = 0; rep < 4; rep++) {
+        DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
+        if (kind == 0)
+            fma_probe<float><<<blocks, threads, 0, ctx->stream>>>((float *)out, iters, 0.999f, 0.001f);
+        else
+            fma_probe<double><<<blocks, threads, 0, ctx->stream>>>((double *)out, iters, 0.999, 0.001);
+        DM_CUDA(ctx, cudaGetLastError());
+        DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
+        DM_CUDA(ctx, cudaEventSynchronize(b));
+        float ms = 0.0f;
+        DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+        const double flops = 2.0 * 16.0 * (double)iters * threads * (double)blocks;
+        best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    *tflops = best;
+    return DM_OK;
+}
+
+int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const double *vx,
+                    const double *vy, const double *q, const double *m, dm_cloud **out) {
+    if (!ctx || !out || n < 1 || !x || !y || !vx || !vy || !q || !m)
+        return ctx ? ctx->fail(DM_ERR_ARG, "dm_cloud_create: bad argument") : DM_ERR_ARG;
+    *out = nullptr;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    dm_cloud *c = new dm_cloud();
+    c->ctx = ctx;
+    c->n = n;
+    c->n_pad = (n + 63) & ~63;
+    c->coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);
+    const size_t nd = align256((size_t)c->n_pad * sizeof(double));
+    const size_t nf4 = align256((size_t)c->n_pad * sizeof(float4));
+    const size_t total = nd * (6 + 2 + 8 + 4 + 2) + nf4 * 4 + 1024;
+    cudaError_t e = cudaMalloc(&c->block, total);
+    if (e != cudaSuccess) {
+        delete c;
+        return ctx->fail(DM_ERR_NOMEM, "dm_cloud_create: cudaMalloc(%zu) failed: %s", total, cudaGetErrorString(e));
+    }
+    char *p = (char *)c->block;
+    auto takeD = [&]() { double *r = (double *)p; p += nd; return r; };
+    auto takeF4 = [&]() { float4 *r = (float4 *)p; p += nf4; return r; };
+    c->d.n = n;
+    c->d.n_pad = c->n_pad;
+    c->d.x = takeD(); c->d.y = takeD(); c->d.vx = takeD(); c->d.vy = takeD();
+    c->d.q = takeD(); c->d.m = takeD();
+    c->d.vxc = takeD(); c->d.vyc = takeD();
+    for (int k = 0; k < 4; k++) c->d.a1[k] = takeD();
+    for (int k = 0; k < 4; k++) c->d.a23[k] = takeD();
+    for (int b = 0; b < 2; b++) { c->d.px[b] = takeD(); c->d.py[b] = takeD(); }
+    c->d_fx = takeD();
+    c->d_fy = takeD();
+    for (int b = 0; b < 2; b++) { c->d.pa[b] = takeF4(); c->d.pb[b] = takeF4(); }
+    c->d.step_ctr = (unsigned long long *)p; p += 256;
+    c->d.err = (int *)p; p += 256;
+    c->d_dt = (double *)p; p += 256;
+    c->d_min = (unsigned int *)p; c->d_dmin = (float *)(p + 64); p += 256;
+    cudaStream_t s = ctx->stream;
+    const size_t bytes = (size_t)n * sizeof(double);
+    e = cudaMemsetAsync(c->block, 0, total, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.x, x, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.y, y, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.vx, vx, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.vy, vy, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.q, q, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.m, m, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaFree(c->block);
+        delete c;
+        return ctx->fail(DM_ERR_CUDA, "dm_cloud_create: %s", cudaGetErrorString(e));
+    }
+    c->f.flags = kConfinement | kDrag | kShieldedCoulomb;
+    c->f.shielding = 2e4;
+    c->f.confine = 100;
+    c->f.gamma = 10.0;
+    *out = c;
+    return DM_OK;
+}
+
+int dm_cloud_destroy(dm_cloud *c) {
+    if (!c) return DM_ERR_ARG;
+    cudaSetDevice(c->ctx->device);
+    cudaStreamSynchronize(c->ctx->stream);
+    c->drop_graphs();
+    cudaFree(c->block);
+    delete c;
+    return DM_OK;
+}
+
+int dm_cloud_size(const dm_cloud *c, int *n) {
+    if (!c || !n) return DM_ERR_ARG;
+    *n = c->n;
+    return DM_OK;
+}
+
+int dm_cloud_upload(dm_cloud *c, const double *x, const double *y, const double *vx, const double *vy) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    if (!x || !y || !vx || !vy) return ctx->fail(DM_ERR_ARG, "dm_cloud_upload: NULL array");
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)c->n * sizeof(double);
+    DM_CUDA(ctx, cudaMemcpyAsync(c->d.x, x, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(c->d.y, y, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(c->d.vx, vx, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(c->d.vy, vy, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
+    DM_CUDA(ctx, cudaGetLastError());
+    return DM_OK;
+}
+
+int dm_cloud_download(dm_cloud *c, double *x, double *y, double *vx, double *vy) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)c->n * sizeof(double);
+    if (x) DM_CUDA(ctx, cudaMemcpyAsync(x, c->d.x, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, c->d.y, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, c->d.vx, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vy) DM_CUDA(ctx, cudaMemcpyAsync(vy, c->d.vy, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_device_errors(ctx, c);
+}
+
+int dm_cloud_set_charge_mass(dm_cloud *c, const double *q, const double *m) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)c->n * sizeof(double);
+    if (q) DM_CUDA(ctx, cudaMemcpyAsync(c->d.q, q, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (m) DM_CUDA(ctx, cudaMemcpyAsync(c->d.m, m, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    // the float charge copy lives in the stage buffers: refresh buffer 0
+    init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
+    DM_CUDA(ctx, cudaGetLastError());
+    return DM_OK;
+}
+
+int dm_cloud_set_forces(dm_cloud *c, const dm_force_params *p) {
+    if (!c || !p) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    const long long known = kConfinement | kDrag | kShieldedCoulomb | kThermal | kRectConfinement;
+    if (p->flags & ~known)
+        return ctx->fail(DM_ERR_UNSUPPORTED, "dm_cloud_set_forces: unsupported force flags 0x%llx",
+                         (unsigned long long)(p->flags & ~known));
+    if ((p->flags & kShieldedCoulomb) && !(p->shielding > 0.0 && std::isfinite(p->shielding)))
+        return ctx->fail(DM_ERR_ARG, "dm_cloud_set_forces: shielding must be positive and finite");
+    if (p->thermal_mode != 0 && p->thermal_mode != 1)
+        return ctx->fail(DM_ERR_ARG, "dm_cloud_set_forces: thermal_mode must be 0 or 1");
+    std::memcpy(&c->f, p, sizeof(ForceParams));
+    c->drop_graphs();
+    return DM_OK;
+}
+
+int dm_cloud_eval_forces_device(dm_cloud *c, int precision, double *d_fx, double *d_fy) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    if (precision != DM_FP64 && precision != DM_FP32C)
+        return ctx->fail(DM_ERR_ARG, "bad precision %d", precision);
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = launch_stage(c, precision, 1, kModeForceOnly, 0.0, nullptr);
+    if (rc) return rc;
+    const size_t bytes = (size_t)c->n * sizeof(double);
+    if (d_fx && d_fx != c->d_fx) DM_CUDA(ctx, cudaMemcpyAsync(d_fx, c->d_fx, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (d_fy && d_fy != c->d_fy) DM_CUDA(ctx, cudaMemcpyAsync(d_fy, c->d_fy, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return DM_OK;
+}
+
+int dm_cloud_eval_forces(dm_cloud *c, int precision, double *fx, double *fy) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    if (!fx || !fy) return ctx->fail(DM_ERR_ARG, "dm_cloud_eval_forces: NULL output");
+    int rc = dm_cloud_eval_forces_device(c, precision, nullptr, nullptr);
+    if (rc) return rc;
+    const size_t bytes = (size_t)c->n * sizeof(double);
+    DM_CUDA(ctx, cudaMemcpyAsync(fx, c->d_fx, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(fy, c->d_fy, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DM_OK;
+}
+
+int dm_cloud_step(dm_cloud *c, int nsteps, double dt, int precision, double *t_inout) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    if (nsteps < 0 || !std::isfinite(dt)) return ctx->fail(DM_ERR_ARG, "dm_cloud_step: bad nsteps/dt");
+    if (precision != DM_FP64 && precision != DM_FP32C)
+        return ctx->fail(DM_ERR_ARG, "bad precision %d", precision);
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = run_steps(c, nsteps, dt, precision);
+    if (rc) return rc;
+    if (t_inout)
+        for (int s = 0; s < nsteps; s++) *t_inout += dt;
+    return DM_OK;
+}
+
+int dm_cloud_modify_timestep(dm_cloud *c, double init_dt, float *min_dist, double *dt_out) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    if (c->n % 4 != 0 || c->n < 4)
+        return ctx->fail(DM_ERR_ARG, "adaptive time step needs n %% 4 == 0 (Integrator.cpp:87-107)");
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    DM_CUDA(ctx, cudaMemsetAsync(c->d_min, 0x7f, sizeof(unsigned int), ctx->stream));
+    const int nb = c->n / 4;
+    const long long total = (long long)nb * (nb + 1) / 2;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, (long long)ctx->num_sms * 16);
+    checked_min_dist2<<<std::max(blocks, 1), 256, 0, ctx->stream>>>(c->d.x, c->d.y, nb, c->d_min);
+    DM_CUDA(ctx, cudaGetLastError());
+    adaptive_dt<<<1, 1, 0, ctx->stream>>>(c->d_min, init_dt, c->d_dt, c->d_dmin, c->d.err);
+    DM_CUDA(ctx, cudaGetLastError());
+    if (min_dist) DM_CUDA(ctx, cudaMemcpyAsync(min_dist, c->d_dmin, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    if (dt_out) DM_CUDA(ctx, cudaMemcpyAsync(dt_out, c->d_dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_device_errors(ctx, c);
+}
+
+int dm_cloud_move_particles(dm_cloud *c, double end_time, double dt, int precision, int adaptive,
+                            double *t_inout, int *steps) {
+    if (!c || !t_inout) return c ? c->ctx->fail(DM_ERR_ARG, "t_inout is NULL") : DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    if (!(dt > 0.0)) return ctx->fail(DM_ERR_ARG, "dt must be positive");
+    double t = *t_inout;
+    int count = 0;
+    if (!adaptive) {
+        // same accumulation as `while (currentTime < endTime) currentTime += dt`
+        while (t < end_time) {
+            t += dt;
+            count++;
+        }
+        int rc = dm_cloud_step(c, count, dt, precision, nullptr);
+        if (rc) return rc;
+    } else {
+        while (t < end_time) {
+            double step_dt = 0.0;
+            int rc = dm_cloud_modify_timestep(c, dt, nullptr, &step_dt);
+            if (rc) return rc;
+            for (int st = 1; st <= 4; st++) {
+                rc = launch_stage(c, precision, st, kModeStep, 0.0, c->d_dt);
+                if (rc) return rc;
+            }
+            t += step_dt;
+            count++;
+        }
+    }
+    *t_inout = t;
+    if (steps) *steps = count;
+    return DM_OK;
+}
+
+int dm_cloud_diagnostics(dm_cloud *c, double out[5]) {
+    if (!c || !out) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int nt = 128;
+    const int blocks = (c->n + nt - 1) / nt;
+    double *partial = nullptr;
+    DM_CUDA(ctx, cudaMallocAsync((void **)&partial, sizeof(double) * 5 * blocks, ctx->stream));
+    diagnostics_partial<nt><<<blocks, nt, 0, ctx->stream>>>(c->d, c->f, c->coulomb, partial);
+    cudaError_t e = cudaGetLastError();
+    std::vector<double> h((size_t)5 * blocks);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h.data(), partial, sizeof(double) * 5 * blocks, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(partial, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->fail(DM_ERR_CUDA, "dm_cloud_diagnostics: %s", cudaGetErrorString(e));
+    for (int k = 0; k < 5; k++) out[k] = 0.0;
+    for (int b = 0; b < blocks; b++)
+        for (int k = 0; k < 5; k++) out[k] += h[(size_t)b * 5 + k];
+    return DM_OK;
+}
+
+int dm_cloud_set_step_counter(dm_cloud *c, uint64_t step) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    unsigned long long v[2] = {step, step};
+    DM_CUDA(ctx, cudaMemcpyAsync(c->d.step_ctr, v, sizeof(v), cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DM_OK;
+}
+
+int dm_cloud_get_step_counter(dm_cloud *c, uint64_t *step) {
+    if (!c || !step) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    unsigned long long v = 0;
+    DM_CUDA(ctx, cudaMemcpyAsync(&v, c->d.step_ctr, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *step = v;
+    return DM_OK;
+}
+
+}  // extern "C"

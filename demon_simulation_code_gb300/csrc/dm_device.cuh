@@ -1,0 +1,259 @@
+// dm_device.cuh -- device-side data layout and per-particle arithmetic of the
+// DEMON hot path on sm_103a.
+//
+// Layout in HBM (one cloud, n particles padded to n_pad, a multiple of 64):
+//   base state       x, y, vx, vy, q, m                      FP64 [n_pad]
+//   stage velocity   vxc, vyc  (CacheOperator's VxCache/VyCache) FP64 [n_pad]
+//   RK4 increments   a1[4] = k1, l1, m1, n1                 FP64 [n_pad]
+//                    a23[4] = k2+k3, l2+l3, m2+m3, n2+n3     FP64 [n_pad]
+//   stage positions  two buffers b = 0, 1; stage s reads b = (s-1)&1 and its
+//                    epilogue writes the next stage's positions into b^1:
+//                      px[b], py[b]  FP64 (CacheOperator's xCache/yCache)
+//                      pa[b] = (xh, yh, xh^2+yh^2, (float)q)  float4
+//                      pb[b] = (xl, yl, 0, 0)                  float4
+//                    with x = xh + xl exactly to 48 bits (two-float form).
+//   padding          particles n..n_pad-1 sit at 1e18 m with q = 0, so the
+//                    cutoff test never selects them.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dm {
+
+constexpr long long kConfinement = 1;
+constexpr long long kDrag = 2;
+constexpr long long kShieldedCoulomb = 4;
+constexpr long long kThermal = 16;
+constexpr long long kRectConfinement = 8192;
+
+constexpr float kPadPosition = 1.0e18f;
+
+struct ForceParams {  // same layout as dm_force_params
+    long long flags;
+    double shielding, confine, confine_x, confine_y, gamma, heat;
+    int thermal_mode, reserved;
+    unsigned long long seed;
+};
+
+struct CloudDev {
+    int n, n_pad;
+    double *x, *y, *vx, *vy, *q, *m;
+    double *vxc, *vyc;
+    double *a1[4];
+    double *a23[4];
+    double *px[2], *py[2];
+    float4 *pa[2], *pb[2];
+    unsigned long long *step_ctr;  // [2], see stage_step_index()
+    int *err;                      // device error flags
+};
+
+enum StageMode : int { kModeStep = 0, kModeForceOnly = 1 };
+
+// Everything a stage kernel needs, passed by value.
+struct StageParams {
+    CloudDev c;
+    ForceParams f;
+    int stage;            // 1..4
+    int mode;             // StageMode
+    double dt;            // fixed dt (used when dt_dev == nullptr)
+    const double *dt_dev; // adaptive dt computed on the device
+    double coulomb;       // 1/(4 pi eps0)
+    double *fx_out, *fy_out;  // kModeForceOnly outputs
+    // pair-kernel constants
+    double rc2;           // (10/kappa)^2
+    float rc2_lo, rc2_hi; // FP32 certain-in / certain-out bounds on r^2
+    float kappa_f;
+};
+
+// ---------------------------------------------------------------------------
+// Counter-based RNG: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t hi0 = __umulhi(M0, c[0]), lo0 = M0 * c[0];
+        const uint32_t hi1 = __umulhi(M1, c[2]), lo1 = M1 * c[2];
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += W0; k1 += W1;
+    }
+}
+
+// 53-bit uniform strictly inside (0, 1).
+__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+    const unsigned long long v = ((unsigned long long)a << 21) ^ ((unsigned long long)b >> 11);
+    return __dmul_rn(__dadd_rn((double)v, 0.5), 1.0 / 9007199254740992.0);
+}
+
+// Thermal kick for particle i at (step, stage).  Mode 0 is the reference's
+// form heatVal*U*(cos t, sin t) (ThermalForce.cpp:118-140) with counter-based
+// uniforms; mode 1 is a Gaussian of standard deviation `heat` per axis.
+__device__ __forceinline__ void thermal_kick(const ForceParams &f, uint32_t i,
+                                             unsigned long long step, int stage,
+                                             double &tx, double &ty) {
+    uint32_t c[4] = {i, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)stage};
+    philox4x32_10(c, (uint32_t)f.seed, (uint32_t)(f.seed >> 32));
+    const double u1 = u53(c[0], c[1]);
+    const double u2 = u53(c[2], c[3]);
+    const double th = __dmul_rn(u2, 2.0 * 3.14159265358979323846);
+    double s, co;
+    sincos(th, &s, &co);
+    if (f.thermal_mode == 0) {
+        const double a = __dmul_rn(u1, f.heat);
+        tx = __dmul_rn(a, co);
+        ty = __dmul_rn(a, s);
+    } else {
+        const double rad = sqrt(__dmul_rn(-2.0, log(u1)));
+        tx = __dmul_rn(f.heat, __dmul_rn(rad, co));
+        ty = __dmul_rn(f.heat, __dmul_rn(rad, s));
+    }
+}
+
+// RNG step index of the running stage.  Stage 1 reads slot 0 and copies it
+// to slot 1; stages 2-4 read slot 1; stage 4 advances slot 0.  Each slot is
+// written only in a launch that never reads it, so no launch races itself.
+__device__ __forceinline__ unsigned long long stage_step_index(const StageParams &P) {
+    const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
+    return (s == 1) ? P.c.step_ctr[0] : P.c.step_ctr[1];
+}
+__device__ __forceinline__ void stage_step_advance(const StageParams &P) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (P.mode == kModeForceOnly) return;
+    if (P.stage == 1) P.c.step_ctr[1] = P.c.step_ctr[0];
+    else if (P.stage == 4) P.c.step_ctr[0] = P.c.step_ctr[1] + 1ull;
+}
+
+// Two-float split of a position: x = hi + lo.
+__device__ __forceinline__ void split2(double x, float &hi, float &lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(__dsub_rn(x, (double)hi));
+}
+
+__device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, int i,
+                                                     double xs, double ys) {
+    c.px[b][i] = xs;
+    c.py[b][i] = ys;
+    float xh, xl, yh, yl;
+    split2(xs, xh, xl);
+    split2(ys, yh, yl);
+    c.pa[b][i] = make_float4(xh, yh, fmaf(yh, yh, xh * xh), __double2float_rn(c.q[i]));
+    c.pb[b][i] = make_float4(xl, yl, 0.0f, 0.0f);
+}
+
+// Reference cutoff decision for one pair, bit for bit:
+// r = sqrt(dx*dx + dy*dy) (no fused multiply-add, SSE4.2 has none),
+// kappa*r < 10 (ShieldedCoulombForce.cpp:144-147, 175-178).
+__device__ __forceinline__ bool ref_in_cutoff(double dx, double dy, double kappa, double &r,
+                                              double &a) {
+    r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    a = __dmul_rn(r, kappa);
+    return a < 10.0;
+}
+
+// The per-particle epilogue of one RK stage for particle i, given the
+// shielded-Coulomb pair sum (fpx, fpy) at the stage positions:
+//  - sums the enabled forces in the reference driver's order
+//    (driver.cpp:372-402): Confinement (ConfinementForce.cpp:48-54), Drag
+//    (DragForce.cpp:49-55), RectConfinement (RectConfinementForce.cpp:50-59),
+//    ShieldedCoulomb, Thermal;
+//  - stage increments k = (dt*Fx)/m, l = dt*Vx_stage (Runge_Kutta4.cpp:32-104);
+//  - the next stage's CacheOperator values (CacheOperator.cpp:28-73);
+//  - after stage 4 the combine v += (k1 + (2*(k2+k3) + k4))/6
+//    (Runge_Kutta4.cpp:107-133, 147-151).
+// Every FP64 operation is an explicit round-to-nearest intrinsic so nothing
+// is contracted into an FMA: given the same forces the state update is bit
+// for bit the reference's.
+__device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, double fpx,
+                                               double fpy) {
+    const CloudDev &c = P.c;
+    const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
+    const int b = (s - 1) & 1;
+    const double xs = c.px[b][i], ys = c.py[b][i];
+    const double vxs = (s == 1) ? c.vx[i] : c.vxc[i];
+    const double vys = (s == 1) ? c.vy[i] : c.vyc[i];
+    const double q = c.q[i], m = c.m[i];
+    const long long fl = P.f.flags;
+    double Fx = 0.0, Fy = 0.0;
+    if (fl & kConfinement) {
+        const double cq = __dmul_rn(q, P.f.confine);
+        Fx = __dadd_rn(Fx, __dmul_rn(cq, xs));
+        Fy = __dadd_rn(Fy, __dmul_rn(cq, ys));
+    }
+    if (fl & kDrag) {
+        const double d = __dmul_rn(m, -P.f.gamma);
+        Fx = __dadd_rn(Fx, __dmul_rn(d, vxs));
+        Fy = __dadd_rn(Fy, __dmul_rn(d, vys));
+    }
+    if (fl & kRectConfinement) {
+        Fx = __dadd_rn(Fx, __dmul_rn(__dmul_rn(q, P.f.confine_x), xs));
+        Fy = __dadd_rn(Fy, __dmul_rn(__dmul_rn(q, P.f.confine_y), ys));
+    }
+    if (fl & kShieldedCoulomb) {
+        Fx = __dadd_rn(Fx, fpx);
+        Fy = __dadd_rn(Fy, fpy);
+    }
+    if (fl & kThermal) {
+        double tx, ty;
+        thermal_kick(P.f, (uint32_t)i, stage_step_index(P), s, tx, ty);
+        Fx = __dadd_rn(Fx, tx);
+        Fy = __dadd_rn(Fy, ty);
+    }
+    if (P.mode == kModeForceOnly) {
+        P.fx_out[i] = Fx;
+        P.fy_out[i] = Fy;
+        return;
+    }
+    const double dt = P.dt_dev ? *P.dt_dev : P.dt;
+    const double k = __ddiv_rn(__dmul_rn(dt, Fx), m);
+    const double l = __dmul_rn(dt, vxs);
+    const double mm = __ddiv_rn(__dmul_rn(dt, Fy), m);
+    const double nn = __dmul_rn(dt, vys);
+    const double x = c.x[i], y = c.y[i], vx = c.vx[i], vy = c.vy[i];
+    double nx, ny, nvx = 0.0, nvy = 0.0;
+    if (s == 1 || s == 2) {
+        if (s == 1) {
+            c.a1[0][i] = k; c.a1[1][i] = l; c.a1[2][i] = mm; c.a1[3][i] = nn;
+        } else {
+            c.a23[0][i] = k; c.a23[1][i] = l; c.a23[2][i] = mm; c.a23[3][i] = nn;
+        }
+        // operation2 / operation3: cache = 0.5*tidbit + base
+        nx = __dadd_rn(__dmul_rn(0.5, l), x);
+        ny = __dadd_rn(__dmul_rn(0.5, nn), y);
+        nvx = __dadd_rn(__dmul_rn(0.5, k), vx);
+        nvy = __dadd_rn(__dmul_rn(0.5, mm), vy);
+    } else if (s == 3) {
+        c.a23[0][i] = __dadd_rn(c.a23[0][i], k);
+        c.a23[1][i] = __dadd_rn(c.a23[1][i], l);
+        c.a23[2][i] = __dadd_rn(c.a23[2][i], mm);
+        c.a23[3][i] = __dadd_rn(c.a23[3][i], nn);
+        // operation4: cache = base + tidbit
+        nx = __dadd_rn(x, l);
+        ny = __dadd_rn(y, nn);
+        nvx = __dadd_rn(vx, k);
+        nvy = __dadd_rn(vy, mm);
+    } else {
+        // da(a1, a2, a3, a4) = (a1 + ((a2 + a3)*2 + a4)) / 6
+        const double dvx = __ddiv_rn(__dadd_rn(c.a1[0][i], __dadd_rn(__dmul_rn(c.a23[0][i], 2.0), k)), 6.0);
+        const double dx = __ddiv_rn(__dadd_rn(c.a1[1][i], __dadd_rn(__dmul_rn(c.a23[1][i], 2.0), l)), 6.0);
+        const double dvy = __ddiv_rn(__dadd_rn(c.a1[2][i], __dadd_rn(__dmul_rn(c.a23[2][i], 2.0), mm)), 6.0);
+        const double dy = __ddiv_rn(__dadd_rn(c.a1[3][i], __dadd_rn(__dmul_rn(c.a23[3][i], 2.0), nn)), 6.0);
+        const double xn = __dadd_rn(x, dx), yn = __dadd_rn(y, dy);
+        c.vx[i] = __dadd_rn(vx, dvx);
+        c.x[i] = xn;
+        c.vy[i] = __dadd_rn(vy, dvy);
+        c.y[i] = yn;
+        nx = xn;
+        ny = yn;
+    }
+    write_stage_position(c, b ^ 1, i, nx, ny);
+    if (s < 4) {
+        c.vxc[i] = nvx;
+        c.vyc[i] = nvy;
+    }
+    if (!isfinite(nx) || !isfinite(ny)) atomicOr(c.err, 1);
+}
+
+}  // namespace dm

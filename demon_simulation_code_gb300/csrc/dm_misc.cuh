@@ -1,0 +1,167 @@
+// dm_misc.cuh -- O(N) and reduction kernels around the pair kernels:
+// stage-position initialisation, the adaptive-dt distance test, FP64
+// diagnostics and the peak-throughput probe.
+#pragma once
+
+#include "dm_device.cuh"
+
+namespace dm {
+
+// Writes stage buffer 0 (FP64 and two-float copies) from the base
+// positions, and the padding particles of both buffers.
+__global__ void init_positions(CloudDev c) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n_pad) return;
+    if (i < c.n) {
+        write_stage_position(c, 0, i, c.x[i], c.y[i]);
+    } else {
+        for (int b = 0; b < 2; b++) {
+            c.px[b][i] = (double)kPadPosition;
+            c.py[b][i] = (double)kPadPosition;
+            c.pa[b][i] = make_float4(kPadPosition, kPadPosition, kPadPosition * kPadPosition, 0.0f);
+            c.pb[b][i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        c.q[i] = 0.0;
+        c.m[i] = 1.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adaptive dt (Integrator::modifyTimeStep, Integrator.cpp:68-134).
+// Pairs checked: all 6 pairs inside each 4-block; between 4-blocks o < p,
+// element k of o with element (k - d) mod 4 of p for d = 0, 1, 2.
+// Separations are computed from (float)x exactly as the SSE code does
+// (sub, mul, mul, add, sqrt in FP32, no fused multiply-add).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float sep2_f32(float ax, float ay, float bx, float by) {
+    const float sx = __fsub_rn(ax, bx), sy = __fsub_rn(ay, by);
+    return __fadd_rn(__fmul_rn(sx, sx), __fmul_rn(sy, sy));
+}
+
+// One thread per (outer block o, inner block p >= o) visit, grid-strided over
+// the upper triangle of 4-blocks.  The minimum r^2 (a non-negative float, so
+// its bit pattern orders like an unsigned int) is combined with atomicMin,
+// which is order-independent.
+__global__ void checked_min_dist2(const double *__restrict__ x, const double *__restrict__ y,
+                                  int nb, unsigned int *out) {
+    const long long total = (long long)nb * (nb + 1) / 2;
+    float best = INFINITY;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        // decode t -> (o, p) with p >= o, row-major over o
+        long long o = (long long)((2.0 * nb + 1.0 - sqrt((2.0 * nb + 1.0) * (2.0 * nb + 1.0) - 8.0 * (double)t)) / 2.0);
+        if (o < 0) o = 0;
+        if (o >= nb) o = nb - 1;
+        while (o > 0 && o * nb - o * (o - 1) / 2 > t) o--;
+        while ((o + 1) * nb - (o + 1) * o / 2 <= t) o++;
+        const long long p = o + (t - (o * nb - o * (o - 1) / 2));
+        float ox[4], oy[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            ox[k] = __double2float_rn(x[4 * o + k]);
+            oy[k] = __double2float_rn(y[4 * o + k]);
+        }
+        if (p == o) {
+            const int ia[6] = {0, 2, 0, 1, 1, 0}, ib[6] = {1, 3, 3, 2, 3, 2};
+#pragma unroll
+            for (int e = 0; e < 6; e++) best = fminf(best, sep2_f32(ox[ia[e]], oy[ia[e]], ox[ib[e]], oy[ib[e]]));
+        } else {
+            float ix[4], iy[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                ix[k] = __double2float_rn(x[4 * p + k]);
+                iy[k] = __double2float_rn(y[4 * p + k]);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const int mi = (k - d + 4) & 3;
+                    best = fminf(best, sep2_f32(ox[k], oy[k], ix[mi], iy[mi]));
+                }
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) best = fminf(best, __shfl_xor_sync(0xffffffffu, best, off));
+    if ((threadIdx.x & 31) == 0) atomicMin(out, __float_as_uint(best));
+}
+
+// tryToReduceTimeStep (Integrator.cpp:144-155) applied to the minimum:
+// while dmin <= dist: dist /= 10.0f, dt /= 10.0.  A zero separation (where
+// the reference never terminates) sets error bit 2 and leaves dt unchanged.
+__global__ void adaptive_dt(const unsigned int *min_r2_bits, double init_dt, double *dt_out,
+                            float *dmin_out, int *err) {
+    const float dmin = __fsqrt_rn(__uint_as_float(*min_r2_bits));
+    float dist = 1.0e-4f;
+    double dt = init_dt;
+    if (dmin > 0.0f) {
+        for (int it = 0; it < 200 && dmin <= dist; it++) {
+            dist = __fdiv_rn(dist, 10.0f);
+            dt = __ddiv_rn(dt, 10.0);
+        }
+    } else {
+        atomicOr(err, 2);
+    }
+    *dt_out = dt;
+    if (dmin_out) *dmin_out = dmin;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 diagnostics: per-block partial sums of kinetic energy, Yukawa
+// potential (kappa*r < 10, counted once per unordered pair), confinement
+// potential and momentum, written to partial[blockIdx.x*5 + ...] and summed
+// in block order on the host.
+// ---------------------------------------------------------------------------
+template <int NT>
+__global__ void __launch_bounds__(NT) diagnostics_partial(const CloudDev c, const ForceParams f,
+                                                          double coulomb, double *partial) {
+    __shared__ double red[5][NT];
+    const int i = blockIdx.x * NT + threadIdx.x;
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (i < c.n) {
+        const double x = c.x[i], y = c.y[i], vx = c.vx[i], vy = c.vy[i], q = c.q[i], m = c.m[i];
+        v[0] = 0.5 * m * (vx * vx + vy * vy);
+        v[3] = m * vx;
+        v[4] = m * vy;
+        if (f.flags & kConfinement) v[2] += -0.5 * q * f.confine * (x * x + y * y);
+        if (f.flags & kRectConfinement) v[2] += -0.5 * q * (f.confine_x * x * x + f.confine_y * y * y);
+        if (f.flags & kShieldedCoulomb) {
+            double pe = 0.0;
+            for (int j = 0; j < c.n; j++) {
+                if (j == i) continue;
+                const double dx = x - c.x[j], dy = y - c.y[j];
+                double r, a;
+                if (ref_in_cutoff(dx, dy, f.shielding, r, a)) pe += coulomb * q * c.q[j] * exp(-a) / r;
+            }
+            v[1] = 0.5 * pe;
+        }
+    }
+    for (int e = 0; e < 5; e++) red[e][threadIdx.x] = v[e];
+    __syncthreads();
+    for (int s = NT / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int e = 0; e < 5; e++) red[e][threadIdx.x] += red[e][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int e = 0; e < 5; e++) partial[blockIdx.x * 5 + e] = red[e][0];
+}
+
+// ---------------------------------------------------------------------------
+// Peak probe: 16 independent FMA chains per thread.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void fma_probe(T *out, int iters, T a, T b) {
+    T acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) acc[k] = (T)(threadIdx.x + k);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) acc[k] = acc[k] * a + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) s += acc[k];
+    if (s == (T)-1.2345) out[0] = s;  // keeps the loop alive
+}
+
+}  // namespace dm

@@ -1,0 +1,160 @@
+"""Seeded synthetic inputs for the DEMON hot-path workloads.
+
+The reference publishes no dataset; every workload is generated here from a
+seed so the CUDA path, the oracle and the CPU baseline see identical inputs.
+Constants follow the reference's units: positions [m], velocities [m/s],
+charge [C], mass [kg] (m = 4/3 pi rho r^3 with rho = 2200 kg/m^3 and
+r = 1.45e-6 m, Cloud.cpp:74-81 gives 2.81e-14 kg).
+
+Workloads (name: sizes):
+  disk512     N=512 in a disk of radius 5e-3 m, kappa=2e4, k_c=1e8, drag 3,
+              thermal off, dt=1e-4, 1000 steps
+  disk16k     N=16384 in a disk of radius 2e-2 m, same constants, Gaussian
+              thermal kicks sigma=1e-14 N (counter RNG seed 1), dt=1e-4,
+              10000 steps
+  square256k  N=262144 in a 0.1 m x 0.1 m square, RectConfinementForce 1e8/1e8,
+              charges normal(-1.6e-15, 5%), kappa=5e4, drag 3, dt=5e-5, 100 steps
+  batch256    256 clouds, N ~ U{64..4096}, per-cloud kappa ~ U[1e4,5e4],
+              q ~ U[-2e-15,-1e-15], k_c ~ U[5e7,2e8], disk radius 2e-4*sqrt(N),
+              drag 3, thermal off, dt=1e-4, 2000 steps
+  adjoint64   64 clouds of N=2048 in a disk of radius 9e-3 m, true
+              (kappa, q, k_c) = (2e4, -1.6e-15, 1e8), 200 steps of dt=1e-4
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+CONFINEMENT = 1
+DRAG = 2
+SHIELDED_COULOMB = 4
+THERMAL = 16
+RECT_CONFINEMENT = 8192
+
+Q_DUST = -1.6e-15
+M_DUST = 2.81e-14
+
+
+@dataclass
+class Cloud:
+    """One cloud: state arrays plus force parameters (dm_force_params fields)."""
+
+    x: np.ndarray
+    y: np.ndarray
+    vx: np.ndarray
+    vy: np.ndarray
+    q: np.ndarray
+    m: np.ndarray
+    flags: int = CONFINEMENT | DRAG | SHIELDED_COULOMB
+    shielding: float = 2e4
+    confine: float = 1e8
+    confine_x: float = 0.0
+    confine_y: float = 0.0
+    gamma: float = 3.0
+    heat: float = 0.0
+    thermal_mode: int = 1
+    seed: int = 0
+
+    @property
+    def n(self) -> int:
+        return len(self.x)
+
+    def params(self) -> dict:
+        return dict(flags=self.flags, shielding=self.shielding, confine=self.confine,
+                    confine_x=self.confine_x, confine_y=self.confine_y, gamma=self.gamma,
+                    heat=self.heat, thermal_mode=self.thermal_mode, seed=self.seed)
+
+    def copy(self) -> "Cloud":
+        c = Cloud(**{k: (v.copy() if isinstance(v, np.ndarray) else v)
+                     for k, v in self.__dict__.items()})
+        return c
+
+
+def uniform_disk(rng: np.random.Generator, n: int, radius: float):
+    """r = R*sqrt(u), theta = 2*pi*u'."""
+    r = radius * np.sqrt(rng.random(n))
+    th = 2.0 * np.pi * rng.random(n)
+    return r * np.cos(th), r * np.sin(th)
+
+
+def disk_cloud(n: int, radius: float, seed: int, *, shielding=2e4, confine=1e8, gamma=3.0,
+               q=Q_DUST, m=M_DUST, heat=0.0, thermal_seed=0) -> Cloud:
+    rng = np.random.default_rng(seed)
+    x, y = uniform_disk(rng, n, radius)
+    flags = CONFINEMENT | DRAG | SHIELDED_COULOMB | (THERMAL if heat > 0 else 0)
+    return Cloud(x=x, y=y, vx=np.zeros(n), vy=np.zeros(n), q=np.full(n, q), m=np.full(n, m),
+                 flags=flags, shielding=shielding, confine=confine, gamma=gamma, heat=heat,
+                 thermal_mode=1, seed=thermal_seed)
+
+
+@dataclass
+class Workload:
+    name: str
+    clouds: list
+    dt: float
+    steps: int
+    description: str = ""
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def pairs_per_eval(self) -> int:
+        """Ordered pairs (i, j), i != j, in one force evaluation."""
+        return int(sum(c.n * (c.n - 1) for c in self.clouds))
+
+
+def disk512(seed: int = 0) -> Workload:
+    c = disk_cloud(512, 5e-3, seed)
+    return Workload("disk512", [c], 1e-4, 1000,
+                    "N=512 disk R=5e-3 m, kappa=2e4, k_c=1e8, drag 3, thermal off, dt=1e-4")
+
+
+def disk16k(seed: int = 1, thermal: bool = True) -> Workload:
+    c = disk_cloud(16384, 2e-2, seed, heat=1e-14 if thermal else 0.0, thermal_seed=1)
+    return Workload("disk16k", [c], 1e-4, 10000,
+                    "N=16384 disk R=2e-2 m, kappa=2e4, k_c=1e8, drag 3, "
+                    f"thermal {'Gaussian sigma=1e-14 N' if thermal else 'off'}, dt=1e-4")
+
+
+def square256k(seed: int = 2, n: int = 262144) -> Workload:
+    rng = np.random.default_rng(seed)
+    x = (rng.random(n) - 0.5) * 0.1
+    y = (rng.random(n) - 0.5) * 0.1
+    q = rng.normal(Q_DUST, abs(Q_DUST) * 0.05, n)
+    c = Cloud(x=x, y=y, vx=np.zeros(n), vy=np.zeros(n), q=q, m=np.full(n, M_DUST),
+              flags=RECT_CONFINEMENT | DRAG | SHIELDED_COULOMB, shielding=5e4, confine=0.0,
+              confine_x=1e8, confine_y=1e8, gamma=3.0)
+    return Workload("square256k", [c], 5e-5, 100,
+                    f"N={n} square 0.1 m, Rect 1e8/1e8, q~N(-1.6e-15,5%), kappa=5e4, dt=5e-5")
+
+
+def batch256(seed: int = 3, nclouds: int = 256, nmin: int = 64, nmax: int = 4096) -> Workload:
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(nmin, nmax + 1, nclouds)
+    clouds = []
+    for c in range(nclouds):
+        n = int(ns[c])
+        kappa = rng.uniform(1e4, 5e4)
+        q = rng.uniform(-2e-15, -1e-15)
+        kc = rng.uniform(5e7, 2e8)
+        x, y = uniform_disk(rng, n, 2e-4 * np.sqrt(n))
+        clouds.append(Cloud(x=x, y=y, vx=np.zeros(n), vy=np.zeros(n), q=np.full(n, q),
+                            m=np.full(n, M_DUST), shielding=kappa, confine=kc, gamma=3.0))
+    return Workload("batch256", clouds, 1e-4, 2000,
+                    f"{nclouds} clouds, N~U{{{nmin}..{nmax}}}, per-cloud kappa/q/k_c, dt=1e-4")
+
+
+def adjoint64(seed: int = 4, nclouds: int = 64, n: int = 2048) -> Workload:
+    rng = np.random.default_rng(seed)
+    clouds = []
+    for _ in range(nclouds):
+        x, y = uniform_disk(rng, n, 9e-3)
+        clouds.append(Cloud(x=x, y=y, vx=np.zeros(n), vy=np.zeros(n), q=np.full(n, Q_DUST),
+                            m=np.full(n, M_DUST), shielding=2e4, confine=1e8, gamma=3.0))
+    return Workload("adjoint64", clouds, 1e-4, 200,
+                    f"{nclouds} clouds N={n} disk R=9e-3, true (kappa,q,k_c)=(2e4,-1.6e-15,1e8)",
+                    extra={"perturb": 0.2, "checkpoint_every": 20})
+
+
+WORKLOADS = {"disk512": disk512, "disk16k": disk16k, "square256k": square256k,
+             "batch256": batch256, "adjoint64": adjoint64}

@@ -1,0 +1,194 @@
+/*
+ * demon_gb300.h -- C ABI of the GB300 (sm_103a) implementation of DEMON's
+ * RK4 / shielded-Coulomb hot path.
+ *
+ * The reference (AU-PSL/demon_simulation_code) has no C ABI: its hot path is
+ * a set of C++ virtual classes.  Each entry point below replaces one piece of
+ * that class API; the comment on each names the reference interface it
+ * stands in for (file:line).  The C++ classes in
+ * demon_simulation_code_gb300/csrc/host/ re-expose the reference's class
+ * names on top of these calls.
+ *
+ * Conventions
+ *  - Every call returns an int status: 0 (DM_OK) on success, a DM_ERR_* code
+ *    otherwise; dm_last_error() returns the message.  No call exits the
+ *    process or throws across the ABI (the reference exit(1)s on FITS errors,
+ *    driver.cpp:202-213).
+ *  - Plain pointers and sizes only.  "host" arrays are ordinary CPU memory
+ *    (pinned memory makes copies faster but is not required); "device"
+ *    arrays are CUDA device pointers on the context's device.
+ *  - One context drives one GPU through one CUDA stream.  Calls on one
+ *    context are not thread-safe; use one context per host thread.
+ *  - All particle arrays are FP64 structure-of-arrays, like the reference's
+ *    Cloud (Cloud.h:21-29).  Units: m, m/s, C, kg, N, s.
+ */
+#ifndef DEMON_GB300_H
+#define DEMON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DM_ABI_VERSION 1
+
+typedef enum dm_status {
+    DM_OK = 0,
+    DM_ERR_ARG = 1,         /* invalid argument (null pointer, bad size, bad enum) */
+    DM_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    DM_ERR_NOMEM = 3,       /* device or host allocation failed */
+    DM_ERR_STATE = 4,       /* object in the wrong state for this call */
+    DM_ERR_NUMERIC = 5,     /* non-finite result detected on the device */
+    DM_ERR_UNSUPPORTED = 6  /* feature not available on this device/build */
+} dm_status;
+
+/* Pair-force arithmetic.  The RK4 state update is FP64 in both modes. */
+typedef enum dm_precision {
+    DM_FP64 = 0,   /* all pair arithmetic in FP64 */
+    DM_FP32C = 1   /* FP32 pair arithmetic, two-float position differences,
+                      Kahan-compensated per-particle sums, FP64 cutoff
+                      decision for borderline pairs */
+} dm_precision;
+
+/* Force flag bits: identical values to the reference's ForceFlag enum
+ * (Force.h:75-91). */
+#define DM_CONFINEMENT_FORCE       1LL
+#define DM_DRAG_FORCE              2LL
+#define DM_SHIELDED_COULOMB_FORCE  4LL
+#define DM_THERMAL_FORCE           16LL
+#define DM_RECT_CONFINEMENT_FORCE  8192LL
+
+/* Parameters of the in-scope forces; one struct replaces the constructor
+ * arguments of ConfinementForce (ConfinementForce.h:15-16),
+ * RectConfinementForce (RectConfinementForce.h:18-19), DragForce
+ * (DragForce.h:16-17), ShieldedCoulombForce (ShieldedCoulombForce.h:17) and
+ * ThermalForce (ThermalForce.h:16). */
+typedef struct dm_force_params {
+    long long flags;        /* ForceFlag bitmask of enabled forces */
+    double shielding;       /* kappa [1/m]; pairs count only while kappa*r < 10 */
+    double confine;         /* ConfinementForce: F = q*confine*(x, y) */
+    double confine_x;       /* RectConfinementForce: Fx = q*confine_x*x */
+    double confine_y;       /*                       Fy = q*confine_y*y */
+    double gamma;           /* DragForce: F = -gamma*m*v */
+    double heat;            /* ThermalForce: heatVal [N] (mode 0) or sigma [N] (mode 1) */
+    int thermal_mode;       /* 0: heat*U(0,1)*(cos t, sin t), t~U(0,2pi) (ThermalForce.cpp:118-122)
+                               1: Gaussian N(0, heat^2) per axis */
+    int reserved;           /* must be 0 */
+    uint64_t seed;          /* thermal RNG key (Philox4x32-10, counter = particle, step, stage) */
+} dm_force_params;
+
+typedef struct dm_ctx dm_ctx;
+typedef struct dm_cloud dm_cloud;
+typedef struct dm_batch dm_batch;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* ABI version of the loaded library (DM_ABI_VERSION). */
+int dm_version(void);
+
+/* Creates a context on CUDA device `device` with its own stream.
+ * No reference counterpart (the reference is host-only). */
+int dm_ctx_create(int device, dm_ctx **out);
+int dm_ctx_destroy(dm_ctx *ctx);
+
+/* Use an existing cudaStream_t (passed as void*) for all later work; NULL
+ * restores the context's own stream. */
+int dm_ctx_set_stream(dm_ctx *ctx, void *cuda_stream);
+
+/* Blocks until all work queued on the context's stream has finished and
+ * reports any asynchronous error (including device-side numeric flags). */
+int dm_ctx_synchronize(dm_ctx *ctx);
+
+/* Copies the last error message of `ctx` (or of the last failed
+ * dm_ctx_create if ctx is NULL) into buf. */
+int dm_last_error(const dm_ctx *ctx, char *buf, size_t len);
+
+/* Kernel-duration accounting: when enabled, every pair-force kernel launch
+ * is bracketed by CUDA events on the context's stream (CUDA graphs are not
+ * used while enabled).  dm_ctx_profile_read synchronizes and returns the
+ * summed duration [ms], the launch count and the ordered pairs those
+ * launches covered, then resets the counters. */
+int dm_ctx_profile_enable(dm_ctx *ctx, int enable);
+int dm_ctx_profile_read(dm_ctx *ctx, double *total_ms, long long *launches, double *pairs);
+
+/* Measures this GPU's FP32 FMA (kind 0) or FP64 FMA (kind 1) throughput
+ * [TFLOP/s] with a dependent-chain-free FMA loop; used as the roofline peak. */
+int dm_probe_peak(dm_ctx *ctx, int kind, double *tflops);
+
+/* ---- one cloud -------------------------------------------------------- */
+
+/* Creates a device-resident cloud of n particles from host arrays (copied).
+ * Replaces `new Cloud(n)` + filling its arrays (Cloud.cpp:23-37); the
+ * device owns its buffers for the life of the cloud.  n >= 1 (the reference
+ * requires even n, ShieldedCoulombForce.cpp:15-19; this library does not). */
+int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y,
+                    const double *vx, const double *vy, const double *q,
+                    const double *m, dm_cloud **out);
+int dm_cloud_destroy(dm_cloud *cloud);
+int dm_cloud_size(const dm_cloud *cloud, int *n);
+
+/* Host -> device state (positions, velocities); charges/masses unchanged.
+ * Replaces writing Cloud::x/y/Vx/Vy directly (Cloud.h:22). */
+int dm_cloud_upload(dm_cloud *cloud, const double *x, const double *y,
+                    const double *vx, const double *vy);
+
+/* Device -> host state.  The reference's driver reads Cloud::x.. before
+ * Cloud::writeTimeStep (driver.cpp:448-449, Cloud.cpp:258-271). */
+int dm_cloud_download(dm_cloud *cloud, double *x, double *y, double *vx,
+                      double *vy);
+
+/* Replaces per-particle charges and masses (Cloud::charge, Cloud::mass). */
+int dm_cloud_set_charge_mass(dm_cloud *cloud, const double *q, const double *m);
+
+/* Selects the forces and their parameters.  Replaces constructing the
+ * ForceArray (driver.cpp:372-402, Force.h:71). */
+int dm_cloud_set_forces(dm_cloud *cloud, const dm_force_params *params);
+
+/* One force evaluation of every enabled force at the current state, i.e.
+ * the sum of Force::force1 over the ForceArray (Runge_Kutta2.cpp:90-93,
+ * Force.h:28-49) written to host fx, fy (not accumulated).  `thermal_step`
+ * is the RNG step index used for ThermalForce. */
+int dm_cloud_eval_forces(dm_cloud *cloud, int precision, double *fx, double *fy);
+
+/* Same, writing to device arrays of n doubles. */
+int dm_cloud_eval_forces_device(dm_cloud *cloud, int precision, double *d_fx,
+                                double *d_fy);
+
+/* Advances nsteps RK4 steps of fixed dt: Runge_Kutta4::moveParticles
+ * (Runge_Kutta4.cpp:23-137) with CacheOperator (CacheOperator.cpp:18-73)
+ * for an explicit step count, without the adaptive dt of line 25.
+ * *t_inout (may be NULL) is advanced by dt per step with the reference's
+ * accumulation (currentTime += dt). */
+int dm_cloud_step(dm_cloud *cloud, int nsteps, double dt, int precision,
+                  double *t_inout);
+
+/* Runge_Kutta4::moveParticles(endTime) (Runge_Kutta4.cpp:23-137): steps
+ * while *t_inout < end_time.  adaptive = 0 uses dt throughout; adaptive = 1
+ * reproduces Integrator::modifyTimeStep (Integrator.cpp:68-134), reducing
+ * dt by 10x per 10x reduction of the 1e-4 m test distance.  Returns the
+ * steps taken in *steps (may be NULL). */
+int dm_cloud_move_particles(dm_cloud *cloud, double end_time, double dt,
+                            int precision, int adaptive, double *t_inout,
+                            int *steps);
+
+/* The adaptive-dt test alone: the minimum FP32 separation over the pairs
+ * Integrator::modifyTimeStep checks (Integrator.cpp:90-131) and the dt it
+ * would return for init_dt.  Requires n % 4 == 0. */
+int dm_cloud_modify_timestep(dm_cloud *cloud, double init_dt, float *min_dist,
+                             double *dt_out);
+
+/* FP64 diagnostics at the current state: out[0] kinetic energy, out[1]
+ * Yukawa potential energy (pairs with kappa*r < 10), out[2] confinement
+ * potential energy, out[3..4] momentum.  No reference counterpart. */
+int dm_cloud_diagnostics(dm_cloud *cloud, double out[5]);
+
+/* RNG step counter used by ThermalForce (advanced by one per RK4 step). */
+int dm_cloud_set_step_counter(dm_cloud *cloud, uint64_t step);
+int dm_cloud_get_step_counter(dm_cloud *cloud, uint64_t *step);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DEMON_GB300_H */

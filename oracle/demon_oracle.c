@@ -1,0 +1,498 @@
+/*
+ * demon_oracle.c -- CPU oracle (test infrastructure only; see demon_oracle.h).
+ *
+ * Plain-C restatement of the reference's hot path.  Every function cites the
+ * reference file:line it follows.  Build with -ffp-contract=off so no
+ * multiply-add is fused: the reference is compiled for SSE4.2, which has no
+ * FMA, and on aarch64 GCC would otherwise contract a*b+c.
+ */
+#include "demon_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* Cloud::epsilon0 (Cloud.cpp:16) and ShieldedCoulombForce::coulomb
+ * (ShieldedCoulombForce.cpp:21). */
+static const double kEpsilon0 = 8.8541878E-12;
+
+double or_coulomb(void) { return 1.0 / (4.0 * M_PI * kEpsilon0); }
+
+/* ---------------------------------------------------------------------------
+ * Shielded Coulomb (Yukawa) pair force.
+ * ------------------------------------------------------------------------- */
+
+/* Block form used for every pair outside the (i, i+1) 2-block
+ * (ShieldedCoulombForce.cpp:172-198 and 211-237):
+ *   r = sqrt(dx*dx + dy*dy); a = r*kappa; if a < 10:
+ *   f = C*qq*(1+a)*exp(-a)/(r*r*r), F = f*(dx, dy).
+ * Returns 1 and the force on the i side if the pair is inside the cutoff. */
+static inline int pair_block(double dx, double dy, double qq, double kappa,
+                             double coulomb, double *fxo, double *fyo) {
+    const double r = sqrt(dx * dx + dy * dy);
+    const double a = r * kappa;
+    if (!(a < 10.0)) return 0;
+    const double f = coulomb * qq * (1.0 + a) * exp(-a) / (r * r * r);
+    *fxo = f * dx;
+    *fyo = f * dy;
+    return 1;
+}
+
+/* Intra-block form for the pair (i, i+1) (ShieldedCoulombForce.cpp:138-159):
+ *   f = C*qq*(1+a)/(r*r*r*exp(a)). */
+static inline int pair_intra(double dx, double dy, double qq, double kappa,
+                             double coulomb, double *fxo, double *fyo) {
+    const double r = sqrt(dx * dx + dy * dy);
+    const double a = r * kappa;
+    if (!(a < 10.0)) return 0;
+    const double f = coulomb * qq * (1.0 + a) / (r * r * r * exp(a));
+    *fxo = f * dx;
+    *fyo = f * dy;
+    return 1;
+}
+
+/* One call of the 2-lane block routines for i-block ib and j-block jb:
+ * force(i, j) then forcer(i, j) (ShieldedCoulombForce.cpp:54-55), with each
+ * element's += / -= in the reference's order. */
+static inline void block_pair_serial(int ib, int jb, const double *x,
+                                     const double *y, const double *q,
+                                     double kappa, double C, double *fx,
+                                     double *fy) {
+    double ax, ay, bx, by;
+    int ha, hb;
+    /* force(i, j): lane0 = (ib, jb), lane1 = (ib+1, jb+1); F_i += ; F_j -= */
+    ha = pair_block(x[ib] - x[jb], y[ib] - y[jb], q[ib] * q[jb], kappa, C, &ax, &ay);
+    hb = pair_block(x[ib + 1] - x[jb + 1], y[ib + 1] - y[jb + 1], q[ib + 1] * q[jb + 1],
+                    kappa, C, &bx, &by);
+    if (ha || hb) {
+        if (ha) { fx[ib] += ax; fy[ib] += ay; }
+        if (hb) { fx[ib + 1] += bx; fy[ib + 1] += by; }
+        if (ha) { fx[jb] -= ax; fy[jb] -= ay; }
+        if (hb) { fx[jb + 1] -= bx; fy[jb + 1] -= by; }
+    }
+    /* forcer(i, j): lane0 = (ib, jb+1), lane1 = (ib+1, jb);
+     * minusEqualr_pd subtracts lane0 from F_{j+1} and lane1 from F_j
+     * (ShieldedCoulombForce.cpp:294-300). */
+    ha = pair_block(x[ib] - x[jb + 1], y[ib] - y[jb + 1], q[ib] * q[jb + 1], kappa, C, &ax, &ay);
+    hb = pair_block(x[ib + 1] - x[jb], y[ib + 1] - y[jb], q[ib + 1] * q[jb], kappa, C, &bx, &by);
+    if (ha || hb) {
+        if (ha) { fx[ib] += ax; fy[ib] += ay; }
+        if (hb) { fx[ib + 1] += bx; fy[ib + 1] += by; }
+        if (hb) { fx[jb] -= bx; fy[jb] -= by; }
+        if (ha) { fx[jb + 1] -= ax; fy[jb + 1] -= ay; }
+    }
+}
+
+void or_shielded_coulomb(int n, const double *x, const double *y,
+                         const double *q, double kappa, double *fx,
+                         double *fy) {
+    const double C = or_coulomb();
+    const int ne = n & ~1; /* the reference requires even n */
+    /* ShieldedCoulombForce.cpp:43: for (i = 0; i < n-1; i += 2) */
+    for (int ib = 0; ib + 1 < ne; ib += 2) {
+        double ax, ay;
+        /* force(i, q_i*q_{i+1}, hsub(x, y)) (ShieldedCoulombForce.cpp:51) */
+        if (pair_intra(x[ib] - x[ib + 1], y[ib] - y[ib + 1], q[ib] * q[ib + 1], kappa,
+                       C, &ax, &ay)) {
+            fx[ib] += ax; fy[ib] += ay;
+            fx[ib + 1] += -ax; fy[ib + 1] += -ay;
+        }
+        /* ShieldedCoulombForce.cpp:52-56 */
+        for (int jb = ib + 2; jb < ne; jb += 2)
+            block_pair_serial(ib, jb, x, y, q, kappa, C, fx, fy);
+    }
+    if (n & 1) {
+        /* odd tail (outside the reference's domain): same block formula */
+        const int k = n - 1;
+        for (int i = 0; i < k; i++) {
+            double ax, ay;
+            if (pair_block(x[i] - x[k], y[i] - y[k], q[i] * q[k], kappa, C, &ax, &ay)) {
+                fx[i] += ax; fy[i] += ay;
+                fx[k] -= ax; fy[k] -= ay;
+            }
+        }
+    }
+}
+
+void or_shielded_coulomb_omp(int n, const double *x, const double *y,
+                             const double *q, double kappa, double *fx,
+                             double *fy, int nthreads) {
+#ifdef _OPENMP
+    const double C = or_coulomb();
+    const int ne = n & ~1;
+    const int nblocks = ne / 2;
+    omp_lock_t *locks = (omp_lock_t *)malloc(sizeof(omp_lock_t) * (size_t)(nblocks > 0 ? nblocks : 1));
+    for (int b = 0; b < nblocks; b++) omp_init_lock(&locks[b]);
+    if (nthreads <= 0) nthreads = omp_get_num_procs();
+    /* ShieldedCoulombForce.cpp:43-57: OpenMP dynamic over i blocks, one lock
+     * per 2-particle block taken around each += and -= (lines 154-157,
+     * 188-197, 227-236). */
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+    for (int ib = 0; ib < ne - 1; ib += 2) {
+        double ax, ay, bx, by;
+        int ha, hb;
+        if (pair_intra(x[ib] - x[ib + 1], y[ib] - y[ib + 1], q[ib] * q[ib + 1], kappa, C,
+                       &ax, &ay)) {
+            omp_set_lock(&locks[ib / 2]);
+            fx[ib] += ax; fy[ib] += ay;
+            fx[ib + 1] += -ax; fy[ib + 1] += -ay;
+            omp_unset_lock(&locks[ib / 2]);
+        }
+        for (int jb = ib + 2; jb < ne; jb += 2) {
+            ha = pair_block(x[ib] - x[jb], y[ib] - y[jb], q[ib] * q[jb], kappa, C, &ax, &ay);
+            hb = pair_block(x[ib + 1] - x[jb + 1], y[ib + 1] - y[jb + 1],
+                            q[ib + 1] * q[jb + 1], kappa, C, &bx, &by);
+            if (ha || hb) {
+                omp_set_lock(&locks[ib / 2]);
+                if (ha) { fx[ib] += ax; fy[ib] += ay; }
+                if (hb) { fx[ib + 1] += bx; fy[ib + 1] += by; }
+                omp_unset_lock(&locks[ib / 2]);
+                omp_set_lock(&locks[jb / 2]);
+                if (ha) { fx[jb] -= ax; fy[jb] -= ay; }
+                if (hb) { fx[jb + 1] -= bx; fy[jb + 1] -= by; }
+                omp_unset_lock(&locks[jb / 2]);
+            }
+            ha = pair_block(x[ib] - x[jb + 1], y[ib] - y[jb + 1], q[ib] * q[jb + 1], kappa, C,
+                            &ax, &ay);
+            hb = pair_block(x[ib + 1] - x[jb], y[ib + 1] - y[jb], q[ib + 1] * q[jb], kappa, C,
+                            &bx, &by);
+            if (ha || hb) {
+                omp_set_lock(&locks[ib / 2]);
+                if (ha) { fx[ib] += ax; fy[ib] += ay; }
+                if (hb) { fx[ib + 1] += bx; fy[ib + 1] += by; }
+                omp_unset_lock(&locks[ib / 2]);
+                omp_set_lock(&locks[jb / 2]);
+                if (hb) { fx[jb] -= bx; fy[jb] -= by; }
+                if (ha) { fx[jb + 1] -= ax; fy[jb + 1] -= ay; }
+                omp_unset_lock(&locks[jb / 2]);
+            }
+        }
+    }
+    for (int b = 0; b < nblocks; b++) omp_destroy_lock(&locks[b]);
+    free(locks);
+    if (n & 1) {
+        const int k = n - 1;
+        for (int i = 0; i < k; i++) {
+            double ax, ay;
+            if (pair_block(x[i] - x[k], y[i] - y[k], q[i] * q[k], kappa, C, &ax, &ay)) {
+                fx[i] += ax; fy[i] += ay;
+                fx[k] -= ax; fy[k] -= ay;
+            }
+        }
+    }
+#else
+    (void)nthreads;
+    or_shielded_coulomb(n, x, y, q, kappa, fx, fy);
+#endif
+}
+
+/* ---------------------------------------------------------------------------
+ * Counter-based thermal kick.
+ * ------------------------------------------------------------------------- */
+
+/* Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2,
+ * 3", SC'11): 10 rounds of two 32x32->64 multiplies with the published
+ * multipliers and Weyl key increments. */
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; r++) {
+        const uint64_t p0 = (uint64_t)M0 * c0;
+        const uint64_t p1 = (uint64_t)M1 * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += W0;
+        k1 += W1;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* 53-bit uniform strictly inside (0, 1) from two 32-bit words. */
+static inline double u53(uint32_t a, uint32_t b) {
+    const uint64_t v = ((uint64_t)a << 21) ^ ((uint64_t)b >> 11);
+    return ((double)v + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
+                    double *tx, double *ty) {
+    const uint32_t ctr[4] = {i, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)stage};
+    const uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
+    uint32_t o[4];
+    or_philox4x32_10(ctr, key, o);
+    const double u1 = u53(o[0], o[1]);
+    const double u2 = u53(o[2], o[3]);
+    const double th = u2 * (2.0 * M_PI);
+    if (p->thermal_mode == 0) {
+        /* ThermalForce::force (ThermalForce.cpp:118-122): heatVal*U*(cos, sin) */
+        const double a = u1 * p->heat;
+        *tx = a * cos(th);
+        *ty = a * sin(th);
+    } else {
+        /* Gaussian kick, sigma = heat per axis (Box-Muller) */
+        const double rad = sqrt(-2.0 * log(u1));
+        *tx = p->heat * (rad * cos(th));
+        *ty = p->heat * (rad * sin(th));
+    }
+}
+
+/* ---------------------------------------------------------------------------
+ * All forces of one RK stage.
+ * ------------------------------------------------------------------------- */
+
+void or_forces(int n, const double *xs, const double *ys, const double *vxs,
+               const double *vys, const double *q, const double *m,
+               const or_params *p, uint64_t step, int stage, double *fx,
+               double *fy, int nthreads) {
+    for (int i = 0; i < n; i++) { fx[i] = 0.0; fy[i] = 0.0; }
+    /* driver.cpp:372-402 push order: Confinement, Drag, RectConfinement,
+     * ShieldedCoulomb, Thermal. */
+    if (p->flags & OR_CONFINEMENT_FORCE) {
+        /* ConfinementForce::force (ConfinementForce.cpp:48-54) */
+        for (int i = 0; i < n; i++) {
+            const double c = q[i] * p->confine;
+            fx[i] += c * xs[i];
+            fy[i] += c * ys[i];
+        }
+    }
+    if (p->flags & OR_DRAG_FORCE) {
+        /* DragForce::force (DragForce.cpp:49-55), dragConst = -gamma (DragForce.h:16-17) */
+        const double dragConst = -p->gamma;
+        for (int i = 0; i < n; i++) {
+            const double d = m[i] * dragConst;
+            fx[i] += d * vxs[i];
+            fy[i] += d * vys[i];
+        }
+    }
+    if (p->flags & OR_RECT_CONFINEMENT_FORCE) {
+        /* RectConfinementForce::force (RectConfinementForce.cpp:50-59) */
+        for (int i = 0; i < n; i++) {
+            fx[i] += (q[i] * p->confine_x) * xs[i];
+            fy[i] += (q[i] * p->confine_y) * ys[i];
+        }
+    }
+    if (p->flags & OR_SHIELDED_COULOMB_FORCE) {
+        if (nthreads == 1)
+            or_shielded_coulomb(n, xs, ys, q, p->shielding, fx, fy);
+        else
+            or_shielded_coulomb_omp(n, xs, ys, q, p->shielding, fx, fy, nthreads);
+    }
+    if (p->flags & OR_THERMAL_FORCE) {
+        for (int i = 0; i < n; i++) {
+            double tx, ty;
+            or_thermal_one(p, (uint32_t)i, step, stage, &tx, &ty);
+            fx[i] += tx;
+            fy[i] += ty;
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------------
+ * RK4.
+ * ------------------------------------------------------------------------- */
+
+/* Runge_Kutta4::da (Runge_Kutta4.cpp:147-151): (a1 + (2*(a2+a3) + a4)) / 6 */
+static inline double rk_da(double a1, double a2, double a3, double a4) {
+    return (a1 + ((a2 + a3) * 2.0 + a4)) / 6.0;
+}
+
+typedef struct rk_work {
+    double *k[4], *l[4], *mm[4], *nn[4];
+    double *xc, *yc, *vxc, *vyc, *fx, *fy;
+    double *block;
+} rk_work;
+
+static int rk_work_alloc(rk_work *w, int n) {
+    const size_t sz = (size_t)(n > 0 ? n : 1);
+    w->block = (double *)calloc(sz * 22, sizeof(double));
+    if (!w->block) return -1;
+    double *b = w->block;
+    for (int s = 0; s < 4; s++) {
+        w->k[s] = b; b += sz;
+        w->l[s] = b; b += sz;
+        w->mm[s] = b; b += sz;
+        w->nn[s] = b; b += sz;
+    }
+    w->xc = b; b += sz;
+    w->yc = b; b += sz;
+    w->vxc = b; b += sz;
+    w->vyc = b; b += sz;
+    w->fx = b; b += sz;
+    w->fy = b;
+    return 0;
+}
+
+/* One RK4 step with a given dt (Runge_Kutta4.cpp:26-135 after line 25). */
+static void rk4_one_step(int n, double *x, double *y, double *vx, double *vy,
+                         const double *q, const double *m, const or_params *p,
+                         double dt, uint64_t step, int nthreads, rk_work *w) {
+    for (int s = 0; s < 4; s++) {
+        const double *xs, *ys, *vxs, *vys;
+        if (s == 0) {
+            /* operation1 is a no-op (CacheOperator.cpp:18-20): stage 1 reads x, Vx */
+            xs = x; ys = y; vxs = vx; vys = vy;
+        } else {
+            /* operation2/3: cache = 0.5*tidbit + base (CacheOperator.cpp:28-56,
+             * fmadd_pd is mul then add under SSE4.2, VectorCompatibility.h:99-105);
+             * operation4: cache = base + tidbit (CacheOperator.cpp:64-73) */
+            const double *kp = w->k[s - 1], *lp = w->l[s - 1];
+            const double *mp = w->mm[s - 1], *np = w->nn[s - 1];
+            for (int i = 0; i < n; i++) {
+                if (s < 3) {
+                    w->xc[i] = 0.5 * lp[i] + x[i];
+                    w->yc[i] = 0.5 * np[i] + y[i];
+                    w->vxc[i] = 0.5 * kp[i] + vx[i];
+                    w->vyc[i] = 0.5 * mp[i] + vy[i];
+                } else {
+                    w->xc[i] = x[i] + lp[i];
+                    w->yc[i] = y[i] + np[i];
+                    w->vxc[i] = vx[i] + kp[i];
+                    w->vyc[i] = vy[i] + mp[i];
+                }
+            }
+            xs = w->xc; ys = w->yc; vxs = w->vxc; vys = w->vyc;
+        }
+        or_forces(n, xs, ys, vxs, vys, q, m, p, step, s + 1, w->fx, w->fy, nthreads);
+        /* stage kernels (Runge_Kutta4.cpp:32-47 etc.):
+         * k = (dt*Fx)/m, l = dt*Vx_stage, m = (dt*Fy)/m, n = dt*Vy_stage */
+        for (int i = 0; i < n; i++) {
+            w->k[s][i] = (dt * w->fx[i]) / m[i];
+            w->l[s][i] = dt * vxs[i];
+            w->mm[s][i] = (dt * w->fy[i]) / m[i];
+            w->nn[s][i] = dt * vys[i];
+        }
+    }
+    /* Runge_Kutta4.cpp:107-133 */
+    for (int i = 0; i < n; i++) {
+        vx[i] += rk_da(w->k[0][i], w->k[1][i], w->k[2][i], w->k[3][i]);
+        x[i] += rk_da(w->l[0][i], w->l[1][i], w->l[2][i], w->l[3][i]);
+        vy[i] += rk_da(w->mm[0][i], w->mm[1][i], w->mm[2][i], w->mm[3][i]);
+        y[i] += rk_da(w->nn[0][i], w->nn[1][i], w->nn[2][i], w->nn[3][i]);
+    }
+}
+
+void or_rk4_fixed(int n, double *x, double *y, double *vx, double *vy,
+                  const double *q, const double *m, const or_params *p,
+                  double dt, int nsteps, uint64_t step0, int nthreads) {
+    rk_work w;
+    if (rk_work_alloc(&w, n)) return;
+    for (int s = 0; s < nsteps; s++)
+        rk4_one_step(n, x, y, vx, vy, q, m, p, dt, step0 + (uint64_t)s, nthreads, &w);
+    free(w.block);
+}
+
+/* ---------------------------------------------------------------------------
+ * Adaptive time step.
+ * ------------------------------------------------------------------------- */
+
+static inline float sep_r2(float ax, float ay, float bx, float by) {
+    const float sx = ax - bx, sy = ay - by;
+    return sx * sx + sy * sy;
+}
+
+/* Integrator::modifyTimeStep (Integrator.cpp:90-131).  loadFloatVector
+ * (Integrator.cpp:162-169) puts x[o+3-L] in lane L; the two hsub tests
+ * (lines 96-104) cover all 6 pairs inside a 4-block; between 4-blocks the
+ * shuffles (lines 112-129; _MM_SHUFFLE(3,2,1,0) is the identity) pair outer
+ * element k with inner element (k - d) mod 4 for d = 0, 1, 2 only. */
+float or_checked_min_dist(int n, const double *x, const double *y) {
+    float best = INFINITY;
+    for (int o = 0; o + 3 < n; o += 4) {
+        float ox[4], oy[4];
+        for (int k = 0; k < 4; k++) { ox[k] = (float)x[o + k]; oy[k] = (float)y[o + k]; }
+        static const int intra[6][2] = {{0, 1}, {2, 3}, {0, 3}, {1, 2}, {1, 3}, {0, 2}};
+        for (int t = 0; t < 6; t++) {
+            const float r2 = sep_r2(ox[intra[t][0]], oy[intra[t][0]], ox[intra[t][1]], oy[intra[t][1]]);
+            if (r2 < best) best = r2;
+        }
+        for (int in = o + 4; in + 3 < n; in += 4) {
+            float ix[4], iy[4];
+            for (int k = 0; k < 4; k++) { ix[k] = (float)x[in + k]; iy[k] = (float)y[in + k]; }
+            for (int k = 0; k < 4; k++)
+                for (int d = 0; d < 3; d++) {
+                    const int mi = (k - d + 4) & 3;
+                    const float r2 = sep_r2(ox[k], oy[k], ix[mi], iy[mi]);
+                    if (r2 < best) best = r2;
+                }
+        }
+    }
+    return sqrtf(best);
+}
+
+double or_modify_timestep(int n, const double *x, const double *y, float dist,
+                          double dt) {
+    const float dmin = or_checked_min_dist(n, x, y);
+    if (!(dmin > 0.0f)) return -1.0;
+    /* tryToReduceTimeStep (Integrator.cpp:144-155): while within distance,
+     * distance /= 10.0f, time /= 10.0f (a double divided by 10.0). */
+    while (dmin <= dist) {
+        dist /= 10.0f;
+        dt /= 10.0f;
+    }
+    return dt;
+}
+
+int or_rk4_move_particles(int n, double *x, double *y, double *vx, double *vy,
+                          const double *q, const double *m, const or_params *p,
+                          double init_dt, double *t_inout, double end_time,
+                          uint64_t step0, int nthreads) {
+    rk_work w;
+    if (rk_work_alloc(&w, n)) return -1;
+    int steps = 0;
+    double t = *t_inout;
+    /* Runge_Kutta4::moveParticles (Runge_Kutta4.cpp:24-136) */
+    while (t < end_time) {
+        const double dt = or_modify_timestep(n, x, y, 1.0e-4f, init_dt);
+        if (dt < 0.0) break;
+        rk4_one_step(n, x, y, vx, vy, q, m, p, dt, step0 + (uint64_t)steps, nthreads, &w);
+        t += dt;
+        steps++;
+    }
+    *t_inout = t;
+    free(w.block);
+    return steps;
+}
+
+/* ---------------------------------------------------------------------------
+ * Diagnostics (no reference counterpart; FP64 definitions of the energies
+ * whose forces the reference integrates).
+ * ------------------------------------------------------------------------- */
+
+void or_diagnostics(int n, const double *x, const double *y, const double *vx,
+                    const double *vy, const double *q, const double *m,
+                    const or_params *p, double out[5]) {
+    const double C = or_coulomb();
+    double ke = 0.0, pe = 0.0, pc = 0.0, px = 0.0, py = 0.0;
+    for (int i = 0; i < n; i++) {
+        ke += 0.5 * m[i] * (vx[i] * vx[i] + vy[i] * vy[i]);
+        px += m[i] * vx[i];
+        py += m[i] * vy[i];
+        /* F = q*k*x  =>  U = -q*k*x^2/2 */
+        if (p->flags & OR_CONFINEMENT_FORCE)
+            pc += -0.5 * q[i] * p->confine * (x[i] * x[i] + y[i] * y[i]);
+        if (p->flags & OR_RECT_CONFINEMENT_FORCE)
+            pc += -0.5 * q[i] * (p->confine_x * x[i] * x[i] + p->confine_y * y[i] * y[i]);
+    }
+    if (p->flags & OR_SHIELDED_COULOMB_FORCE) {
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) {
+                const double dx = x[i] - x[j], dy = y[i] - y[j];
+                const double r = sqrt(dx * dx + dy * dy);
+                const double a = r * p->shielding;
+                if (a < 10.0) pe += C * q[i] * q[j] * exp(-a) / r;
+            }
+    }
+    out[0] = ke; out[1] = pe; out[2] = pc; out[3] = px; out[4] = py;
+}

@@ -1,0 +1,58 @@
+"""The C-ABI library: builds, loads, exports every declared symbol (no GPU)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from demon_simulation_code_gb300 import _lib, workloads as W
+from demon_simulation_code_gb300.build import ROOT, build
+
+HEADER = os.path.join(ROOT, "include", "demon_gb300.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*int\s+(dm_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    path = build()
+    lib = _lib.load(path)
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+        assert s in _lib.SIGNATURES, s
+    assert lib.dm_version() == 1
+
+
+def test_create_error_is_reported_without_gpu():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    from demon_simulation_code_gb300 import Context, DemonError
+
+    with pytest.raises(DemonError):
+        Context(0)
+
+
+def test_force_params_layout_matches_oracle():
+    import ctypes
+
+    import oracle
+
+    assert ctypes.sizeof(_lib.ForceParams) == ctypes.sizeof(oracle.Params) == 72
+    assert [f[0] for f in _lib.ForceParams._fields_] == [f[0] for f in oracle.Params._fields_]
+
+
+def test_workloads_are_seeded():
+    a = W.disk16k().clouds[0]
+    b = W.disk16k().clouds[0]
+    assert np.array_equal(a.x, b.x) and a.n == 16384
+    assert np.all(np.hypot(a.x, a.y) <= 2e-2)
+    w = W.batch256()
+    ns = [c.n for c in w.clouds]
+    assert len(ns) == 256 and min(ns) >= 64 and max(ns) <= 4096
+    assert W.disk512().pairs_per_eval == 512 * 511

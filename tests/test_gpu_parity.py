@@ -1,0 +1,251 @@
+"""CUDA path vs the oracle and the reference's golden fixtures (needs a GB300).
+
+Tolerances (force error e_F = ||F_gpu - F_ref||_2 / ||F_ref||_2 over the 2N
+vector, as the parity target states them): FP64 <= 1e-12, FP32C <= 1e-6.
+The cutoff decision itself must agree exactly, which the per-particle check
+(|dF_i| / sum_j |F_ij|) would expose: a flipped pair changes one particle's
+force by a finite fraction.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from demon_simulation_code_gb300 import DeviceCloud, workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL = {"fp64": 1e-12, "fp32c": 1e-6}
+
+
+def golden(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def e_F(fx, fy, rx, ry):
+    return np.sqrt(np.sum((fx - rx) ** 2 + (fy - ry) ** 2) / np.sum(rx**2 + ry**2))
+
+
+def abs_pair_sum(x, y, q, kappa, C):
+    """sum_j |F_ij| per particle (normaliser robust to cancellation)."""
+    dx = x[:, None] - x[None, :]
+    dy = y[:, None] - y[None, :]
+    r = np.sqrt(dx * dx + dy * dy)
+    np.fill_diagonal(r, np.inf)
+    a = r * kappa
+    f = np.where(a < 10.0, np.abs(C * q[:, None] * q[None, :]) * (1 + a) * np.exp(-a) / r**2, 0.0)
+    return f.sum(axis=1)
+
+
+def coulomb_cloud(ctx, x, y, q, kappa):
+    n = len(x)
+    return DeviceCloud(ctx, x, y, np.zeros(n), np.zeros(n), q, np.full(n, W.M_DUST),
+                       dict(flags=W.SHIELDED_COULOMB, shielding=kappa))
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+@pytest.mark.parametrize("name", ["pair_n2", "pair_n4", "pair_n64_dense", "pair_n256_k1e2",
+                                  "pair_disk512"])
+def test_pair_force_vs_reference_golden(gpu_ctx, oracle_lib, name, prec):
+    g = golden(name)
+    kappa = float(g["kappa"])
+    c = coulomb_cloud(gpu_ctx, g["x"], g["y"], g["q"], kappa)
+    fx, fy = c.eval_forces(prec)
+    err = e_F(fx, fy, g["fx"], g["fy"])
+    assert err <= TOL[prec], err
+    s = abs_pair_sum(g["x"], g["y"], g["q"], kappa, oracle_lib.coulomb())
+    worst = np.max(np.hypot(fx - g["fx"], fy - g["fy"]) / np.maximum(s, 1e-300))
+    assert worst <= 10 * TOL[prec], worst
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 63, 64, 65, 511, 513, 1000, 2049])
+def test_pair_force_ragged_sizes(gpu_ctx, oracle_lib, n, prec):
+    rng = np.random.default_rng(n)
+    R = 3e-4 * np.sqrt(max(n, 1))
+    x, y = W.uniform_disk(rng, n, R)
+    q = rng.normal(W.Q_DUST, 5e-17, n)
+    c = coulomb_cloud(gpu_ctx, x, y, q, 2e4)
+    fx, fy = c.eval_forces(prec)
+    rx, ry = oracle_lib.shielded_coulomb(x, y, q, 2e4)
+    if n == 1:
+        assert fx[0] == 0.0 and fy[0] == 0.0
+        return
+    assert e_F(fx, fy, rx, ry) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_pair_force_disk16k(gpu_ctx, oracle_lib, prec):
+    c0 = W.disk16k(thermal=False).clouds[0]
+    c = coulomb_cloud(gpu_ctx, c0.x, c0.y, c0.q, 2e4)
+    fx, fy = c.eval_forces(prec)
+    rx, ry = oracle_lib.shielded_coulomb(c0.x, c0.y, c0.q, 2e4, nthreads=8)
+    err = e_F(fx, fy, rx, ry)
+    print(f"disk16k {prec} e_F = {err:.3e}")
+    assert err <= TOL[prec]
+
+
+def test_cutoff_borderline_pairs_decided_like_reference(gpu_ctx, oracle_lib):
+    """Pairs placed within a few ulp of kappa*r = 10 on both sides."""
+    kappa = 2e4
+    rc = 10.0 / kappa
+    n = 64
+    x = np.zeros(n)
+    y = np.zeros(n)
+    for k in range(n // 2):
+        d = rc * (1.0 + (k - n // 4) * 2.0**-50)
+        x[2 * k] = 0.01 * k
+        x[2 * k + 1] = 0.01 * k + d
+        y[2 * k] = y[2 * k + 1] = 1e-3 * k
+    q = np.full(n, W.Q_DUST)
+    rx, ry = oracle_lib.shielded_coulomb(x, y, q, kappa)
+    assert 0 < np.count_nonzero(rx) < n
+    for prec in ("fp64", "fp32c"):
+        c = coulomb_cloud(gpu_ctx, x, y, q, kappa)
+        fx, fy = c.eval_forces(prec)
+        assert np.array_equal(fx != 0.0, rx != 0.0), prec
+        assert e_F(fx, fy, rx, ry) <= TOL[prec]
+
+
+@pytest.mark.parametrize("name", ["forces_conf_drag_coul", "forces_rect_drag_coul"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_all_forces_vs_reference_golden(gpu_ctx, name, prec):
+    g = golden(name)
+    c = DeviceCloud(gpu_ctx, g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"],
+                    dict(flags=int(g["flags"]), shielding=2e4, confine=1e8, confine_x=1e8,
+                         confine_y=2e8, gamma=3.0))
+    fx, fy = c.eval_forces(prec)
+    assert rel(fx, g["fx"]) <= TOL[prec] and rel(fy, g["fy"]) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_rk4_fixed_vs_reference_golden(gpu_ctx, prec):
+    g = golden("rk4_fixed_n64")
+    c = DeviceCloud(gpu_ctx, g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"],
+                    dict(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0))
+    t = c.step(int(g["steps"]), float(g["dt"]), prec, t=0.0)
+    x, y, vx, vy = c.download()
+    tol = 1e-12 if prec == "fp64" else 1e-7
+    for a, k in zip((x, y, vx, vy), ("x1", "y1", "vx1", "vy1")):
+        assert rel(a, g[k]) <= tol, (k, rel(a, g[k]))
+    assert t == pytest.approx(25e-4)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_rk4_disk512_trajectory_vs_oracle(gpu_ctx, oracle_lib, prec):
+    c0 = W.disk512().clouds[0]
+    p = oracle.make_params(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0)
+    ref = oracle_lib.rk4_fixed(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m, p, 1e-4, 100)
+    c = DeviceCloud.from_cloud(gpu_ctx, c0)
+    c.step(100, 1e-4, prec)  # 100 steps: CUDA-graph replays + remainder
+    out = c.download()
+    R = 5e-3
+    errx = np.max(np.hypot(out[0] - ref[0], out[1] - ref[1])) / R
+    assert errx <= (1e-12 if prec == "fp64" else 1e-7), errx
+
+
+def test_graph_and_direct_steps_identical(gpu_ctx):
+    c0 = W.disk512().clouds[0]
+    a = DeviceCloud.from_cloud(gpu_ctx, c0)
+    b = DeviceCloud.from_cloud(gpu_ctx, c0)
+    a.step(40, 1e-4, "fp32c")
+    for _ in range(40):
+        b.step(1, 1e-4, "fp32c")
+    assert all(np.array_equal(u, v) for u, v in zip(a.download(), b.download()))
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_thermal_force_vs_oracle(gpu_ctx, oracle_lib, mode):
+    n = 3000
+    rng = np.random.default_rng(9)
+    x, y = W.uniform_disk(rng, n, 1e-2)
+    params = dict(flags=W.THERMAL, heat=1e-14, thermal_mode=mode, seed=77)
+    c = DeviceCloud(gpu_ctx, x, y, np.zeros(n), np.zeros(n), np.full(n, W.Q_DUST),
+                    np.full(n, W.M_DUST), params)
+    c.set_step_counter(123)
+    fx, fy = c.eval_forces("fp64")
+    tx, ty = oracle_lib.thermal(oracle.make_params(**params), n, 123, 1)
+    assert rel(fx, tx) < 1e-14 and rel(fy, ty) < 1e-14
+
+
+def test_thermal_rk4_fp64_vs_oracle(gpu_ctx, oracle_lib):
+    c0 = W.disk512().clouds[0]
+    params = dict(flags=1 | 2 | 4 | 16, shielding=2e4, confine=1e8, gamma=3.0, heat=1e-14,
+                  thermal_mode=1, seed=1)
+    ref = oracle_lib.rk4_fixed(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m,
+                               oracle.make_params(**params), 1e-4, 20, step0=5)
+    c = DeviceCloud(gpu_ctx, c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m, params)
+    c.set_step_counter(5)
+    c.step(20, 1e-4, "fp64")
+    assert c.get_step_counter() == 25
+    out = c.download()
+    for a, b in zip(out, ref):
+        assert rel(a, b) < 1e-12
+
+
+def test_adaptive_dt_vs_reference_golden(gpu_ctx):
+    g = golden("move_adaptive_disk512")
+    c = DeviceCloud(gpu_ctx, g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"],
+                    dict(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0))
+    t, steps = c.move_particles(float(g["end"]), float(g["dt"]), 0.0, "fp64", adaptive=True)
+    assert steps == int(g["steps"]) and t == float(g["t1"])
+    out = c.download()
+    for a, k in zip(out, ("x1", "y1", "vx1", "vy1")):
+        assert rel(a, g[k]) <= 1e-12, k
+
+
+def test_modify_timestep_vs_oracle(gpu_ctx, oracle_lib):
+    for seed in range(4):
+        c0 = W.disk_cloud(1024, 5e-3 * (seed + 1), seed)
+        c = DeviceCloud.from_cloud(gpu_ctx, c0)
+        dmin, dt = c.modify_timestep(1e-4)
+        assert dmin == np.float32(oracle_lib.checked_min_dist(c0.x, c0.y))
+        assert dt == oracle_lib.modify_timestep(c0.x, c0.y, 1e-4)
+
+
+def test_diagnostics_vs_oracle(gpu_ctx, oracle_lib):
+    c0 = W.disk_cloud(2000, 2e-3, 5)
+    rng = np.random.default_rng(1)
+    c0.vx = rng.normal(0, 1e-3, c0.n)
+    c0.vy = rng.normal(0, 1e-3, c0.n)
+    c = DeviceCloud.from_cloud(gpu_ctx, c0)
+    d = c.diagnostics()
+    r = oracle_lib.diagnostics(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m,
+                               oracle.make_params(**c0.params()))
+    np.testing.assert_allclose(d, r, rtol=1e-11)
+
+
+def test_nonfinite_position_is_reported(gpu_ctx):
+    from demon_simulation_code_gb300 import DemonError
+
+    c0 = W.disk512().clouds[0]
+    c0.x[3] = np.nan
+    c = DeviceCloud.from_cloud(gpu_ctx, c0)
+    c.step(1, 1e-4, "fp32c")
+    with pytest.raises(DemonError):
+        c.download()
+    # the context stays usable
+    ok = DeviceCloud.from_cloud(gpu_ctx, W.disk512().clouds[0])
+    ok.step(1, 1e-4, "fp32c")
+    assert np.all(np.isfinite(ok.download()[0]))
+
+
+def test_bad_arguments_rejected(gpu_ctx):
+    from demon_simulation_code_gb300 import DemonError
+
+    c = DeviceCloud.from_cloud(gpu_ctx, W.disk512().clouds[0])
+    with pytest.raises(DemonError):
+        c.set_forces(dict(flags=4, shielding=-1.0))
+    with pytest.raises(DemonError):
+        c.set_forces(dict(flags=1 << 20))
+    with pytest.raises(DemonError):
+        c.step(-1, 1e-4)
+    odd = DeviceCloud(gpu_ctx, np.zeros(6), np.arange(6.0), np.zeros(6), np.zeros(6),
+                      np.full(6, W.Q_DUST), np.full(6, W.M_DUST))
+    with pytest.raises(DemonError):
+        odd.modify_timestep(1e-4)
