@@ -69,7 +69,7 @@ struct PairTuning {
 // ---------------------------------------------------------------------------
 template <int NT, int ILP, int JT>
 __global__ void __launch_bounds__(NT) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *s_pa = reinterpret_cast<float4 *>(smem_raw);
     float4 *s_pb = s_pa + JT;
     float4 *s_red = s_pb + JT;  // [ILP][NT] (sx, sy, cx, cy)
@@ -199,7 +199,7 @@ struct alignas(32) JD {
 
 template <int NT, int ILP, int JT>
 __global__ void __launch_bounds__(NT) pair_stage_fp64(const StageParams P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     JD *s_j = reinterpret_cast<JD *>(smem_raw);
     double2 *s_red = reinterpret_cast<double2 *>(s_j + JT);  // [ILP][NT]
 
