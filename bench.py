@@ -223,7 +223,9 @@ def run_gb300(args, world, rank, local):
     c0 = w.clouds[0]
     n = c0.n
     pairs_step = 4.0 * n * (n - 1)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream shared by torch events and the library
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = Context(local)
     ctx.set_stream(stream.cuda_stream)
     cloud = DeviceCloud.from_cloud(ctx, c0)
@@ -309,7 +311,7 @@ def run_gb300(args, world, rank, local):
         t = torch.tensor([e2e_el], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_el = float(t.item())
-    e2e_value = pairs_step * args.e2e_steps * world / e2e_el
+    e2e_value = pairs_step * args.e2e_steps * world / e2e_el if args.e2e_steps > 0 else None
 
     # roofline of the dominant kernel (fused pair + stage, FP32 pipe bound)
     peak = ctx.probe_peak("fp32")

@@ -27,8 +27,10 @@ namespace {
 
 std::string g_create_error;
 
-constexpr int kNT32 = 128, kILP32 = 4, kJT32 = 512;
-constexpr int kNT64 = 128, kILP64 = 2, kJT64 = 256;
+// FP32C: 4 j-groups x 128 i-lanes, 4 particles per lane, 1024-particle j tiles
+constexpr int kNI32 = 128, kG32 = 4, kILP32 = 4, kJT32 = 1024;
+// FP64: 2 j-groups x 128 i-lanes, 2 particles per lane, 512-particle j tiles
+constexpr int kNI64 = 128, kG64 = 2, kILP64 = 2, kJT64 = 512;
 constexpr int kGraphSteps = 16;
 
 }  // namespace
@@ -78,6 +80,7 @@ struct dm_cloud {
     double *d_dt = nullptr;
     unsigned int *d_min = nullptr;
     float *d_dmin = nullptr;
+    int split[2] = {0, 0};  // cluster size per precision (0 = not chosen yet)
     std::map<GraphKey, cudaGraphExec_t> graphs;
     cudaStream_t graph_stream = nullptr;  // stream the graphs were built for
 
@@ -151,50 +154,20 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     return P;
 }
 
-// Cluster size (j split) for a cloud: aim for ~4 CTAs per SM.
-int pick_split(int n_pad, int tile, int num_sms) {
-    const int ntiles = (n_pad + tile - 1) / tile;
-    int s = 1;
-    while (s < 16 && ntiles * s < num_sms * 4 && (n_pad / (s * 2)) >= 256) s *= 2;
-    return s;
-}
+struct KernelShape {
+    const void *fn;
+    int nt;      // threads per CTA
+    int tile;    // particles per i tile
+    int groups;  // j groups per CTA
+    size_t smem;
+};
 
-template <typename K>
-int launch_cluster(dm_ctx *ctx, K kernel, int ntiles, int S, int nt, size_t smem,
-                   const StageParams &P) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(ntiles * S, 1, 1);
-    cfg.blockDim = dim3(nt, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = ctx->stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = S;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, kernel, P));
-    return DM_OK;
-}
-
-template <typename K>
-int launch_cluster32(dm_ctx *ctx, K kernel, int ntiles, int S, int nt, size_t smem,
-                     const StageParams &P, const ExpConsts &E) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(ntiles * S, 1, 1);
-    cfg.blockDim = dim3(nt, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = ctx->stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = S;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, kernel, P, E));
-    return DM_OK;
+KernelShape shape_of(int precision) {
+    if (precision == DM_FP32C)
+        return {(const void *)pair_stage_fp32c<kNI32, kG32, kILP32, kJT32>, kNI32 * kG32,
+                kNI32 * kILP32, kG32, Fp32cSmem<kNI32, kG32, kILP32>::bytes(kJT32)};
+    return {(const void *)pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, kNI64 * kG64,
+            kNI64 * kILP64, kG64, Fp64Smem<kNI64, kG64, kILP64>::bytes(kJT64)};
 }
 
 int ensure_kernel_attrs(dm_ctx *ctx) {
@@ -202,11 +175,51 @@ int ensure_kernel_attrs(dm_ctx *ctx) {
     int dev = ctx->device;
     if (dev < 0 || dev >= 64) dev = 0;
     if (done[dev]) return DM_OK;
-    DM_CUDA(ctx, cudaFuncSetAttribute(pair_stage_fp32c<kNT32, kILP32, kJT32>,
-                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    DM_CUDA(ctx, cudaFuncSetAttribute(pair_stage_fp64<kNT64, kILP64, kJT64>,
-                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    for (int prec : {DM_FP64, DM_FP32C}) {
+        const KernelShape k = shape_of(prec);
+        DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
+    }
     done[dev] = true;
+    return DM_OK;
+}
+
+// j split (cluster size S) for a cloud: the S in [1, 16] that minimises the
+// number of co-resident cluster waves per unit of work (waves / S), using the
+// device's own count of co-resident clusters of that size.  Ties go to the
+// smaller S (fewer partial sums).
+int pick_split(dm_ctx *ctx, int precision, int n, int n_pad, int *out) {
+    const KernelShape k = shape_of(precision);
+    const int ntiles = (n + k.tile - 1) / k.tile;
+    int best_s = 1;
+    double best_cost = 1e300;
+    for (int S = 1; S <= 16; S++) {
+        if (S > 1 && n_pad / S < 64 * k.groups) break;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(ntiles * S, 1, 1);
+        cfg.blockDim = dim3(k.nt, 1, 1);
+        cfg.dynamicSmemBytes = k.smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = S;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        cudaError_t e = cudaOccupancyMaxActiveClusters(&nc, k.fn, &cfg);
+        if (e != cudaSuccess || nc <= 0) {
+            cudaGetLastError();
+            continue;
+        }
+        const int waves = (ntiles + nc - 1) / nc;
+        const double cost = (double)waves / S;
+        if (cost < best_cost * 0.98) {
+            best_cost = cost;
+            best_s = S;
+        }
+    }
+    *out = best_s;
     return DM_OK;
 }
 
@@ -215,6 +228,11 @@ int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, con
     dm_ctx *ctx = c->ctx;
     int rc = ensure_kernel_attrs(ctx);
     if (rc) return rc;
+    int &S = c->split[precision == DM_FP32C ? 1 : 0];
+    if (S <= 0) {
+        rc = pick_split(ctx, precision, c->n, c->n_pad, &S);
+        if (rc) return rc;
+    }
     const StageParams P = make_stage_params(c, stage, mode, dt, dt_dev);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ctx->prof) {
@@ -229,21 +247,24 @@ int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, con
         ctx->prof_used++;
         DM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
     }
-    if (precision == DM_FP32C) {
-        const int tile = kNT32 * kILP32;
-        const int S = pick_split(c->n_pad, tile, ctx->num_sms);
-        const int ntiles = (c->n + tile - 1) / tile;
-        const size_t smem = (size_t)kJT32 * 2 * sizeof(float4) + (size_t)kILP32 * kNT32 * sizeof(float4);
-        rc = launch_cluster32(ctx, pair_stage_fp32c<kNT32, kILP32, kJT32>, ntiles, S, kNT32, smem, P,
-                              exp_consts());
-    } else {
-        const int tile = kNT64 * kILP64;
-        const int S = pick_split(c->n_pad, tile, ctx->num_sms);
-        const int ntiles = (c->n + tile - 1) / tile;
-        const size_t smem = (size_t)kJT64 * sizeof(JD) + (size_t)kILP64 * kNT64 * sizeof(double2);
-        rc = launch_cluster(ctx, pair_stage_fp64<kNT64, kILP64, kJT64>, ntiles, S, kNT64, smem, P);
-    }
-    if (rc) return rc;
+    const KernelShape k = shape_of(precision);
+    const int ntiles = (c->n + k.tile - 1) / k.tile;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ntiles * S, 1, 1);
+    cfg.blockDim = dim3(k.nt, 1, 1);
+    cfg.dynamicSmemBytes = k.smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (precision == DM_FP32C)
+        DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, pair_stage_fp32c<kNI32, kG32, kILP32, kJT32>, P, exp_consts()));
+    else
+        DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, P));
     if (ctx->prof) {
         DM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
         ctx->prof_launches++;

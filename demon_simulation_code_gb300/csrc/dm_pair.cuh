@@ -66,19 +66,77 @@ struct PairTuning {
 
 // ---------------------------------------------------------------------------
 // FP32-compensated kernel.
+//
+// CTA = G j-groups x NI i-lanes.  Lane t of every group owns the ILP
+// particles i = tile*NI*ILP + k*NI + t; group g sweeps the g-th quarter
+// (for G = 4) of every shared-memory j tile, so all G groups reuse one tile.
+// Hot registers per particle: -2*xh, -2*yh (packed in pairs for the f32x2
+// FMA) and the filter threshold; everything only the rare precise path
+// needs (lo parts, C*q_i, index, Kahan accumulators) lives in shared memory.
+// Per j the warp takes ONE uniform branch (vote over all its lanes and
+// slots); the precise path runs only when some lane's filter fired.
 // ---------------------------------------------------------------------------
-template <int NT, int ILP, int JT>
-__global__ void __launch_bounds__(NT) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+template <int NI, int G, int ILP>
+struct Fp32cSmem {
+    static constexpr size_t cold = (size_t)ILP * NI * sizeof(float4);
+    static constexpr size_t acc = (size_t)G * ILP * NI * sizeof(float4);
+    static constexpr size_t red = (size_t)ILP * NI * sizeof(double2);
+    static size_t bytes(int jt) { return (size_t)jt * 2 * sizeof(float4) + cold + acc + red; }
+};
+
+template <int NI, int G, int ILP>
+__device__ __forceinline__ void precise_pair(const StageParams &P, const ExpConsts &E, int b,
+                                             float xh_i, float yh_i, const float4 &A,
+                                             const float4 &Bj, int jg, float4 *cold,
+                                             float4 *acc) {
+    const float4 ic = *cold;  // (xl, yl, C*q_i, bits of i)
+    const int ii = __float_as_int(ic.w);
+    if (jg == ii) return;
+    const float dx = (xh_i - A.x) + (ic.x - Bj.x);
+    const float dy = (yh_i - A.y) + (ic.y - Bj.y);
+    const float r2 = fmaf(dx, dx, dy * dy);
+    bool in = r2 < P.rc2_hi;
+    if (in && !(r2 < P.rc2_lo)) {
+        // borderline: decide exactly as the reference does
+        double r, a;
+        in = ref_in_cutoff(P.c.px[b][ii] - P.c.px[b][jg], P.c.py[b][ii] - P.c.py[b][jg],
+                           P.f.shielding, r, a);
+    }
+    if (!in) return;
+    // 1/r: hardware rsqrt + one Newton step
+    float y = rsqrtf(r2);
+    const float h = r2 * y;
+    const float ee = fmaf(-h, y, 1.0f);
+    y = fmaf(0.5f * ee, y, y);
+    const float r = r2 * y;
+    const float kr = P.kappa_f * r;
+    const float ex = exp_neg(kr, E);
+    // C q_i q_j (1 + kr) e^{-kr} / r^3
+    const float s = ((ic.z * A.w) * (1.0f + kr)) * ex * ((y * y) * y);
+    float4 v = *acc;
+    kahan_add(v.x, v.z, s * dx);
+    kahan_add(v.y, v.w, s * dy);
+    *acc = v;
+}
+
+template <int NI, int G, int ILP, int JT>
+__global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+    constexpr int NT = NI * G;
+    constexpr int NP = ILP / 2;
+    static_assert(ILP % 2 == 0 && NI % 32 == 0 && JT % G == 0, "shape");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *s_pa = reinterpret_cast<float4 *>(smem_raw);
     float4 *s_pb = s_pa + JT;
-    float4 *s_red = s_pb + JT;  // [ILP][NT] (sx, sy, cx, cy)
+    float4 *s_cold = s_pb + JT;            // [ILP][NI]
+    float4 *s_acc = s_cold + ILP * NI;     // [G][ILP][NI]
+    double2 *s_red = reinterpret_cast<double2 *>(s_acc + G * ILP * NI);  // [ILP*NI]
 
     cg::cluster_group cl = cg::this_cluster();
     const int S = (int)cl.num_blocks();
     const int rank = (int)cl.block_rank();
     const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
+    const int t = tid % NI, g = tid / NI;
     const int n = P.c.n, n_pad = P.c.n_pad;
     const int st = (P.mode == kModeForceOnly) ? 1 : P.stage;
     const int b = (st - 1) & 1;
@@ -86,39 +144,36 @@ __global__ void __launch_bounds__(NT) pair_stage_fp32c(const StageParams P, cons
     const float4 *__restrict__ pb = P.c.pb[b];
     const double rc = sqrt(P.rc2);
 
-    float m2x[ILP], m2y[ILP], U[ILP], xl[ILP], yl[ILP], qc[ILP];
-    float sx[ILP], sy[ILP], cx[ILP], cy[ILP];
-    int ii[ILP];
+    float2 mx[NP], my[NP];
+    float U[ILP];
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
-        const int i = tile * NT * ILP + k * NT + tid;
-        ii[k] = i;
-        sx[k] = sy[k] = cx[k] = cy[k] = 0.0f;
+        const int i = tile * NI * ILP + k * NI + t;
+        float ax = 0.0f, ay = 0.0f, u = -INFINITY;
+        float4 cold = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         if (i < n) {
             const float4 A = pa[i];
             const float4 B = pb[i];
-            m2x[k] = -2.0f * A.x;
-            m2y[k] = -2.0f * A.y;
-            xl[k] = B.x;
-            yl[k] = B.y;
-            qc[k] = __double2float_rn(P.coulomb * P.c.q[i]);
-            // filter threshold: (rc^2 - |p_i|^2) + margin, margin covering the
-            // FP32 rounding of the expanded form and of the hi/lo split
-            const double ax = A.x, ay = A.y;
-            const double a2 = ax * ax + ay * ay;
+            ax = A.x;
+            ay = A.y;
+            // filter threshold: rc^2 - |p_i|^2 + margin; the margin covers
+            // the FP32 rounding of the expanded form and of the hi/lo split
+            const double a2 = (double)A.x * A.x + (double)A.y * A.y;
             const double pr = sqrt(a2) + rc;
-            U[k] = __double2float_ru(P.rc2 - a2 + 3.814697265625e-6 * pr * pr);
-        } else {
-            m2x[k] = m2y[k] = xl[k] = yl[k] = qc[k] = 0.0f;
-            U[k] = -INFINITY;
+            u = __double2float_ru(P.rc2 - a2 + 3.814697265625e-6 * pr * pr);
+            cold = make_float4(B.x, B.y, __double2float_rn(P.coulomb * P.c.q[i]), __int_as_float(i));
         }
+        if (k & 1) { mx[k / 2].y = -2.0f * ax; my[k / 2].y = -2.0f * ay; }
+        else { mx[k / 2].x = -2.0f * ax; my[k / 2].x = -2.0f * ay; }
+        U[k] = u;
+        if (g == 0) s_cold[k * NI + t] = cold;
+        s_acc[(g * ILP + k) * NI + t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 
     const int per = ((n_pad + S - 1) / S + 63) & ~63;
     const int j0 = rank * per;
     const int j1 = min(n_pad, j0 + per);
-    const float kap = P.kappa_f;
-    const float rc2_lo = P.rc2_lo, rc2_hi = P.rc2_hi;
+    constexpr int SUB = JT / G;
 
     for (int jt = j0; jt < j1; jt += JT) {
         const int cnt = min(JT, j1 - jt);
@@ -128,60 +183,58 @@ __global__ void __launch_bounds__(NT) pair_stage_fp32c(const StageParams P, cons
             s_pb[e] = pb[jt + e];
         }
         __syncthreads();
-#pragma unroll 2
-        for (int jj = 0; jj < cnt; jj++) {
+        const int lo = g * SUB;
+        const int hi = min(cnt, lo + SUB);
+#pragma unroll 4
+        for (int jj = lo; jj < hi; jj++) {
             const float4 A = s_pa[jj];
+            const float2 X = make_float2(A.x, A.x), Y = make_float2(A.y, A.y), Bv = make_float2(A.z, A.z);
+            float2 r2[NP];
+            bool hit = false;
 #pragma unroll
-            for (int k = 0; k < ILP; k++) {
-                const float r2e = fmaf(m2x[k], A.x, fmaf(m2y[k], A.y, A.z));
-                if (r2e < U[k]) {
-                    const int jg = jt + jj;
-                    if (jg != ii[k]) {
-                        const float4 Bj = s_pb[jj];
-                        const float dx = (-0.5f * m2x[k] - A.x) + (xl[k] - Bj.x);
-                        const float dy = (-0.5f * m2y[k] - A.y) + (yl[k] - Bj.y);
-                        const float r2 = fmaf(dx, dx, dy * dy);
-                        bool in = r2 < rc2_hi;
-                        if (in && !(r2 < rc2_lo)) {
-                            // borderline: decide exactly as the reference does
-                            double r, a;
-                            in = ref_in_cutoff(P.c.px[b][ii[k]] - P.c.px[b][jg],
-                                               P.c.py[b][ii[k]] - P.c.py[b][jg],
-                                               P.f.shielding, r, a);
-                        }
-                        if (in) {
-                            // 1/r: hardware rsqrt + one Newton step
-                            float y = rsqrtf(r2);
-                            const float h = r2 * y;
-                            const float ee = fmaf(-h, y, 1.0f);
-                            y = fmaf(0.5f * ee, y, y);
-                            const float r = r2 * y;
-                            const float kr = kap * r;
-                            const float ex = exp_neg(kr, E);
-                            // C q_i q_j (1 + kr) e^{-kr} / r^3
-                            const float s = ((qc[k] * A.w) * (1.0f + kr)) * ex * ((y * y) * y);
-                            kahan_add(sx[k], cx[k], s * dx);
-                            kahan_add(sy[k], cy[k], s * dy);
-                        }
+            for (int p = 0; p < NP; p++) {
+                r2[p] = __ffma2_rn(mx[p], X, __ffma2_rn(my[p], Y, Bv));
+                hit |= (r2[p].x < U[2 * p]) | (r2[p].y < U[2 * p + 1]);
+            }
+            if (__any_sync(0xffffffffu, hit)) {
+                const float4 Bj = s_pb[jj];
+                const int jg = jt + jj;
+#pragma unroll
+                for (int k = 0; k < ILP; k++) {
+                    const float rk = (k & 1) ? r2[k / 2].y : r2[k / 2].x;
+                    const bool hk = rk < U[k];
+                    if (__any_sync(0xffffffffu, hk) && hk) {
+                        const float xh = -0.5f * ((k & 1) ? mx[k / 2].y : mx[k / 2].x);
+                        const float yh = -0.5f * ((k & 1) ? my[k / 2].y : my[k / 2].x);
+                        precise_pair<NI, G, ILP>(P, E, b, xh, yh, A, Bj, jg, s_cold + k * NI + t,
+                                                 s_acc + (g * ILP + k) * NI + t);
                     }
                 }
             }
         }
     }
 
+    __syncthreads();
+    // combine the G groups (fixed order, FP64), then the S cluster ranks
+    for (int e = tid; e < ILP * NI; e += NT) {
+        double fx = 0.0, fy = 0.0;
 #pragma unroll
-    for (int k = 0; k < ILP; k++) s_red[k * NT + tid] = make_float4(sx[k], sy[k], cx[k], cy[k]);
+        for (int gg = 0; gg < G; gg++) {
+            const float4 v = s_acc[gg * ILP * NI + e];
+            fx += (double)v.x - (double)v.z;
+            fy += (double)v.y - (double)v.w;
+        }
+        s_red[e] = make_double2(fx, fy);
+    }
     cl.sync();
-    // finalize 1/S of the tile's particles in this CTA: combine the S partial
-    // sums (rank order, FP64) and run the stage epilogue
-    for (int e = rank * NT + tid; e < NT * ILP; e += NT * S) {
-        const int i = tile * NT * ILP + e;
+    for (int e = rank * NT + tid; e < NI * ILP; e += NT * S) {
+        const int i = tile * NI * ILP + e;
         if (i < n) {
             double fx = 0.0, fy = 0.0;
             for (int r = 0; r < S; r++) {
-                const float4 v = *cl.map_shared_rank(s_red + e, r);
-                fx += (double)v.x - (double)v.z;
-                fy += (double)v.y - (double)v.w;
+                const double2 v = *cl.map_shared_rank(s_red + e, r);
+                fx += v.x;
+                fy += v.y;
             }
             stage_epilogue(P, i, fx, fy);
         }
@@ -191,23 +244,35 @@ __global__ void __launch_bounds__(NT) pair_stage_fp32c(const StageParams P, cons
 }
 
 // ---------------------------------------------------------------------------
-// Plain FP64 kernel (same decomposition, every operation in FP64).
+// Plain FP64 kernel: same decomposition (G j-groups x NI i-lanes, cluster
+// j split, one uniform branch per j), every operation in FP64.
 // ---------------------------------------------------------------------------
 struct alignas(32) JD {
     double x, y, b, q;
 };
 
-template <int NT, int ILP, int JT>
-__global__ void __launch_bounds__(NT) pair_stage_fp64(const StageParams P) {
+template <int NI, int G, int ILP>
+struct Fp64Smem {
+    static constexpr size_t part = (size_t)G * ILP * NI * sizeof(double2);
+    static constexpr size_t red = (size_t)ILP * NI * sizeof(double2);
+    static size_t bytes(int jt) { return (size_t)jt * sizeof(JD) + part + red; }
+};
+
+template <int NI, int G, int ILP, int JT>
+__global__ void __launch_bounds__(NI * G, 2) pair_stage_fp64(const StageParams P) {
+    constexpr int NT = NI * G;
+    static_assert(NI % 32 == 0 && JT % G == 0, "shape");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     JD *s_j = reinterpret_cast<JD *>(smem_raw);
-    double2 *s_red = reinterpret_cast<double2 *>(s_j + JT);  // [ILP][NT]
+    double2 *s_part = reinterpret_cast<double2 *>(s_j + JT);  // [G][ILP][NI]
+    double2 *s_red = s_part + G * ILP * NI;                     // [ILP*NI]
 
     cg::cluster_group cl = cg::this_cluster();
     const int S = (int)cl.num_blocks();
     const int rank = (int)cl.block_rank();
     const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
+    const int t = tid % NI, g = tid / NI;
     const int n = P.c.n, n_pad = P.c.n_pad;
     const int st = (P.mode == kModeForceOnly) ? 1 : P.stage;
     const int b = (st - 1) & 1;
@@ -222,7 +287,7 @@ __global__ void __launch_bounds__(NT) pair_stage_fp64(const StageParams P) {
     int ii[ILP];
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
-        const int i = tile * NT * ILP + k * NT + tid;
+        const int i = tile * NI * ILP + k * NI + t;
         ii[k] = i;
         fx[k] = fy[k] = 0.0;
         if (i < n) {
@@ -241,6 +306,7 @@ __global__ void __launch_bounds__(NT) pair_stage_fp64(const StageParams P) {
     const int per = ((n_pad + S - 1) / S + 63) & ~63;
     const int j0 = rank * per;
     const int j1 = min(n_pad, j0 + per);
+    constexpr int SUB = JT / G;
 
     for (int jt = j0; jt < j1; jt += JT) {
         const int cnt = min(JT, j1 - jt);
@@ -255,15 +321,23 @@ __global__ void __launch_bounds__(NT) pair_stage_fp64(const StageParams P) {
             s_j[e] = d;
         }
         __syncthreads();
+        const int lo = g * SUB;
+        const int hi = min(cnt, lo + SUB);
 #pragma unroll 2
-        for (int jj = 0; jj < cnt; jj++) {
+        for (int jj = lo; jj < hi; jj++) {
             const JD d = s_j[jj];
+            double r2e[ILP];
+            bool hit = false;
 #pragma unroll
             for (int k = 0; k < ILP; k++) {
-                const double r2e = fma(-2.0 * xi[k], d.x, fma(-2.0 * yi[k], d.y, d.b));
-                if (r2e < U[k]) {
-                    const int jg = jt + jj;
-                    if (jg != ii[k]) {
+                r2e[k] = fma(-2.0 * xi[k], d.x, fma(-2.0 * yi[k], d.y, d.b));
+                hit |= r2e[k] < U[k];
+            }
+            if (__any_sync(0xffffffffu, hit)) {
+                const int jg = jt + jj;
+#pragma unroll
+                for (int k = 0; k < ILP; k++) {
+                    if (r2e[k] < U[k] && jg != ii[k]) {
                         const double dx = __dsub_rn(xi[k], d.x);
                         const double dy = __dsub_rn(yi[k], d.y);
                         double r, a;
@@ -285,10 +359,21 @@ __global__ void __launch_bounds__(NT) pair_stage_fp64(const StageParams P) {
     }
 
 #pragma unroll
-    for (int k = 0; k < ILP; k++) s_red[k * NT + tid] = make_double2(fx[k], fy[k]);
+    for (int k = 0; k < ILP; k++) s_part[(g * ILP + k) * NI + t] = make_double2(fx[k], fy[k]);
+    __syncthreads();
+    for (int e = tid; e < ILP * NI; e += NT) {
+        double sx = 0.0, sy = 0.0;
+#pragma unroll
+        for (int gg = 0; gg < G; gg++) {
+            const double2 v = s_part[gg * ILP * NI + e];
+            sx = __dadd_rn(sx, v.x);
+            sy = __dadd_rn(sy, v.y);
+        }
+        s_red[e] = make_double2(sx, sy);
+    }
     cl.sync();
-    for (int e = rank * NT + tid; e < NT * ILP; e += NT * S) {
-        const int i = tile * NT * ILP + e;
+    for (int e = rank * NT + tid; e < NI * ILP; e += NT * S) {
+        const int i = tile * NI * ILP + e;
         if (i < n) {
             double sxx = 0.0, syy = 0.0;
             for (int r = 0; r < S; r++) {

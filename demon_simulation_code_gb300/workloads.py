@@ -78,6 +78,45 @@ def uniform_disk(rng: np.random.Generator, n: int, radius: float):
     return r * np.cos(th), r * np.sin(th)
 
 
+def uniform_disk_minsep(rng: np.random.Generator, n: int, radius: float, min_sep: float):
+    """Uniform in a disk with every pair at least `min_sep` apart (random
+    sequential addition).  Keeps RK4 at dt ~ 1e-4 s well conditioned: the
+    reference itself shrinks dt whenever a pair is closer than 1e-4 m
+    (Integrator.cpp:68-134)."""
+    xs = np.empty(n)
+    ys = np.empty(n)
+    k = 0
+    tries = 0
+    while k < n:
+        tries += 1
+        if tries > 200 * n:
+            raise ValueError("min_sep too large for this disk")
+        r = radius * np.sqrt(rng.random())
+        th = 2.0 * np.pi * rng.random()
+        x, y = r * np.cos(th), r * np.sin(th)
+        if k and np.min((xs[:k] - x) ** 2 + (ys[:k] - y) ** 2) < min_sep * min_sep:
+            continue
+        xs[k] = x
+        ys[k] = y
+        k += 1
+    return xs, ys
+
+
+def calm_cloud(n: int = 512, radius: float = 1e-2, seed: int = 0, min_sep: float = 4e-4,
+               vscale: float = 1e-4) -> Cloud:
+    """A well-conditioned cloud for gated trajectory comparisons: minimum pair
+    separation 4e-4 m, kappa = 5e3 (Coulomb is ~25-70% of the force),
+    k_c = 1e4 (no collapse within a few hundred steps of 1e-4 s), small random
+    velocities.  A 1e-15 relative perturbation stays ~1e-15 over 300 steps,
+    so FP64 trajectories can be gated at 1e-12."""
+    rng = np.random.default_rng(seed)
+    x, y = uniform_disk_minsep(rng, n, radius, min_sep)
+    return Cloud(x=x, y=y, vx=rng.normal(0, vscale, n), vy=rng.normal(0, vscale, n),
+                 q=np.full(n, Q_DUST), m=np.full(n, M_DUST),
+                 flags=CONFINEMENT | DRAG | SHIELDED_COULOMB, shielding=5e3, confine=1e4,
+                 gamma=3.0)
+
+
 def disk_cloud(n: int, radius: float, seed: int, *, shielding=2e4, confine=1e8, gamma=3.0,
                q=Q_DUST, m=M_DUST, heat=0.0, thermal_seed=0) -> Cloud:
     rng = np.random.default_rng(seed)

@@ -63,14 +63,15 @@ def main():
                                confine_y=2e8, gamma=3.0)
         fx, fy = ref.forces(x, y, vx, vy, q, m, p)
         out[name] = dict(x=x, y=y, vx=vx, vy=vy, q=q, m=m, flags=np.int64(flags), fx=fx, fy=fy)
-    # 3. fixed-dt RK4 (reference CacheOperator + forces, stage bookkeeping restated)
-    x, y, vx, vy = disk(64, 1e-3, 30, vscale=1e-3)
-    q = np.full(64, Q)
-    m = np.full(64, M)
-    p = oracle.make_params(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0)
+    # 3. fixed-dt RK4 (reference CacheOperator + forces, stage bookkeeping
+    # restated) on a well-conditioned cloud (see workloads.calm_cloud)
+    c = W.calm_cloud(64, 3e-3, 30)
+    x, y, vx, vy, q, m = c.x, c.y, c.vx, c.vy, c.q, c.m
+    p = oracle.make_params(**c.params())
     rx, ry, rvx, rvy = ref.rk4_fixed(x, y, vx, vy, q, m, p, 1e-4, 25)
     out["rk4_fixed_n64"] = dict(x=x, y=y, vx=vx, vy=vy, q=q, m=m, dt=np.float64(1e-4),
-                                steps=np.int64(25), x1=rx, y1=ry, vx1=rvx, vy1=rvy)
+                                steps=np.int64(25), x1=rx, y1=ry, vx1=rvx, vy1=rvy,
+                                kappa=np.float64(c.shielding), confine=np.float64(c.confine))
     # 4. the reference's own moveParticles (adaptive dt), disk512 workload
     c = W.disk512().clouds[0]
     p = oracle.make_params(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0)

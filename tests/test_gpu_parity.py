@@ -127,7 +127,8 @@ def test_all_forces_vs_reference_golden(gpu_ctx, name, prec):
 def test_rk4_fixed_vs_reference_golden(gpu_ctx, prec):
     g = golden("rk4_fixed_n64")
     c = DeviceCloud(gpu_ctx, g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"],
-                    dict(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0))
+                    dict(flags=1 | 2 | 4, shielding=float(g["kappa"]), confine=float(g["confine"]),
+                         gamma=3.0))
     t = c.step(int(g["steps"]), float(g["dt"]), prec, t=0.0)
     x, y, vx, vy = c.download()
     tol = 1e-12 if prec == "fp64" else 1e-7
@@ -137,16 +138,22 @@ def test_rk4_fixed_vs_reference_golden(gpu_ctx, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32c"])
-def test_rk4_disk512_trajectory_vs_oracle(gpu_ctx, oracle_lib, prec):
-    c0 = W.disk512().clouds[0]
-    p = oracle.make_params(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0)
+def test_rk4_trajectory_100_steps_vs_oracle(gpu_ctx, oracle_lib, prec):
+    """Gated short-horizon trajectory on a well-conditioned cloud (minimum
+    separation 4e-4 m).  Uniform-random disks contain pairs ~1e-6 m apart
+    for which RK4 at dt = 1e-4 s is unstable, so last-bit force differences
+    grow without bound there; those are reported, not gated."""
+    c0 = W.calm_cloud(512, 1e-2, 1)
+    p = oracle.make_params(**c0.params())
     ref = oracle_lib.rk4_fixed(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m, p, 1e-4, 100)
     c = DeviceCloud.from_cloud(gpu_ctx, c0)
     c.step(100, 1e-4, prec)  # 100 steps: CUDA-graph replays + remainder
     out = c.download()
-    R = 5e-3
+    R = 1e-2
     errx = np.max(np.hypot(out[0] - ref[0], out[1] - ref[1])) / R
+    errv = rel(out[2], ref[2])
     assert errx <= (1e-12 if prec == "fp64" else 1e-7), errx
+    assert errv <= (1e-10 if prec == "fp64" else 1e-5), errv
 
 
 def test_graph_and_direct_steps_identical(gpu_ctx):
@@ -174,8 +181,8 @@ def test_thermal_force_vs_oracle(gpu_ctx, oracle_lib, mode):
 
 
 def test_thermal_rk4_fp64_vs_oracle(gpu_ctx, oracle_lib):
-    c0 = W.disk512().clouds[0]
-    params = dict(flags=1 | 2 | 4 | 16, shielding=2e4, confine=1e8, gamma=3.0, heat=1e-14,
+    c0 = W.calm_cloud(512, 1e-2, 2)
+    params = dict(flags=1 | 2 | 4 | 16, shielding=5e3, confine=1e4, gamma=3.0, heat=1e-14,
                   thermal_mode=1, seed=1)
     ref = oracle_lib.rk4_fixed(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m,
                                oracle.make_params(**params), 1e-4, 20, step0=5)

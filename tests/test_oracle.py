@@ -43,7 +43,8 @@ def test_all_forces_match_reference_golden(oracle_lib, name):
 
 def test_rk4_fixed_matches_reference_golden(oracle_lib):
     g = load("rk4_fixed_n64")
-    p = oracle.make_params(flags=1 | 2 | 4, shielding=2e4, confine=1e8, gamma=3.0)
+    p = oracle.make_params(flags=1 | 2 | 4, shielding=float(g["kappa"]), confine=float(g["confine"]),
+                           gamma=3.0)
     out = oracle_lib.rk4_fixed(g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"], p,
                                float(g["dt"]), int(g["steps"]))
     for a, k in zip(out, ("x1", "y1", "vx1", "vy1")):
