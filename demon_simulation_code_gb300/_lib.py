@@ -13,6 +13,7 @@ import numpy as np
 from .build import LIB
 
 DM_OK = 0
+DM_ERR_ARG = 1
 DM_FP64 = 0
 DM_FP32C = 1
 
@@ -80,6 +81,10 @@ SIGNATURES = {
     "dm_cloud_diagnostics": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "dm_cloud_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dm_cloud_get_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "dm_diagnostics_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.POINTER(ForceParams),
+                                              ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 

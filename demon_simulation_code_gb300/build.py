@@ -18,7 +18,7 @@ BUILD = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["dm_api.cu"]
+SOURCES = ["dm_api.cu", "dm_noalloc.cu"]
 
 
 def nvcc() -> str:

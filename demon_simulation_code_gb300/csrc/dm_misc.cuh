@@ -9,7 +9,7 @@ namespace dm {
 
 // Writes stage buffer 0 (FP64 and two-float copies) from the base
 // positions, and the padding particles of both buffers.
-__global__ void init_positions(CloudDev c) {
+static __global__ void init_positions(CloudDev c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n_pad) return;
     if (i < c.n) {
@@ -42,7 +42,7 @@ __device__ __forceinline__ float sep2_f32(float ax, float ay, float bx, float by
 // the upper triangle of 4-blocks.  The minimum r^2 (a non-negative float, so
 // its bit pattern orders like an unsigned int) is combined with atomicMin,
 // which is order-independent.
-__global__ void checked_min_dist2(const double *__restrict__ x, const double *__restrict__ y,
+static __global__ void checked_min_dist2(const double *__restrict__ x, const double *__restrict__ y,
                                   int nb, unsigned int *out) {
     const long long total = (long long)nb * (nb + 1) / 2;
     float best = INFINITY;
@@ -88,7 +88,7 @@ __global__ void checked_min_dist2(const double *__restrict__ x, const double *__
 // tryToReduceTimeStep (Integrator.cpp:144-155) applied to the minimum:
 // while dmin <= dist: dist /= 10.0f, dt /= 10.0.  A zero separation (where
 // the reference never terminates) sets error bit 2 and leaves dt unchanged.
-__global__ void adaptive_dt(const unsigned int *min_r2_bits, double init_dt, double *dt_out,
+static __global__ void adaptive_dt(const unsigned int *min_r2_bits, double init_dt, double *dt_out,
                             float *dmin_out, int *err) {
     const float dmin = __fsqrt_rn(__uint_as_float(*min_r2_bits));
     float dist = 1.0e-4f;

@@ -188,6 +188,32 @@ int dm_cloud_diagnostics(dm_cloud *cloud, double out[5]);
 int dm_cloud_set_step_counter(dm_cloud *cloud, uint64_t step);
 int dm_cloud_get_step_counter(dm_cloud *cloud, uint64_t *step);
 
+/* ---- allocation-free diagnostics ------------------------------------- */
+
+/* No counterpart in the reference.  dm_cloud_diagnostics' computation for
+ * callers that can't allocate device memory: a host application that owns
+ * every device byte through its own pool or budget, or code that must not
+ * trigger cudaMalloc's implicit device-wide synchronisation while its other
+ * streams run.  The caller passes its own device arrays (n FP64 values each),
+ * the force parameters (host struct) and a device output of 5 doubles
+ * (same meaning as dm_cloud_diagnostics' out); the work is queued on
+ * `stream` (a cudaStream_t, NULL = the legacy default stream) and the call
+ * returns without waiting.  It needs no dm_ctx or dm_cloud and calls no
+ * allocating CUDA or library routine: its partial sums live in a fixed
+ * file-scope device array of 4096 x 5 doubles (160 KiB, held by every GPU
+ * that loads this library until the process exits).
+ *  - n must be in [1, 524288]; larger n returns DM_ERR_ARG without launching.
+ *  - The first call on each device looks up that array's device address with
+ *    the device current; make that first call before any stream capture.
+ *  - All calls share the array: calls that overlap on the GPU race on it and
+ *    must be serialised by the caller (e.g. one stream).
+ * Errors are reported by the status code only (dm_last_error is not set). */
+int dm_diagnostics_noalloc(int n, const double *d_x, const double *d_y,
+                           const double *d_vx, const double *d_vy,
+                           const double *d_q, const double *d_m,
+                           const dm_force_params *params, double *d_out,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif
