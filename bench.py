@@ -237,6 +237,8 @@ def run_gb300(args, world, rank, local):
 
             dist.barrier()
 
+    step_ms = []
+
     def timed_steps(prec, k):
         evs = []
         for _ in range(k):
@@ -248,7 +250,9 @@ def run_gb300(args, world, rank, local):
             b.record(stream)
             evs.append((a, b))
         torch.cuda.synchronize()
-        return sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        ms = [a.elapsed_time(b) for a, b in evs]
+        step_ms[:] = ms
+        return sum(ms) / 1e3
 
     # warm-up (untimed)
     cloud.step(max(args.warmup, 3), w.dt, args.precision)
@@ -261,6 +265,7 @@ def run_gb300(args, world, rank, local):
     with ClockSampler(local) as clk:
         elapsed = timed_steps(args.precision, args.steps)
     pair_ms, launches, pairs_prof = ctx.profile_read()
+    main_step_ms = list(step_ms)
     ctx.profile(False)
     t_max = elapsed
     if world > 1:
@@ -341,6 +346,8 @@ def run_gb300(args, world, rank, local):
             "fp32c_over_fp64": (value / world / fp64_value) if fp64_value else None,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * n,
                     "d2h_bytes_per_step": 4 * 8 * n, "steps": args.e2e_steps},
+            "step_ms_percentiles": {p: float(np.percentile(main_step_ms, q))
+                                    for p, q in (("p10", 10), ("p50", 50), ("p90", 90), ("max", 100))},
             "gpu_launches": 4 * args.steps,
             "roofline": {"bound": "fp32-pipe", "kernel": kname, "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,

@@ -23,6 +23,8 @@
 
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "dm_device.cuh"
 
 namespace dm {
@@ -68,38 +70,75 @@ struct PairTuning {
 // FP32-compensated kernel.
 //
 // CTA = G j-groups x NI i-lanes.  Lane t of every group owns the ILP
-// particles i = tile*NI*ILP + k*NI + t; group g sweeps the g-th quarter
-// (for G = 4) of every shared-memory j tile, so all G groups reuse one tile.
-// Hot registers per particle: -2*xh, -2*yh (packed in pairs for the f32x2
-// FMA) and the filter threshold; everything only the rare precise path
-// needs (lo parts, C*q_i, index, Kahan accumulators) lives in shared memory.
-// Per j the warp takes ONE uniform branch (vote over all its lanes and
-// slots); the precise path runs only when some lane's filter fired.
+// particles i = tile*NI*ILP + k*NI + t; group g sweeps every G-th j of each
+// shared-memory tile, so all G groups reuse one tile.  Hot registers per
+// particle: -2*xh, -2*yh (packed in pairs for the f32x2 FMA), the filter
+// threshold and the Kahan sums; the rest of the particle's data lives in
+// shared memory.
+//
+// Filter hits are not evaluated where they are found.  Per j the warp takes
+// one uniform branch (vote over lanes and slots); when some lane's filter
+// fired, the warp ballots each slot and queues (j, ballot) in shared memory.
+// Every 32 queued entries of a slot (and at the end of a tile) a 32x32
+// bit-matrix transpose gives each lane the set of queued j it hit, and all
+// lanes run the precise path on their own hits together.  Each lane
+// accumulates only into its own sums, so the result is deterministic and no
+// atomics are needed; SIMD utilisation of the precise path goes from ~1/32
+// (sparse) or the hit fraction (dense) to mean/max of the per-lane hit count.
 // ---------------------------------------------------------------------------
 template <int NI, int G, int ILP>
 struct Fp32cSmem {
     static constexpr size_t cold = (size_t)ILP * NI * sizeof(float4);
-    static constexpr size_t acc = (size_t)G * ILP * NI * sizeof(float4);
-    static constexpr size_t red = (size_t)ILP * NI * sizeof(double2);
-    static size_t bytes(int jt) { return (size_t)jt * 2 * sizeof(float4) + cold + acc + red; }
+    static constexpr size_t queue = (size_t)G * (NI / 32) * ILP * 32 * sizeof(int2);
+    static constexpr size_t red = (size_t)G * ILP * NI * sizeof(double2);
+    static size_t bytes(int jt) { return (size_t)jt * 2 * sizeof(float4) + cold + queue + red; }
 };
 
-template <int NI, int G, int ILP>
+// 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
+// column r (bit c = bit r of row c) on exit.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int st = 0; st < 5; st++) {
+        const int j = 16 >> st;
+        const uint32_t m = masks[st];
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+        // lanes with bit j clear keep their low half-blocks and take the
+        // partner's; lanes with it set the reverse
+        if (lane & j) x = (x & ~m) | ((y & ~m) >> j);
+        else x = (x & m) | ((y & m) << j);
+    }
+    return x;
+}
+
+// Calls f(std::integral_constant<int, k>) for k = 0 .. K-1 (compile-time k).
+template <int K, typename F>
+__device__ __forceinline__ void static_for(F &&f) {
+    if constexpr (K > 0) {
+        static_for<K - 1>(f);
+        f(std::integral_constant<int, K - 1>{});
+    }
+}
+
+struct PairCtx {
+    float xl, yl, qc;
+    int ii;
+};
+
 __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpConsts &E, int b,
-                                             float xh_i, float yh_i, const float4 &A,
-                                             const float4 &Bj, int jg, float4 *cold,
-                                             float4 *acc) {
-    const float4 ic = *cold;  // (xl, yl, C*q_i, bits of i)
-    const int ii = __float_as_int(ic.w);
-    if (jg == ii) return;
-    const float dx = (xh_i - A.x) + (ic.x - Bj.x);
-    const float dy = (yh_i - A.y) + (ic.y - Bj.y);
+                                             float xh_i, float yh_i, const PairCtx &ic,
+                                             const float4 &A, const float4 &Bj, int jg, float &sx,
+                                             float &sy, float &cx, float &cy) {
+    if (jg == ic.ii) return;
+    const float dx = (xh_i - A.x) + (ic.xl - Bj.x);
+    const float dy = (yh_i - A.y) + (ic.yl - Bj.y);
     const float r2 = fmaf(dx, dx, dy * dy);
     bool in = r2 < P.rc2_hi;
     if (in && !(r2 < P.rc2_lo)) {
         // borderline: decide exactly as the reference does
         double r, a;
-        in = ref_in_cutoff(P.c.px[b][ii] - P.c.px[b][jg], P.c.py[b][ii] - P.c.py[b][jg],
+        in = ref_in_cutoff(P.c.px[b][ic.ii] - P.c.px[b][jg], P.c.py[b][ic.ii] - P.c.py[b][jg],
                            P.f.shielding, r, a);
     }
     if (!in) return;
@@ -112,30 +151,30 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
     const float kr = P.kappa_f * r;
     const float ex = exp_neg(kr, E);
     // C q_i q_j (1 + kr) e^{-kr} / r^3
-    const float s = ((ic.z * A.w) * (1.0f + kr)) * ex * ((y * y) * y);
-    float4 v = *acc;
-    kahan_add(v.x, v.z, s * dx);
-    kahan_add(v.y, v.w, s * dy);
-    *acc = v;
+    const float s = ((ic.qc * A.w) * (1.0f + kr)) * ex * ((y * y) * y);
+    kahan_add(sx, cx, s * dx);
+    kahan_add(sy, cy, s * dy);
 }
 
 template <int NI, int G, int ILP, int JT>
 __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
     constexpr int NT = NI * G;
     constexpr int NP = ILP / 2;
+    constexpr int NW = NT / 32;
     static_assert(ILP % 2 == 0 && NI % 32 == 0 && JT % G == 0, "shape");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *s_pa = reinterpret_cast<float4 *>(smem_raw);
     float4 *s_pb = s_pa + JT;
-    float4 *s_cold = s_pb + JT;            // [ILP][NI]
-    float4 *s_acc = s_cold + ILP * NI;     // [G][ILP][NI]
-    double2 *s_red = reinterpret_cast<double2 *>(s_acc + G * ILP * NI);  // [ILP*NI]
+    float4 *s_cold = s_pb + JT;                                   // [ILP][NI]
+    int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * NI);  // [NW][ILP][32]
+    double2 *s_red = reinterpret_cast<double2 *>(s_queue + NW * ILP * 32);  // [G][ILP*NI]
 
     cg::cluster_group cl = cg::this_cluster();
     const int S = (int)cl.num_blocks();
     const int rank = (int)cl.block_rank();
     const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const int t = tid % NI, g = tid / NI;
     const int n = P.c.n, n_pad = P.c.n_pad;
     const int st = (P.mode == kModeForceOnly) ? 1 : P.stage;
@@ -143,9 +182,11 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     const float4 *__restrict__ pa = P.c.pa[b];
     const float4 *__restrict__ pb = P.c.pb[b];
     const double rc = sqrt(P.rc2);
+    int2 *my_queue = s_queue + (tid >> 5) * ILP * 32;
 
     float2 mx[NP], my[NP];
     float U[ILP];
+    float sx[ILP], sy[ILP], cx[ILP], cy[ILP];
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
         const int i = tile * NI * ILP + k * NI + t;
@@ -167,13 +208,43 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
         else { mx[k / 2].x = -2.0f * ax; my[k / 2].x = -2.0f * ay; }
         U[k] = u;
         if (g == 0) s_cold[k * NI + t] = cold;
-        s_acc[(g * ILP + k) * NI + t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        sx[k] = sy[k] = cx[k] = cy[k] = 0.0f;
     }
 
     const int per = ((n_pad + S - 1) / S + 63) & ~63;
     const int j0 = rank * per;
     const int j1 = min(n_pad, j0 + per);
-    constexpr int SUB = JT / G;
+    int qn[ILP];
+#pragma unroll
+    for (int k = 0; k < ILP; k++) qn[k] = 0;
+    __syncthreads();  // s_cold complete
+
+    // Run the precise path on the queued entries of slot K, then empty it.
+    auto flush = [&](auto kc, int jt) {
+        constexpr int K = decltype(kc)::value;
+        __syncwarp();
+        const int2 ent = (lane < qn[K]) ? my_queue[K * 32 + lane] : make_int2(0, 0);
+        uint32_t mask = warp_transpose32((uint32_t)ent.y);
+        const float4 c4 = s_cold[K * NI + t];
+        PairCtx ic;
+        ic.xl = c4.x;
+        ic.yl = c4.y;
+        ic.qc = c4.z;
+        ic.ii = __float_as_int(c4.w);
+        const float xh = -0.5f * ((K & 1) ? mx[K / 2].y : mx[K / 2].x);
+        const float yh = -0.5f * ((K & 1) ? my[K / 2].y : my[K / 2].x);
+        while (__any_sync(0xffffffffu, mask != 0u)) {
+            if (mask) {
+                const int e = __ffs(mask) - 1;
+                mask &= mask - 1u;
+                const int jj = my_queue[K * 32 + e].x;
+                precise_pair(P, E, b, xh, yh, ic, s_pa[jj], s_pb[jj], jt + jj, sx[K], sy[K],
+                             cx[K], cy[K]);
+            }
+        }
+        __syncwarp();
+        qn[K] = 0;
+    };
 
     for (int jt = j0; jt < j1; jt += JT) {
         const int cnt = min(JT, j1 - jt);
@@ -183,10 +254,8 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
             s_pb[e] = pb[jt + e];
         }
         __syncthreads();
-        const int lo = g * SUB;
-        const int hi = min(cnt, lo + SUB);
-#pragma unroll 4
-        for (int jj = lo; jj < hi; jj++) {
+#pragma unroll 2
+        for (int jj = g; jj < cnt; jj += G) {
             const float4 A = s_pa[jj];
             const float2 X = make_float2(A.x, A.x), Y = make_float2(A.y, A.y), Bv = make_float2(A.z, A.z);
             float2 r2[NP];
@@ -197,32 +266,35 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
                 hit |= (r2[p].x < U[2 * p]) | (r2[p].y < U[2 * p + 1]);
             }
             if (__any_sync(0xffffffffu, hit)) {
-                const float4 Bj = s_pb[jj];
-                const int jg = jt + jj;
-#pragma unroll
-                for (int k = 0; k < ILP; k++) {
+                static_for<ILP>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
                     const float rk = (k & 1) ? r2[k / 2].y : r2[k / 2].x;
-                    const bool hk = rk < U[k];
-                    if (__any_sync(0xffffffffu, hk) && hk) {
-                        const float xh = -0.5f * ((k & 1) ? mx[k / 2].y : mx[k / 2].x);
-                        const float yh = -0.5f * ((k & 1) ? my[k / 2].y : my[k / 2].x);
-                        precise_pair<NI, G, ILP>(P, E, b, xh, yh, A, Bj, jg, s_cold + k * NI + t,
-                                                 s_acc + (g * ILP + k) * NI + t);
+                    const uint32_t bal = __ballot_sync(0xffffffffu, rk < U[k]);
+                    if (bal) {
+                        if (lane == 0) my_queue[k * 32 + qn[k]] = make_int2(jj, (int)bal);
+                        if (++qn[k] == 32) flush(kc, jt);
                     }
-                }
+                });
             }
         }
+        // the queued j index into this tile: drain before it is overwritten
+        static_for<ILP>([&](auto kc) {
+            if (qn[decltype(kc)::value]) flush(kc, jt);
+        });
     }
 
-    __syncthreads();
     // combine the G groups (fixed order, FP64), then the S cluster ranks
-    for (int e = tid; e < ILP * NI; e += NT) {
-        double fx = 0.0, fy = 0.0;
 #pragma unroll
-        for (int gg = 0; gg < G; gg++) {
-            const float4 v = s_acc[gg * ILP * NI + e];
-            fx += (double)v.x - (double)v.z;
-            fy += (double)v.y - (double)v.w;
+    for (int k = 0; k < ILP; k++)
+        s_red[g * ILP * NI + k * NI + t] =
+            make_double2((double)sx[k] - (double)cx[k], (double)sy[k] - (double)cy[k]);
+    __syncthreads();
+    for (int e = tid; e < ILP * NI; e += NT) {
+        double fx = s_red[e].x, fy = s_red[e].y;
+#pragma unroll
+        for (int gg = 1; gg < G; gg++) {
+            fx += s_red[gg * ILP * NI + e].x;
+            fy += s_red[gg * ILP * NI + e].y;
         }
         s_red[e] = make_double2(fx, fy);
     }
