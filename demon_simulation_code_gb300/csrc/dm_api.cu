@@ -184,10 +184,13 @@ int ensure_kernel_attrs(dm_ctx *ctx) {
     return DM_OK;
 }
 
-// j split (cluster size S) for a cloud: the S in [1, 16] that minimises the
-// number of co-resident cluster waves per unit of work (waves / S), using the
-// device's own count of co-resident clusters of that size.  Ties go to the
-// smaller S (fewer partial sums).
+// j split (cluster size S) for a cloud.  All CTAs of a launch do equal work
+// (1/S of a tile), so the launch takes as long as its busiest SM: with X
+// co-resident clusters of size S (the device's own count, GPC packing
+// included) the tiles run in ceil(ntiles / X) cluster waves, and within a
+// wave the busiest SM holds ceil(CTAs_in_wave / num_sms) CTAs.  Cost =
+// sum over waves of that count / S; the smallest S within 2% of the best wins
+// (fewer partial sums).
 int pick_split(dm_ctx *ctx, int precision, int n, int n_pad, int *out) {
     const KernelShape k = shape_of(precision);
     const int ntiles = (n + k.tile - 1) / k.tile;
@@ -212,8 +215,11 @@ int pick_split(dm_ctx *ctx, int precision, int n, int n_pad, int *out) {
             cudaGetLastError();
             continue;
         }
-        const int waves = (ntiles + nc - 1) / nc;
-        const double cost = (double)waves / S;
+        double cost = 0.0;
+        for (int left = ntiles; left > 0; left -= nc) {
+            const int in_wave = std::min(left, nc) * S;
+            cost += (double)((in_wave + ctx->num_sms - 1) / ctx->num_sms) / S;
+        }
         if (cost < best_cost * 0.98) {
             best_cost = cost;
             best_s = S;

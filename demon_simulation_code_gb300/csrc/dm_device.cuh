@@ -166,8 +166,19 @@ __device__ __forceinline__ bool ref_in_cutoff(double dx, double dy, double kappa
 // Every FP64 operation is an explicit round-to-nearest intrinsic so nothing
 // is contracted into an FMA: given the same forces the state update is bit
 // for bit the reference's.
+// Thermal kick of particle i for the running stage (zero when the thermal
+// force is off); computed ahead of the epilogue by the pair kernels.
+__device__ __forceinline__ double2 stage_thermal(const StageParams &P, int i) {
+    double tx = 0.0, ty = 0.0;
+    if (P.f.flags & kThermal) {
+        const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
+        thermal_kick(P.f, (uint32_t)i, stage_step_index(P), s, tx, ty);
+    }
+    return make_double2(tx, ty);
+}
+
 __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, double fpx,
-                                               double fpy) {
+                                               double fpy, double2 therm) {
     const CloudDev &c = P.c;
     const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
     const int b = (s - 1) & 1;
@@ -196,10 +207,8 @@ __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, doub
         Fy = __dadd_rn(Fy, fpy);
     }
     if (fl & kThermal) {
-        double tx, ty;
-        thermal_kick(P.f, (uint32_t)i, stage_step_index(P), s, tx, ty);
-        Fx = __dadd_rn(Fx, tx);
-        Fy = __dadd_rn(Fy, ty);
+        Fx = __dadd_rn(Fx, therm.x);
+        Fy = __dadd_rn(Fy, therm.y);
     }
     if (P.mode == kModeForceOnly) {
         P.fx_out[i] = Fx;

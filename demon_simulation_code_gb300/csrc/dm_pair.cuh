@@ -90,8 +90,12 @@ template <int NI, int G, int ILP>
 struct Fp32cSmem {
     static constexpr size_t cold = (size_t)ILP * NI * sizeof(float4);
     static constexpr size_t queue = (size_t)G * (NI / 32) * ILP * 32 * sizeof(int2);
-    static constexpr size_t red = (size_t)G * ILP * NI * sizeof(double2);
-    static size_t bytes(int jt) { return (size_t)jt * 2 * sizeof(float4) + cold + queue + red; }
+    static constexpr size_t acc = (size_t)ILP * NI * G * sizeof(float4);
+    static constexpr size_t red = (size_t)ILP * NI * sizeof(double2);
+    static constexpr size_t therm = (size_t)NI * G * sizeof(double2);
+    static size_t bytes(int jt) {
+        return (size_t)jt * 2 * sizeof(float4) + cold + queue + acc + red + therm;
+    }
 };
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
@@ -167,7 +171,9 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     float4 *s_pb = s_pa + JT;
     float4 *s_cold = s_pb + JT;                                   // [ILP][NI]
     int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * NI);  // [NW][ILP][32]
-    double2 *s_red = reinterpret_cast<double2 *>(s_queue + NW * ILP * 32);  // [G][ILP*NI]
+    float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);  // [ILP][NT] Kahan sums
+    double2 *s_red = reinterpret_cast<double2 *>(s_acc + ILP * NT);        // [ILP*NI]
+    double2 *s_therm = s_red + ILP * NI;                                    // [NT]
 
     cg::cluster_group cl = cg::this_cluster();
     const int S = (int)cl.num_blocks();
@@ -184,9 +190,18 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     const double rc = sqrt(P.rc2);
     int2 *my_queue = s_queue + (tid >> 5) * ILP * 32;
 
-    float2 mx[NP], my[NP];
-    float U[ILP];
-    float sx[ILP], sy[ILP], cx[ILP], cy[ILP];
+    // This CTA finalises particles [rank*chunk, (rank+1)*chunk) of the tile
+    // (one per thread).  The FP64 thermal kick of that particle is computed
+    // now, so the FP64 pipe works while the other warps run the FP32 loop.
+    const int chunk = (NI * ILP + S - 1) / S;
+    int fin_e = -1;
+    if (tid < chunk) {
+        const int e = rank * chunk + tid;
+        if (e < NI * ILP && tile * NI * ILP + e < n) fin_e = e;
+    }
+    if (fin_e >= 0) s_therm[tid] = stage_thermal(P, tile * NI * ILP + fin_e);
+
+    float2 mx[NP], my[NP], nU[NP];  // nU = -(filter threshold), packed in pairs
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
         const int i = tile * NI * ILP + k * NI + t;
@@ -201,14 +216,13 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
             // the FP32 rounding of the expanded form and of the hi/lo split
             const double a2 = (double)A.x * A.x + (double)A.y * A.y;
             const double pr = sqrt(a2) + rc;
-            u = __double2float_ru(P.rc2 - a2 + 3.814697265625e-6 * pr * pr);
+            u = __double2float_ru(P.rc2 - a2 + 7.62939453125e-6 * pr * pr);
             cold = make_float4(B.x, B.y, __double2float_rn(P.coulomb * P.c.q[i]), __int_as_float(i));
         }
-        if (k & 1) { mx[k / 2].y = -2.0f * ax; my[k / 2].y = -2.0f * ay; }
-        else { mx[k / 2].x = -2.0f * ax; my[k / 2].x = -2.0f * ay; }
-        U[k] = u;
+        if (k & 1) { mx[k / 2].y = -2.0f * ax; my[k / 2].y = -2.0f * ay; nU[k / 2].y = -u; }
+        else { mx[k / 2].x = -2.0f * ax; my[k / 2].x = -2.0f * ay; nU[k / 2].x = -u; }
         if (g == 0) s_cold[k * NI + t] = cold;
-        sx[k] = sy[k] = cx[k] = cy[k] = 0.0f;
+        s_acc[k * NT + tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 
     const int per = ((n_pad + S - 1) / S + 63) & ~63;
@@ -233,14 +247,16 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
         ic.ii = __float_as_int(c4.w);
         const float xh = -0.5f * ((K & 1) ? mx[K / 2].y : mx[K / 2].x);
         const float yh = -0.5f * ((K & 1) ? my[K / 2].y : my[K / 2].x);
-        while (__any_sync(0xffffffffu, mask != 0u)) {
-            if (mask) {
+        if (mask) {
+            float4 acc = s_acc[K * NT + tid];
+            do {
                 const int e = __ffs(mask) - 1;
                 mask &= mask - 1u;
                 const int jj = my_queue[K * 32 + e].x;
-                precise_pair(P, E, b, xh, yh, ic, s_pa[jj], s_pb[jj], jt + jj, sx[K], sy[K],
-                             cx[K], cy[K]);
-            }
+                precise_pair(P, E, b, xh, yh, ic, s_pa[jj], s_pb[jj], jt + jj, acc.x, acc.y,
+                             acc.z, acc.w);
+            } while (mask);
+            s_acc[K * NT + tid] = acc;
         }
         __syncwarp();
         qn[K] = 0;
@@ -258,18 +274,19 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
         for (int jj = g; jj < cnt; jj += G) {
             const float4 A = s_pa[jj];
             const float2 X = make_float2(A.x, A.x), Y = make_float2(A.y, A.y), Bv = make_float2(A.z, A.z);
-            float2 r2[NP];
-            bool hit = false;
+            // d = |p_j|^2 - 2 p_i.p_j - threshold_i: the pair passes iff d < 0
+            float2 d[NP];
+            uint32_t sgn = 0u;
 #pragma unroll
             for (int p = 0; p < NP; p++) {
-                r2[p] = __ffma2_rn(mx[p], X, __ffma2_rn(my[p], Y, Bv));
-                hit |= (r2[p].x < U[2 * p]) | (r2[p].y < U[2 * p + 1]);
+                d[p] = __ffma2_rn(mx[p], X, __ffma2_rn(my[p], Y, __fadd2_rn(Bv, nU[p])));
+                sgn |= __float_as_uint(d[p].x) | __float_as_uint(d[p].y);
             }
-            if (__any_sync(0xffffffffu, hit)) {
+            if (__any_sync(0xffffffffu, (int)sgn < 0)) {
                 static_for<ILP>([&](auto kc) {
                     constexpr int k = decltype(kc)::value;
-                    const float rk = (k & 1) ? r2[k / 2].y : r2[k / 2].x;
-                    const uint32_t bal = __ballot_sync(0xffffffffu, rk < U[k]);
+                    const float dk = (k & 1) ? d[k / 2].y : d[k / 2].x;
+                    const uint32_t bal = __ballot_sync(0xffffffffu, (int)__float_as_uint(dk) < 0);
                     if (bal) {
                         if (lane == 0) my_queue[k * 32 + qn[k]] = make_int2(jj, (int)bal);
                         if (++qn[k] == 32) flush(kc, jt);
@@ -283,33 +300,30 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
         });
     }
 
-    // combine the G groups (fixed order, FP64), then the S cluster ranks
-#pragma unroll
-    for (int k = 0; k < ILP; k++)
-        s_red[g * ILP * NI + k * NI + t] =
-            make_double2((double)sx[k] - (double)cx[k], (double)sy[k] - (double)cy[k]);
+    // combine the G groups (fixed order, FP64; Kahan sum = s - c), then the
+    // S cluster ranks
     __syncthreads();
     for (int e = tid; e < ILP * NI; e += NT) {
-        double fx = s_red[e].x, fy = s_red[e].y;
+        const int k = e / NI, tt = e % NI;
+        double fx = 0.0, fy = 0.0;
 #pragma unroll
-        for (int gg = 1; gg < G; gg++) {
-            fx += s_red[gg * ILP * NI + e].x;
-            fy += s_red[gg * ILP * NI + e].y;
+        for (int gg = 0; gg < G; gg++) {
+            const float4 v = s_acc[k * NT + gg * NI + tt];
+            fx += (double)v.x - (double)v.z;
+            fy += (double)v.y - (double)v.w;
         }
         s_red[e] = make_double2(fx, fy);
     }
     cl.sync();
-    for (int e = rank * NT + tid; e < NI * ILP; e += NT * S) {
-        const int i = tile * NI * ILP + e;
-        if (i < n) {
-            double fx = 0.0, fy = 0.0;
-            for (int r = 0; r < S; r++) {
-                const double2 v = *cl.map_shared_rank(s_red + e, r);
-                fx += v.x;
-                fy += v.y;
-            }
-            stage_epilogue(P, i, fx, fy);
+    if (fin_e >= 0) {
+        const int i = tile * NI * ILP + fin_e;
+        double fx = 0.0, fy = 0.0;
+        for (int r = 0; r < S; r++) {
+            const double2 v = *cl.map_shared_rank(s_red + fin_e, r);
+            fx += v.x;
+            fy += v.y;
         }
+        stage_epilogue(P, i, fx, fy, s_therm[tid]);
     }
     stage_step_advance(P);
     cl.sync();
@@ -453,7 +467,7 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp64(const StageParams P
                 sxx = __dadd_rn(sxx, v.x);
                 syy = __dadd_rn(syy, v.y);
             }
-            stage_epilogue(P, i, sxx, syy);
+            stage_epilogue(P, i, sxx, syy, stage_thermal(P, i));
         }
     }
     stage_step_advance(P);
