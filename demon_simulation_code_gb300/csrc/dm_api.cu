@@ -189,8 +189,8 @@ int ensure_kernel_attrs(dm_ctx *ctx) {
 // co-resident clusters of size S (the device's own count, GPC packing
 // included) the tiles run in ceil(ntiles / X) cluster waves, and within a
 // wave the busiest SM holds ceil(CTAs_in_wave / num_sms) CTAs.  Cost =
-// sum over waves of that count / S; the smallest S within 2% of the best wins
-// (fewer partial sums).
+// sum over waves of that count / S; on ties (within 2%) the larger S wins:
+// more co-resident CTAs hide latency better, which the model ignores.
 int pick_split(dm_ctx *ctx, int precision, int n, int n_pad, int *out) {
     const KernelShape k = shape_of(precision);
     const int ntiles = (n + k.tile - 1) / k.tile;
@@ -220,8 +220,8 @@ int pick_split(dm_ctx *ctx, int precision, int n, int n_pad, int *out) {
             const int in_wave = std::min(left, nc) * S;
             cost += (double)((in_wave + ctx->num_sms - 1) / ctx->num_sms) / S;
         }
-        if (cost < best_cost * 0.98) {
-            best_cost = cost;
+        if (cost <= best_cost * 1.02) {
+            best_cost = std::min(best_cost, cost);
             best_s = S;
         }
     }

@@ -228,16 +228,17 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     const int per = ((n_pad + S - 1) / S + 63) & ~63;
     const int j0 = rank * per;
     const int j1 = min(n_pad, j0 + per);
-    int qn[ILP];
-#pragma unroll
-    for (int k = 0; k < ILP; k++) qn[k] = 0;
+    // queue fill per slot, 8 bits per slot (warp-uniform)
+    static_assert(ILP <= 4, "queue counts are packed in one 32-bit word");
+    uint32_t qn = 0u;
     __syncthreads();  // s_cold complete
 
     // Run the precise path on the queued entries of slot K, then empty it.
     auto flush = [&](auto kc, int jt) {
         constexpr int K = decltype(kc)::value;
         __syncwarp();
-        const int2 ent = (lane < qn[K]) ? my_queue[K * 32 + lane] : make_int2(0, 0);
+        const int fill = (int)((qn >> (8 * K)) & 0xFFu);
+        const int2 ent = (lane < fill) ? my_queue[K * 32 + lane] : make_int2(0, 0);
         uint32_t mask = warp_transpose32((uint32_t)ent.y);
         const float4 c4 = s_cold[K * NI + t];
         PairCtx ic;
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
             s_acc[K * NT + tid] = acc;
         }
         __syncwarp();
-        qn[K] = 0;
+        qn &= ~(0xFFu << (8 * K));
     };
 
     for (int jt = j0; jt < j1; jt += JT) {
@@ -270,33 +271,50 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
             s_pb[e] = pb[jt + e];
         }
         __syncthreads();
-#pragma unroll 2
-        for (int jj = g; jj < cnt; jj += G) {
-            const float4 A = s_pa[jj];
-            const float2 X = make_float2(A.x, A.x), Y = make_float2(A.y, A.y), Bv = make_float2(A.z, A.z);
-            // d = |p_j|^2 - 2 p_i.p_j - threshold_i: the pair passes iff d < 0
-            float2 d[NP];
-            uint32_t sgn = 0u;
+        // JU j per vote: JU independent load/FMA chains between branches
+        constexpr int JU = 4;
+        const int cnt_g = (cnt - g + G - 1) / G;  // j of this group in the tile
+        for (int q0 = 0; q0 < cnt_g; q0 += JU) {
+            float2 d[JU][NP];
+            uint32_t sgn[JU];
 #pragma unroll
-            for (int p = 0; p < NP; p++) {
-                d[p] = __ffma2_rn(mx[p], X, __ffma2_rn(my[p], Y, __fadd2_rn(Bv, nU[p])));
-                sgn |= __float_as_uint(d[p].x) | __float_as_uint(d[p].y);
+            for (int u = 0; u < JU; u++) {
+                const int jj = g + (q0 + u) * G;
+                // past the end: a padding j (never passes the filter)
+                const float4 A = (q0 + u < cnt_g) ? s_pa[jj] : make_float4(kPadPosition, kPadPosition, INFINITY, 0.0f);
+                const float2 X = make_float2(A.x, A.x), Y = make_float2(A.y, A.y),
+                             Bv = make_float2(A.z, A.z);
+                // d = |p_j|^2 - 2 p_i.p_j - threshold_i: the pair passes iff d < 0
+                sgn[u] = 0u;
+#pragma unroll
+                for (int p = 0; p < NP; p++) {
+                    d[u][p] = __ffma2_rn(mx[p], X, __ffma2_rn(my[p], Y, __fadd2_rn(Bv, nU[p])));
+                    sgn[u] |= __float_as_uint(d[u][p].x) | __float_as_uint(d[u][p].y);
+                }
             }
-            if (__any_sync(0xffffffffu, (int)sgn < 0)) {
-                static_for<ILP>([&](auto kc) {
-                    constexpr int k = decltype(kc)::value;
-                    const float dk = (k & 1) ? d[k / 2].y : d[k / 2].x;
-                    const uint32_t bal = __ballot_sync(0xffffffffu, (int)__float_as_uint(dk) < 0);
-                    if (bal) {
-                        if (lane == 0) my_queue[k * 32 + qn[k]] = make_int2(jj, (int)bal);
-                        if (++qn[k] == 32) flush(kc, jt);
+            if (__any_sync(0xffffffffu, (int)(sgn[0] | sgn[1] | sgn[2] | sgn[3]) < 0)) {
+#pragma unroll
+                for (int u = 0; u < JU; u++) {
+                    if (__any_sync(0xffffffffu, (int)sgn[u] < 0)) {
+                        const int jj = g + (q0 + u) * G;
+                        static_for<ILP>([&](auto kc) {
+                            constexpr int k = decltype(kc)::value;
+                            const float dk = (k & 1) ? d[u][k / 2].y : d[u][k / 2].x;
+                            const uint32_t bal = __ballot_sync(0xffffffffu, (int)__float_as_uint(dk) < 0);
+                            if (bal) {
+                                const int fill = (int)((qn >> (8 * k)) & 0xFFu);
+                                if (lane == 0) my_queue[k * 32 + fill] = make_int2(jj, (int)bal);
+                                qn += 1u << (8 * k);
+                                if (fill == 31) flush(kc, jt);
+                            }
+                        });
                     }
-                });
+                }
             }
         }
         // the queued j index into this tile: drain before it is overwritten
         static_for<ILP>([&](auto kc) {
-            if (qn[decltype(kc)::value]) flush(kc, jt);
+            if ((qn >> (8 * decltype(kc)::value)) & 0xFFu) flush(kc, jt);
         });
     }
 
