@@ -469,6 +469,8 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->n = n;
     c->n_pad = (n + 63) & ~63;
     c->coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);
+    c->d.coulomb = c->coulomb;
+    c->d.rc2 = (10.0 / 2e4) * (10.0 / 2e4);  // default kappa until set_forces
     const size_t nd = align256((size_t)c->n_pad * sizeof(double));
     const size_t nf4 = align256((size_t)c->n_pad * sizeof(float4));
     const size_t total = nd * (6 + 2 + 8 + 4 + 2) + nf4 * 4 + 1024;
@@ -591,7 +593,12 @@ int dm_cloud_set_forces(dm_cloud *c, const dm_force_params *p) {
     if (p->thermal_mode != 0 && p->thermal_mode != 1)
         return ctx->fail(DM_ERR_ARG, "dm_cloud_set_forces: thermal_mode must be 0 or 1");
     std::memcpy(&c->f, p, sizeof(ForceParams));
+    c->d.rc2 = (p->shielding > 0.0) ? (10.0 / p->shielding) * (10.0 / p->shielding) : 0.0;
     c->drop_graphs();
+    // the stage buffers carry a per-particle filter bound that depends on kappa
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
+    DM_CUDA(ctx, cudaGetLastError());
     return DM_OK;
 }
 

@@ -10,7 +10,10 @@
 //                    epilogue writes the next stage's positions into b^1:
 //                      px[b], py[b]  FP64 (CacheOperator's xCache/yCache)
 //                      pa[b] = (xh, yh, xh^2+yh^2, (float)q)  float4
-//                      pb[b] = (xl, yl, 0, 0)                  float4
+//                      pb[b] = (xl, yl, -threshold, C*q)      float4
+//                    (threshold = the FP32 pair filter's bound, see
+//                    filter_threshold; computed once per particle here
+//                    instead of in every CTA that reads the particle)
 //                    with x = xh + xl exactly to 48 bits (two-float form).
 //   padding          particles n..n_pad-1 sit at 1e18 m with q = 0, so the
 //                    cutoff test never selects them.
@@ -46,6 +49,8 @@ struct CloudDev {
     float4 *pa[2], *pb[2];
     unsigned long long *step_ctr;  // [2], see stage_step_index()
     int *err;                      // device error flags
+    double rc2;                    // (10/kappa)^2 of the current force parameters
+    double coulomb;                // 1/(4 pi eps0)
 };
 
 enum StageMode : int { kModeStep = 0, kModeForceOnly = 1 };
@@ -132,6 +137,18 @@ __device__ __forceinline__ void split2(double x, float &hi, float &lo) {
     lo = __double2float_rn(__dsub_rn(x, (double)hi));
 }
 
+// Bound of the FP32 pair filter for particle i at hi position (xh, yh):
+// the filter passes pair (i, j) iff |p_j|^2 - 2 p_i.p_j < rc^2 - |p_i|^2 +
+// margin, evaluated in FP32 on the hi parts.  The margin 2^-17 (|p_i| + rc)^2
+// is ~10x the worst FP32 rounding of that expanded form plus the hi/lo split
+// error for any pair within rc of i, so no pair the reference keeps is
+// filtered out.  Rounded up.
+__device__ __forceinline__ float filter_threshold(float xh, float yh, double rc2) {
+    const double a2 = (double)xh * xh + (double)yh * yh;
+    const double pr = sqrt(a2) + sqrt(rc2);
+    return __double2float_ru(rc2 - a2 + 7.62939453125e-6 * pr * pr);
+}
+
 __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, int i,
                                                      double xs, double ys) {
     c.px[b][i] = xs;
@@ -139,8 +156,10 @@ __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, i
     float xh, xl, yh, yl;
     split2(xs, xh, xl);
     split2(ys, yh, yl);
-    c.pa[b][i] = make_float4(xh, yh, fmaf(yh, yh, xh * xh), __double2float_rn(c.q[i]));
-    c.pb[b][i] = make_float4(xl, yl, 0.0f, 0.0f);
+    const double q = c.q[i];
+    c.pa[b][i] = make_float4(xh, yh, fmaf(yh, yh, xh * xh), __double2float_rn(q));
+    c.pb[b][i] = make_float4(xl, yl, -filter_threshold(xh, yh, c.rc2),
+                             __double2float_rn(c.coulomb * q));
 }
 
 // Reference cutoff decision for one pair, bit for bit:

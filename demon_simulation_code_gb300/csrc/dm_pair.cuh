@@ -187,7 +187,6 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     const int b = (st - 1) & 1;
     const float4 *__restrict__ pa = P.c.pa[b];
     const float4 *__restrict__ pb = P.c.pb[b];
-    const double rc = sqrt(P.rc2);
     int2 *my_queue = s_queue + (tid >> 5) * ILP * 32;
 
     // This CTA finalises particles [rank*chunk, (rank+1)*chunk) of the tile
@@ -205,22 +204,18 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
         const int i = tile * NI * ILP + k * NI + t;
-        float ax = 0.0f, ay = 0.0f, u = -INFINITY;
+        float ax = 0.0f, ay = 0.0f, nu = INFINITY;
         float4 cold = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         if (i < n) {
             const float4 A = pa[i];
             const float4 B = pb[i];
             ax = A.x;
             ay = A.y;
-            // filter threshold: rc^2 - |p_i|^2 + margin; the margin covers
-            // the FP32 rounding of the expanded form and of the hi/lo split
-            const double a2 = (double)A.x * A.x + (double)A.y * A.y;
-            const double pr = sqrt(a2) + rc;
-            u = __double2float_ru(P.rc2 - a2 + 7.62939453125e-6 * pr * pr);
-            cold = make_float4(B.x, B.y, __double2float_rn(P.coulomb * P.c.q[i]), __int_as_float(i));
+            nu = B.z;
+            cold = make_float4(B.x, B.y, B.w, __int_as_float(i));
         }
-        if (k & 1) { mx[k / 2].y = -2.0f * ax; my[k / 2].y = -2.0f * ay; nU[k / 2].y = -u; }
-        else { mx[k / 2].x = -2.0f * ax; my[k / 2].x = -2.0f * ay; nU[k / 2].x = -u; }
+        if (k & 1) { mx[k / 2].y = -2.0f * ax; my[k / 2].y = -2.0f * ay; nU[k / 2].y = nu; }
+        else { mx[k / 2].x = -2.0f * ax; my[k / 2].x = -2.0f * ay; nU[k / 2].x = nu; }
         if (g == 0) s_cold[k * NI + t] = cold;
         s_acc[k * NT + tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
