@@ -88,13 +88,15 @@ struct PairTuning {
 // ---------------------------------------------------------------------------
 template <int NI, int G, int ILP>
 struct Fp32cSmem {
+    static constexpr int pad = 4 * G;  // tile padding so 4-j chunks never run past it
     static constexpr size_t cold = (size_t)ILP * NI * sizeof(float4);
     static constexpr size_t queue = (size_t)G * (NI / 32) * ILP * 32 * sizeof(int2);
     static constexpr size_t acc = (size_t)ILP * NI * G * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * NI * sizeof(double2);
     static constexpr size_t therm = (size_t)NI * G * sizeof(double2);
     static size_t bytes(int jt) {
-        return (size_t)jt * 2 * sizeof(float4) + cold + queue + acc + red + therm;
+        return (size_t)(jt + pad) * (3 * sizeof(float) + sizeof(float4)) + cold + queue + acc + red +
+               therm;
     }
 };
 
@@ -163,13 +165,16 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
 template <int NI, int G, int ILP, int JT>
 __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
     constexpr int NT = NI * G;
-    constexpr int NP = ILP / 2;
     constexpr int NW = NT / 32;
-    static_assert(ILP % 2 == 0 && NI % 32 == 0 && JT % G == 0, "shape");
+    constexpr int JP = JT + Fp32cSmem<NI, G, ILP>::pad;
+    static_assert(NI % 32 == 0 && JT % (4 * G) == 0 && ILP <= 4, "shape");
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float4 *s_pa = reinterpret_cast<float4 *>(smem_raw);
-    float4 *s_pb = s_pa + JT;
-    float4 *s_cold = s_pb + JT;                                   // [ILP][NI]
+    // j tile, structure of arrays so one 16-byte load gives 4 consecutive j
+    float *s_x = reinterpret_cast<float *>(smem_raw);  // xh   [JP]
+    float *s_y = s_x + JP;                              // yh   [JP]
+    float *s_b = s_y + JP;                              // xh^2+yh^2 [JP]
+    float4 *s_pb = reinterpret_cast<float4 *>(s_b + JP);  // (xl, yl, q, -) [JP]
+    float4 *s_cold = s_pb + JP;                                   // [ILP][NI]
     int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * NI);  // [NW][ILP][32]
     float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);  // [ILP][NT] Kahan sums
     double2 *s_red = reinterpret_cast<double2 *>(s_acc + ILP * NT);        // [ILP*NI]
@@ -200,7 +205,9 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     }
     if (fin_e >= 0) s_therm[tid] = stage_thermal(P, tile * NI * ILP + fin_e);
 
-    float2 mx[NP], my[NP], nU[NP];  // nU = -(filter threshold), packed in pairs
+    // i side, duplicated into both halves of a packed pair: the packed FMAs
+    // below evaluate two consecutive j against one i
+    float2 mx2[ILP], my2[ILP], nu2[ILP];
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
         const int i = tile * NI * ILP + k * NI + t;
@@ -214,8 +221,9 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
             nu = B.z;
             cold = make_float4(B.x, B.y, B.w, __int_as_float(i));
         }
-        if (k & 1) { mx[k / 2].y = -2.0f * ax; my[k / 2].y = -2.0f * ay; nU[k / 2].y = nu; }
-        else { mx[k / 2].x = -2.0f * ax; my[k / 2].x = -2.0f * ay; nU[k / 2].x = nu; }
+        mx2[k] = make_float2(-2.0f * ax, -2.0f * ax);
+        my2[k] = make_float2(-2.0f * ay, -2.0f * ay);
+        nu2[k] = make_float2(nu, nu);
         if (g == 0) s_cold[k * NI + t] = cold;
         s_acc[k * NT + tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
@@ -224,7 +232,6 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     const int j0 = rank * per;
     const int j1 = min(n_pad, j0 + per);
     // queue fill per slot, 8 bits per slot (warp-uniform)
-    static_assert(ILP <= 4, "queue counts are packed in one 32-bit word");
     uint32_t qn = 0u;
     __syncthreads();  // s_cold complete
 
@@ -235,22 +242,22 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
         const int fill = (int)((qn >> (8 * K)) & 0xFFu);
         const int2 ent = (lane < fill) ? my_queue[K * 32 + lane] : make_int2(0, 0);
         uint32_t mask = warp_transpose32((uint32_t)ent.y);
-        const float4 c4 = s_cold[K * NI + t];
-        PairCtx ic;
-        ic.xl = c4.x;
-        ic.yl = c4.y;
-        ic.qc = c4.z;
-        ic.ii = __float_as_int(c4.w);
-        const float xh = -0.5f * ((K & 1) ? mx[K / 2].y : mx[K / 2].x);
-        const float yh = -0.5f * ((K & 1) ? my[K / 2].y : my[K / 2].x);
         if (mask) {
+            const float4 c4 = s_cold[K * NI + t];
+            PairCtx ic;
+            ic.xl = c4.x;
+            ic.yl = c4.y;
+            ic.qc = c4.z;
+            ic.ii = __float_as_int(c4.w);
+            const float xh = -0.5f * mx2[K].x, yh = -0.5f * my2[K].x;
             float4 acc = s_acc[K * NT + tid];
             do {
                 const int e = __ffs(mask) - 1;
                 mask &= mask - 1u;
                 const int jj = my_queue[K * 32 + e].x;
-                precise_pair(P, E, b, xh, yh, ic, s_pa[jj], s_pb[jj], jt + jj, acc.x, acc.y,
-                             acc.z, acc.w);
+                const float4 Aj = make_float4(s_x[jj], s_y[jj], 0.0f, s_pb[jj].z);
+                precise_pair(P, E, b, xh, yh, ic, Aj, s_pb[jj], jt + jj, acc.x, acc.y, acc.z,
+                             acc.w);
             } while (mask);
             s_acc[K * NT + tid] = acc;
         }
@@ -260,50 +267,60 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
 
     for (int jt = j0; jt < j1; jt += JT) {
         const int cnt = min(JT, j1 - jt);
+        const int nch = (cnt + 3) >> 2;          // 4-j chunks in this tile
         __syncthreads();
-        for (int e = tid; e < cnt; e += NT) {
-            s_pa[e] = pa[jt + e];
-            s_pb[e] = pb[jt + e];
+        for (int e = tid; e < 4 * ((nch + G - 1) / G) * G; e += NT) {
+            if (e < cnt) {
+                const float4 A = pa[jt + e];
+                s_x[e] = A.x;
+                s_y[e] = A.y;
+                s_b[e] = A.z;
+                const float4 B = pb[jt + e];
+                s_pb[e] = make_float4(B.x, B.y, A.w, 0.0f);
+            } else {  // padding j: never passes the filter
+                s_x[e] = kPadPosition;
+                s_y[e] = kPadPosition;
+                s_b[e] = INFINITY;
+                s_pb[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
         }
         __syncthreads();
-        // JU j per vote: JU independent load/FMA chains between branches
-        constexpr int JU = 4;
-        const int cnt_g = (cnt - g + G - 1) / G;  // j of this group in the tile
-        for (int q0 = 0; q0 < cnt_g; q0 += JU) {
-            float2 d[JU][NP];
-            uint32_t sgn[JU];
+        const float4 *x4 = reinterpret_cast<const float4 *>(s_x);
+        const float4 *y4 = reinterpret_cast<const float4 *>(s_y);
+        const float4 *b4 = reinterpret_cast<const float4 *>(s_b);
+        for (int c = g; c < nch; c += G) {
+            const float4 X = x4[c], Y = y4[c], Bq = b4[c];
+            const float2 X01 = make_float2(X.x, X.y), X23 = make_float2(X.z, X.w);
+            const float2 Y01 = make_float2(Y.x, Y.y), Y23 = make_float2(Y.z, Y.w);
+            const float2 B01 = make_float2(Bq.x, Bq.y), B23 = make_float2(Bq.z, Bq.w);
+            // d = |p_j|^2 - 2 p_i.p_j - threshold_i: pair (i, j) passes iff d < 0
+            uint32_t sgn = 0u;
 #pragma unroll
-            for (int u = 0; u < JU; u++) {
-                const int jj = g + (q0 + u) * G;
-                // past the end: a padding j (never passes the filter)
-                const float4 A = (q0 + u < cnt_g) ? s_pa[jj] : make_float4(kPadPosition, kPadPosition, INFINITY, 0.0f);
-                const float2 X = make_float2(A.x, A.x), Y = make_float2(A.y, A.y),
-                             Bv = make_float2(A.z, A.z);
-                // d = |p_j|^2 - 2 p_i.p_j - threshold_i: the pair passes iff d < 0
-                sgn[u] = 0u;
-#pragma unroll
-                for (int p = 0; p < NP; p++) {
-                    d[u][p] = __ffma2_rn(mx[p], X, __ffma2_rn(my[p], Y, __fadd2_rn(Bv, nU[p])));
-                    sgn[u] |= __float_as_uint(d[u][p].x) | __float_as_uint(d[u][p].y);
-                }
+            for (int k = 0; k < ILP; k++) {
+                const float2 d01 = __ffma2_rn(mx2[k], X01, __ffma2_rn(my2[k], Y01, __fadd2_rn(B01, nu2[k])));
+                const float2 d23 = __ffma2_rn(mx2[k], X23, __ffma2_rn(my2[k], Y23, __fadd2_rn(B23, nu2[k])));
+                sgn |= __float_as_uint(d01.x) | __float_as_uint(d01.y) | __float_as_uint(d23.x) |
+                       __float_as_uint(d23.y);
             }
-            if (__any_sync(0xffffffffu, (int)(sgn[0] | sgn[1] | sgn[2] | sgn[3]) < 0)) {
+            if (__any_sync(0xffffffffu, (int)sgn < 0)) {
+                // rare: recompute per j (scalar FMA rounds exactly like the
+                // packed one), ballot per slot, queue the hits
+                const float xs[4] = {X.x, X.y, X.z, X.w};
+                const float ys[4] = {Y.x, Y.y, Y.z, Y.w};
+                const float bs[4] = {Bq.x, Bq.y, Bq.z, Bq.w};
 #pragma unroll
-                for (int u = 0; u < JU; u++) {
-                    if (__any_sync(0xffffffffu, (int)sgn[u] < 0)) {
-                        const int jj = g + (q0 + u) * G;
-                        static_for<ILP>([&](auto kc) {
-                            constexpr int k = decltype(kc)::value;
-                            const float dk = (k & 1) ? d[u][k / 2].y : d[u][k / 2].x;
-                            const uint32_t bal = __ballot_sync(0xffffffffu, (int)__float_as_uint(dk) < 0);
-                            if (bal) {
-                                const int fill = (int)((qn >> (8 * k)) & 0xFFu);
-                                if (lane == 0) my_queue[k * 32 + fill] = make_int2(jj, (int)bal);
-                                qn += 1u << (8 * k);
-                                if (fill == 31) flush(kc, jt);
-                            }
-                        });
-                    }
+                for (int u = 0; u < 4; u++) {
+                    static_for<ILP>([&](auto kc) {
+                        constexpr int k = decltype(kc)::value;
+                        const float dk = fmaf(mx2[k].x, xs[u], fmaf(my2[k].x, ys[u], bs[u] + nu2[k].x));
+                        const uint32_t bal = __ballot_sync(0xffffffffu, (int)__float_as_uint(dk) < 0);
+                        if (bal) {
+                            const int fill = (int)((qn >> (8 * k)) & 0xFFu);
+                            if (lane == 0) my_queue[k * 32 + fill] = make_int2(4 * c + u, (int)bal);
+                            qn += 1u << (8 * k);
+                            if (fill == 31) flush(kc, jt);
+                        }
+                    });
                 }
             }
         }
