@@ -79,6 +79,7 @@ SIGNATURES = {
     "dm_cloud_modify_timestep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                                 ctypes.POINTER(ctypes.c_float), _dp]),
     "dm_cloud_diagnostics": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "dm_cloud_set_reorder_interval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dm_cloud_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dm_cloud_get_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "dm_diagnostics_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,

@@ -158,6 +158,9 @@ class DeviceCloud:
         self._chk(self.lib.dm_cloud_diagnostics(self.h, ptr(out)))
         return out
 
+    def set_reorder_interval(self, steps: int):
+        self._chk(self.lib.dm_cloud_set_reorder_interval(self.h, int(steps)))
+
     def set_step_counter(self, step: int):
         self._chk(self.lib.dm_cloud_set_step_counter(self.h, int(step)))
 

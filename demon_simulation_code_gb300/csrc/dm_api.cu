@@ -18,6 +18,7 @@
 #include "../../include/demon_gb300.h"
 #include "dm_misc.cuh"
 #include "dm_pair.cuh"
+#include "dm_sort.cuh"
 
 using namespace dm;
 
@@ -81,6 +82,11 @@ struct dm_cloud {
     unsigned int *d_min = nullptr;
     float *d_dmin = nullptr;
     int split[2] = {0, 0};  // cluster size per precision (0 = not chosen yet)
+    SortScratch sort{};
+    int sort_blocks = 0;
+    int reorder_interval = 4;   // steps between Morton re-sorts (0 = never)
+    bool order_dirty = true;    // re-sort before the next step
+    unsigned long long host_steps = 0;  // RK4 steps enqueued so far
     std::map<GraphKey, cudaGraphExec_t> graphs;
     cudaStream_t graph_stream = nullptr;  // stream the graphs were built for
 
@@ -279,12 +285,59 @@ int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, con
     return DM_OK;
 }
 
+// Charges and masses back to the caller's order (before orig is reset).
+int gather_to_caller_order(dm_cloud *c) {
+    dm_ctx *ctx = c->ctx;
+    double **st = c->sort.stage;
+    const size_t bytes = (size_t)c->n * sizeof(double);
+    scatter_to_caller<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(
+        c->d.orig, c->n, c->d.q, c->d.m, nullptr, nullptr, st[4], st[5], nullptr, nullptr);
+    DM_CUDA(ctx, cudaGetLastError());
+    DM_CUDA(ctx, cudaMemcpyAsync(c->d.q, st[4], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(c->d.m, st[5], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return DM_OK;
+}
+
+// Puts the cloud in Morton order (dm_sort.cuh); graph-capturable.
+int reorder(dm_cloud *c) {
+    dm_ctx *ctx = c->ctx;
+    cudaStream_t s = ctx->stream;
+    const int n = c->n;
+    const int grid = (n + 255) / 256;
+    SortScratch &z = c->sort;
+    DM_CUDA(ctx, cudaMemsetAsync(z.bbox, 0xFF, 2 * sizeof(unsigned long long), s));
+    DM_CUDA(ctx, cudaMemsetAsync(z.bbox + 2, 0x00, 2 * sizeof(unsigned long long), s));
+    sort_bbox<<<std::min(grid, ctx->num_sms), 256, 0, s>>>(c->d.x, c->d.y, n, z.bbox);
+    sort_keys<<<grid, 256, 0, s>>>(c->d.x, c->d.y, n, z.bbox, z.keys[0], z.vals[0]);
+    int cur = 0;
+    for (int shift = 0; shift < kSortBits; shift += kSortDigitBits) {
+        radix_hist<<<c->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], n, shift, z.hist);
+        radix_scan<<<1, 1024, 0, s>>>(z.hist, kSortBuckets * c->sort_blocks);
+        radix_scatter<<<c->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], z.vals[cur], z.keys[cur ^ 1],
+                                                               z.vals[cur ^ 1], n, shift, z.hist);
+        cur ^= 1;
+    }
+    permute_gather<<<grid, 256, 0, s>>>(c->d, z.vals[cur], z);
+    permute_commit<<<grid, 256, 0, s>>>(c->d, z);
+    init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
+    DM_CUDA(ctx, cudaGetLastError());
+    c->order_dirty = false;
+    return DM_OK;
+}
+
 int enqueue_steps(dm_cloud *c, int nsteps, double dt, int precision) {
-    for (int s = 0; s < nsteps; s++)
+    for (int s = 0; s < nsteps; s++) {
+        if (c->order_dirty ||
+            (c->reorder_interval > 0 && c->host_steps % (unsigned)c->reorder_interval == 0)) {
+            int rc = reorder(c);
+            if (rc) return rc;
+        }
         for (int st = 1; st <= 4; st++) {
             int rc = launch_stage(c, precision, st, kModeStep, dt, nullptr);
             if (rc) return rc;
         }
+        c->host_steps++;
+    }
     return DM_OK;
 }
 
@@ -295,13 +348,24 @@ int run_steps(dm_cloud *c, int nsteps, double dt, int precision) {
         c->drop_graphs();
         c->graph_stream = ctx->stream;
     }
+    // the captured step sequence re-sorts at fixed positions: align the
+    // host step counter and clear a pending re-sort first
+    while (nsteps > 0 && (c->order_dirty ||
+                          (c->reorder_interval > 0 && c->host_steps % kGraphSteps != 0))) {
+        int rc = enqueue_steps(c, 1, dt, precision);
+        if (rc) return rc;
+        nsteps--;
+    }
+    if (nsteps < kGraphSteps) return enqueue_steps(c, nsteps, dt, precision);
     const GraphKey key{precision, kGraphSteps, dt};
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
         cudaGraph_t g = nullptr;
+        const unsigned long long saved = c->host_steps;
         DM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         int rc = enqueue_steps(c, kGraphSteps, dt, precision);
         cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+        c->host_steps = saved;  // capture recorded the steps, it did not run them
         if (rc) {
             if (g) cudaGraphDestroy(g);
             return rc;
@@ -314,7 +378,10 @@ int run_steps(dm_cloud *c, int nsteps, double dt, int precision) {
         it = c->graphs.emplace(key, ge).first;
     }
     const int reps = nsteps / kGraphSteps;
-    for (int r = 0; r < reps; r++) DM_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
+    for (int r = 0; r < reps; r++) {
+        DM_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
+        c->host_steps += kGraphSteps;
+    }
     return enqueue_steps(c, nsteps - reps * kGraphSteps, dt, precision);
 }
 
@@ -473,7 +540,10 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->d.rc2 = (10.0 / 2e4) * (10.0 / 2e4);  // default kappa until set_forces
     const size_t nd = align256((size_t)c->n_pad * sizeof(double));
     const size_t nf4 = align256((size_t)c->n_pad * sizeof(float4));
-    const size_t total = nd * (6 + 2 + 8 + 4 + 2) + nf4 * 4 + 1024;
+    const size_t ni = align256((size_t)c->n_pad * sizeof(int));
+    c->sort_blocks = (n + kSortPerBlock - 1) / kSortPerBlock;
+    const size_t nh = align256((size_t)kSortBuckets * c->sort_blocks * sizeof(uint32_t));
+    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ni * 6 + nh + 1024 + 256;
     cudaError_t e = cudaMalloc(&c->block, total);
     if (e != cudaSuccess) {
         delete c;
@@ -497,6 +567,16 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->d.err = (int *)p; p += 256;
     c->d_dt = (double *)p; p += 256;
     c->d_min = (unsigned int *)p; c->d_dmin = (float *)(p + 64); p += 256;
+    auto takeI = [&]() { int *r = (int *)p; p += ni; return r; };
+    c->d.orig = takeI();
+    c->sort.keys[0] = (uint32_t *)takeI();
+    c->sort.keys[1] = (uint32_t *)takeI();
+    c->sort.vals[0] = takeI();
+    c->sort.vals[1] = takeI();
+    c->sort.orig_stage = takeI();
+    for (int k = 0; k < 6; k++) c->sort.stage[k] = takeD();
+    c->sort.hist = (uint32_t *)p; p += nh;
+    c->sort.bbox = (unsigned long long *)p; p += 256;
     cudaStream_t s = ctx->stream;
     const size_t bytes = (size_t)n * sizeof(double);
     e = cudaMemsetAsync(c->block, 0, total, s);
@@ -507,6 +587,7 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.q, q, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->d.m, m, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
+        set_identity<<<(n + 255) / 256, 256, 0, s>>>(c->d.orig, n);
         init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
         e = cudaGetLastError();
     }
@@ -550,8 +631,13 @@ int dm_cloud_upload(dm_cloud *c, const double *x, const double *y, const double 
     DM_CUDA(ctx, cudaMemcpyAsync(c->d.y, y, bytes, cudaMemcpyHostToDevice, ctx->stream));
     DM_CUDA(ctx, cudaMemcpyAsync(c->d.vx, vx, bytes, cudaMemcpyHostToDevice, ctx->stream));
     DM_CUDA(ctx, cudaMemcpyAsync(c->d.vy, vy, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    // charges and masses stay; bring them back to the caller's order too
+    int rc = gather_to_caller_order(c);
+    if (rc) return rc;
+    set_identity<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->d.orig, c->n);
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
     DM_CUDA(ctx, cudaGetLastError());
+    c->order_dirty = true;
     return DM_OK;
 }
 
@@ -560,10 +646,14 @@ int dm_cloud_download(dm_cloud *c, double *x, double *y, double *vx, double *vy)
     dm_ctx *ctx = c->ctx;
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t bytes = (size_t)c->n * sizeof(double);
-    if (x) DM_CUDA(ctx, cudaMemcpyAsync(x, c->d.x, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, c->d.y, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, c->d.vx, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    if (vy) DM_CUDA(ctx, cudaMemcpyAsync(vy, c->d.vy, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    double **st = c->sort.stage;
+    scatter_to_caller<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(
+        c->d.orig, c->n, c->d.x, c->d.y, c->d.vx, c->d.vy, st[0], st[1], st[2], st[3]);
+    DM_CUDA(ctx, cudaGetLastError());
+    if (x) DM_CUDA(ctx, cudaMemcpyAsync(x, st[0], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, st[1], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, st[2], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vy) DM_CUDA(ctx, cudaMemcpyAsync(vy, st[3], bytes, cudaMemcpyDeviceToHost, ctx->stream));
     DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return check_device_errors(ctx, c);
 }
@@ -573,8 +663,12 @@ int dm_cloud_set_charge_mass(dm_cloud *c, const double *q, const double *m) {
     dm_ctx *ctx = c->ctx;
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t bytes = (size_t)c->n * sizeof(double);
-    if (q) DM_CUDA(ctx, cudaMemcpyAsync(c->d.q, q, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    if (m) DM_CUDA(ctx, cudaMemcpyAsync(c->d.m, m, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    double **st = c->sort.stage;
+    // caller order -> staging -> internal order
+    if (q) DM_CUDA(ctx, cudaMemcpyAsync(st[4], q, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (m) DM_CUDA(ctx, cudaMemcpyAsync(st[5], m, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    gather_from_caller<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(
+        c->d.orig, c->n, q ? st[4] : nullptr, m ? st[5] : nullptr, c->d.q, c->d.m);
     // the float charge copy lives in the stage buffers: refresh buffer 0
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
     DM_CUDA(ctx, cudaGetLastError());
@@ -653,7 +747,12 @@ int dm_cloud_modify_timestep(dm_cloud *c, double init_dt, float *min_dist, doubl
     const int nb = c->n / 4;
     const long long total = (long long)nb * (nb + 1) / 2;
     const int blocks = (int)std::min<long long>((total + 255) / 256, (long long)ctx->num_sms * 16);
-    checked_min_dist2<<<std::max(blocks, 1), 256, 0, ctx->stream>>>(c->d.x, c->d.y, nb, c->d_min);
+    // the checked pair pattern is defined on the caller's order
+    double **st = c->sort.stage;
+    scatter_to_caller<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(
+        c->d.orig, c->n, c->d.x, c->d.y, nullptr, nullptr, st[0], st[1], nullptr, nullptr);
+    DM_CUDA(ctx, cudaGetLastError());
+    checked_min_dist2<<<std::max(blocks, 1), 256, 0, ctx->stream>>>(st[0], st[1], nb, c->d_min);
     DM_CUDA(ctx, cudaGetLastError());
     adaptive_dt<<<1, 1, 0, ctx->stream>>>(c->d_min, init_dt, c->d_dt, c->d_dmin, c->d.err);
     DM_CUDA(ctx, cudaGetLastError());
@@ -715,6 +814,15 @@ int dm_cloud_diagnostics(dm_cloud *c, double out[5]) {
     for (int k = 0; k < 5; k++) out[k] = 0.0;
     for (int b = 0; b < blocks; b++)
         for (int k = 0; k < 5; k++) out[k] += h[(size_t)b * 5 + k];
+    return DM_OK;
+}
+
+int dm_cloud_set_reorder_interval(dm_cloud *c, int steps) {
+    if (!c) return DM_ERR_ARG;
+    if (steps < 0 || steps > kGraphSteps || (steps & (steps - 1)) != 0)
+        return c->ctx->fail(DM_ERR_ARG, "reorder interval must be 0 or a power of two <= %d", kGraphSteps);
+    c->reorder_interval = steps;
+    c->drop_graphs();
     return DM_OK;
 }
 

@@ -51,6 +51,7 @@ struct CloudDev {
     int *err;                      // device error flags
     double rc2;                    // (10/kappa)^2 of the current force parameters
     double coulomb;                // 1/(4 pi eps0)
+    int *orig;                     // caller's index of internal slot s (Morton order)
 };
 
 enum StageMode : int { kModeStep = 0, kModeForceOnly = 1 };
@@ -191,7 +192,7 @@ __device__ __forceinline__ double2 stage_thermal(const StageParams &P, int i) {
     double tx = 0.0, ty = 0.0;
     if (P.f.flags & kThermal) {
         const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
-        thermal_kick(P.f, (uint32_t)i, stage_step_index(P), s, tx, ty);
+        thermal_kick(P.f, (uint32_t)P.c.orig[i], stage_step_index(P), s, tx, ty);
     }
     return make_double2(tx, ty);
 }
@@ -229,9 +230,9 @@ __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, doub
         Fx = __dadd_rn(Fx, therm.x);
         Fy = __dadd_rn(Fy, therm.y);
     }
-    if (P.mode == kModeForceOnly) {
-        P.fx_out[i] = Fx;
-        P.fy_out[i] = Fy;
+    if (P.mode == kModeForceOnly) {  // outputs in the caller's order
+        P.fx_out[c.orig[i]] = Fx;
+        P.fy_out[c.orig[i]] = Fy;
         return;
     }
     const double dt = P.dt_dev ? *P.dt_dev : P.dt;

@@ -1,0 +1,225 @@
+// dm_sort.cuh -- spatial (Morton) ordering of a device-resident cloud.
+//
+// The all-pairs kernels test every pair, but their cost is decided per warp:
+// a warp runs the precise path for a group of j as soon as ONE of its lanes'
+// particles is within the cutoff.  With particles in input order a warp's
+// particles are spread over the whole cloud and nearly every j group wakes
+// it; in Morton order a warp's particles are a compact patch and only the j
+// near that patch do.  The cloud therefore lives in Morton order on the
+// device; `orig[s]` maps internal slot s back to the caller's particle index
+// (used for the thermal RNG counter, for downloads and for the adaptive-dt
+// pair pattern, all of which are defined on the caller's order).
+//
+// Sort: 24-bit Morton keys (12 bits per axis over the cloud's bounding box)
+// and a deterministic, stable LSD radix sort with 4-bit digits (per-block
+// digit histograms, one scan, stable scatter ranked with __match_any_sync).
+// No atomics decide any order; the result depends only on the positions.
+#pragma once
+
+#include "dm_device.cuh"
+
+namespace dm {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortPerBlock = 4 * kSortThreads;  // keys per block
+constexpr int kSortBits = 24;
+constexpr int kSortDigitBits = 4;
+constexpr int kSortBuckets = 1 << kSortDigitBits;
+
+struct SortScratch {
+    unsigned long long *bbox;  // [4]: ordered-bit min x, min y, max x, max y
+    uint32_t *keys[2];
+    int *vals[2];
+    uint32_t *hist;            // [kSortBuckets * nblocks]
+    double *stage[6];          // gather staging for x, y, vx, vy, q, m
+    int *orig_stage;
+};
+
+// Order-preserving map of a double to uint64 (for atomicMin/atomicMax).
+__device__ __forceinline__ unsigned long long ordered_bits(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_ordered_bits(unsigned long long o) {
+    const unsigned long long b = (o & 0x8000000000000000ull) ? (o & 0x7fffffffffffffffull) : ~o;
+    return __longlong_as_double((long long)b);
+}
+
+static __global__ void sort_bbox(const double *__restrict__ x, const double *__restrict__ y, int n,
+                                 unsigned long long *bbox) {
+    double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double a = x[i], b = y[i];
+        if (isfinite(a) && isfinite(b)) {
+            mnx = fmin(mnx, a); mxx = fmax(mxx, a);
+            mny = fmin(mny, b); mxy = fmax(mxy, b);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        mnx = fmin(mnx, __shfl_xor_sync(0xffffffffu, mnx, off));
+        mny = fmin(mny, __shfl_xor_sync(0xffffffffu, mny, off));
+        mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, off));
+        mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&bbox[0], ordered_bits(mnx));
+        atomicMin(&bbox[1], ordered_bits(mny));
+        atomicMax(&bbox[2], ordered_bits(mxx));
+        atomicMax(&bbox[3], ordered_bits(mxy));
+    }
+}
+
+// Spreads the low 12 bits of v to the even bit positions.
+__device__ __forceinline__ uint32_t spread_bits12(uint32_t v) {
+    v &= 0x00000FFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+static __global__ void sort_keys(const double *__restrict__ x, const double *__restrict__ y, int n,
+                                 const unsigned long long *bbox, uint32_t *keys, int *vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x0 = from_ordered_bits(bbox[0]), y0 = from_ordered_bits(bbox[1]);
+    const double x1 = from_ordered_bits(bbox[2]), y1 = from_ordered_bits(bbox[3]);
+    const double ext = fmax(x1 - x0, y1 - y0);
+    const double scale = (ext > 0.0 && isfinite(ext)) ? 4095.0 / ext : 0.0;
+    const double fx = (x[i] - x0) * scale, fy = (y[i] - y0) * scale;
+    const uint32_t qx = (fx > 0.0) ? (uint32_t)fmin(fx, 4095.0) : 0u;
+    const uint32_t qy = (fy > 0.0) ? (uint32_t)fmin(fy, 4095.0) : 0u;
+    keys[i] = spread_bits12(qx) | (spread_bits12(qy) << 1);
+    vals[i] = i;
+}
+
+static __global__ void __launch_bounds__(kSortThreads) radix_hist(const uint32_t *__restrict__ keys, int n,
+                                                                  int shift, uint32_t *hist) {
+    __shared__ uint32_t h[kSortBuckets];
+    if (threadIdx.x < kSortBuckets) h[threadIdx.x] = 0u;
+    __syncthreads();
+    for (int k = 0; k < 4; k++) {
+        const int e = blockIdx.x * kSortPerBlock + k * kSortThreads + threadIdx.x;
+        if (e < n) atomicAdd(&h[(keys[e] >> shift) & (kSortBuckets - 1)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < kSortBuckets) hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of len entries in one block of 1024 threads.
+static __global__ void __launch_bounds__(1024) radix_scan(uint32_t *hist, int len) {
+    __shared__ uint32_t part[1024];
+    const int per = (len + 1023) / 1024;
+    const int lo = threadIdx.x * per, hi = min(len, lo + per);
+    uint32_t s = 0;
+    for (int e = lo; e < hi; e++) s += hist[e];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const uint32_t v = (threadIdx.x >= off) ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;  // exclusive prefix of this segment
+    for (int e = lo; e < hi; e++) {
+        const uint32_t v = hist[e];
+        hist[e] = run;
+        run += v;
+    }
+}
+
+// Stable scatter: elements are ranked in index order (chunk, warp, lane).
+static __global__ void __launch_bounds__(kSortThreads) radix_scatter(
+    const uint32_t *__restrict__ kin, const int *__restrict__ vin, uint32_t *kout, int *vout, int n,
+    int shift, const uint32_t *__restrict__ hist) {
+    constexpr int NWARP = kSortThreads / 32;
+    __shared__ uint32_t base[kSortBuckets];
+    __shared__ uint32_t wcnt[NWARP][kSortBuckets];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < kSortBuckets) base[threadIdx.x] = hist[threadIdx.x * gridDim.x + blockIdx.x];
+    for (int k = 0; k < 4; k++) {
+        for (int e = threadIdx.x; e < NWARP * kSortBuckets; e += kSortThreads) (&wcnt[0][0])[e] = 0u;
+        __syncthreads();
+        const int e = blockIdx.x * kSortPerBlock + k * kSortThreads + threadIdx.x;
+        const bool valid = e < n;
+        const uint32_t key = valid ? kin[e] : 0u;
+        const int d = valid ? (int)((key >> shift) & (kSortBuckets - 1)) : kSortBuckets;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = base[d] + rank;
+            for (int w = 0; w < warp; w++) pos += wcnt[w][d];
+            kout[pos] = key;
+            vout[pos] = vin[e];
+        }
+        __syncthreads();
+        if (threadIdx.x < kSortBuckets) {
+            uint32_t add = 0;
+            for (int w = 0; w < NWARP; w++) add += wcnt[w][threadIdx.x];
+            base[threadIdx.x] += add;
+        }
+        __syncthreads();
+    }
+}
+
+// new slot s takes old slot perm[s]: gather into staging ...
+static __global__ void permute_gather(CloudDev c, const int *__restrict__ perm, SortScratch z) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= c.n) return;
+    const int o = perm[s];
+    z.stage[0][s] = c.x[o];
+    z.stage[1][s] = c.y[o];
+    z.stage[2][s] = c.vx[o];
+    z.stage[3][s] = c.vy[o];
+    z.stage[4][s] = c.q[o];
+    z.stage[5][s] = c.m[o];
+    z.orig_stage[s] = c.orig[o];
+}
+
+// ... and copy back (the cloud's array addresses never change, so captured
+// CUDA graphs stay valid)
+static __global__ void permute_commit(CloudDev c, SortScratch z) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= c.n) return;
+    c.x[s] = z.stage[0][s];
+    c.y[s] = z.stage[1][s];
+    c.vx[s] = z.stage[2][s];
+    c.vy[s] = z.stage[3][s];
+    c.q[s] = z.stage[4][s];
+    c.m[s] = z.stage[5][s];
+    c.orig[s] = z.orig_stage[s];
+}
+
+static __global__ void set_identity(int *orig, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) orig[s] = s;
+}
+
+// out[orig[s]] = in[s] for up to four arrays (internal -> caller order).
+static __global__ void scatter_to_caller(const int *__restrict__ orig, int n, const double *a0,
+                                         const double *a1, const double *a2, const double *a3,
+                                         double *o0, double *o1, double *o2, double *o3) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = orig[s];
+    if (a0) o0[o] = a0[s];
+    if (a1) o1[o] = a1[s];
+    if (a2) o2[o] = a2[s];
+    if (a3) o3[o] = a3[s];
+}
+
+// out[s] = in[orig[s]] for up to two arrays (caller -> internal order).
+static __global__ void gather_from_caller(const int *__restrict__ orig, int n, const double *i0,
+                                          const double *i1, double *o0, double *o1) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int o = orig[s];
+    if (i0) o0[s] = i0[o];
+    if (i1) o1[s] = i1[o];
+}
+
+}  // namespace dm

@@ -184,6 +184,14 @@ int dm_cloud_modify_timestep(dm_cloud *cloud, double init_dt, float *min_dist,
  * potential energy, out[3..4] momentum.  No reference counterpart. */
 int dm_cloud_diagnostics(dm_cloud *cloud, double out[5]);
 
+/* The device keeps the cloud in Morton (space-filling-curve) order so each
+ * warp's particles are spatially compact and the pair kernels' cutoff test
+ * wakes the precise arithmetic for few j; the order is internal (every
+ * array crossing this ABI is in the caller's order).  The cloud is re-sorted
+ * every `steps` RK4 steps (default 4; 0 = only after an upload; otherwise a
+ * power of two <= 16).  No reference counterpart. */
+int dm_cloud_set_reorder_interval(dm_cloud *cloud, int steps);
+
 /* RNG step counter used by ThermalForce (advanced by one per RK4 step). */
 int dm_cloud_set_step_counter(dm_cloud *cloud, uint64_t step);
 int dm_cloud_get_step_counter(dm_cloud *cloud, uint64_t *step);

@@ -256,3 +256,35 @@ def test_bad_arguments_rejected(gpu_ctx):
                       np.full(6, W.Q_DUST), np.full(6, W.M_DUST))
     with pytest.raises(DemonError):
         odd.modify_timestep(1e-4)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_forces_after_morton_reorder_are_in_caller_order(gpu_ctx, oracle_lib, prec):
+    """After steps the device holds the cloud in Morton order; every array
+    crossing the ABI must still be in the caller's order."""
+    c0 = W.calm_cloud(700, 1e-2, 3)
+    c = DeviceCloud.from_cloud(gpu_ctx, c0)
+    c.set_reorder_interval(1)
+    c.step(3, 1e-4, "fp64")
+    x, y, vx, vy = c.download()
+    fx, fy = c.eval_forces(prec)
+    p = oracle.make_params(**c0.params())
+    rx, ry = oracle_lib.forces(x, y, vx, vy, c0.q, c0.m, p)
+    assert e_F(fx, fy, rx, ry) <= TOL[prec]
+    # upload resets the order; charges and masses must survive it
+    c.upload(x, y, vx, vy)
+    fx2, fy2 = c.eval_forces(prec)
+    assert e_F(fx2, fy2, rx, ry) <= TOL[prec]
+
+
+def test_reorder_interval_does_not_change_fp64_results_beyond_rounding(gpu_ctx):
+    c0 = W.calm_cloud(512, 1e-2, 4)
+    outs = []
+    for interval in (0, 1, 4, 16):
+        c = DeviceCloud.from_cloud(gpu_ctx, c0)
+        c.set_reorder_interval(interval)
+        c.step(40, 1e-4, "fp64")
+        outs.append(c.download())
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert rel(a, b) < 1e-13
