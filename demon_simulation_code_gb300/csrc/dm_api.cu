@@ -28,8 +28,9 @@ namespace {
 
 std::string g_create_error;
 
-// FP32C: 4 j-groups x 128 i-lanes, 4 particles per lane, 1024-particle j tiles
-constexpr int kNI32 = 128, kG32 = 4, kILP32 = 4, kJT32 = 1024;
+// FP32C: 8 warps sharing one 128-particle i tile (4 per lane), j tiles of
+// 256 4-j chunks
+constexpr int kNW32 = 8, kILP32 = 4, kTC32 = 256;
 // FP64: 2 j-groups x 128 i-lanes, 2 particles per lane, 512-particle j tiles
 constexpr int kNI64 = 128, kG64 = 2, kILP64 = 2, kJT64 = 512;
 constexpr int kGraphSteps = 16;
@@ -170,8 +171,8 @@ struct KernelShape {
 
 KernelShape shape_of(int precision) {
     if (precision == DM_FP32C)
-        return {(const void *)pair_stage_fp32c<kNI32, kG32, kILP32, kJT32>, kNI32 * kG32,
-                kNI32 * kILP32, kG32, Fp32cSmem<kNI32, kG32, kILP32>::bytes(kJT32)};
+        return {(const void *)pair_stage_fp32c<kNW32, kILP32, kTC32>, kNW32 * 32, 32 * kILP32, 1,
+                Fp32cSmem<kNW32, kILP32, kTC32>::bytes};
     return {(const void *)pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, kNI64 * kG64,
             kNI64 * kILP64, kG64, Fp64Smem<kNI64, kG64, kILP64>::bytes(kJT64)};
 }
@@ -274,7 +275,7 @@ int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, con
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     if (precision == DM_FP32C)
-        DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, pair_stage_fp32c<kNI32, kG32, kILP32, kJT32>, P, exp_consts()));
+        DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, pair_stage_fp32c<kNW32, kILP32, kTC32>, P, exp_consts()));
     else
         DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, P));
     if (ctx->prof) {

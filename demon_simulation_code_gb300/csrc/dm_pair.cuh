@@ -86,18 +86,16 @@ struct PairTuning {
 // atomics are needed; SIMD utilisation of the precise path goes from ~1/32
 // (sparse) or the hit fraction (dense) to mean/max of the per-lane hit count.
 // ---------------------------------------------------------------------------
-template <int NI, int G, int ILP>
+template <int NW, int ILP, int TC>
 struct Fp32cSmem {
-    static constexpr int pad = 4 * G;  // tile padding so 4-j chunks never run past it
-    static constexpr size_t cold = (size_t)ILP * NI * sizeof(float4);
-    static constexpr size_t queue = (size_t)G * (NI / 32) * ILP * 32 * sizeof(int2);
-    static constexpr size_t acc = (size_t)ILP * NI * G * sizeof(float4);
-    static constexpr size_t red = (size_t)ILP * NI * sizeof(double2);
-    static constexpr size_t therm = (size_t)NI * G * sizeof(double2);
-    static size_t bytes(int jt) {
-        return (size_t)(jt + pad) * (3 * sizeof(float) + sizeof(float4)) + cold + queue + acc + red +
-               therm;
-    }
+    // j tile: TC 4-j chunks as structure of arrays (x, y, |p|^2) + precise data
+    static constexpr size_t tile = (size_t)TC * (3 * sizeof(float4) + 4 * sizeof(float4));
+    static constexpr size_t cold = (size_t)ILP * 32 * sizeof(float4);
+    static constexpr size_t queue = (size_t)NW * ILP * 32 * sizeof(int2);
+    static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
+    static constexpr size_t red = (size_t)ILP * 32 * sizeof(double2);
+    static constexpr size_t therm = (size_t)NW * 32 * sizeof(double2);
+    static constexpr size_t bytes = tile + cold + queue + acc + red + therm;
 };
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
@@ -162,55 +160,54 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
     kahan_add(sy, cy, s * dy);
 }
 
-template <int NI, int G, int ILP, int JT>
-__global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
-    constexpr int NT = NI * G;
-    constexpr int NW = NT / 32;
-    constexpr int JP = JT + Fp32cSmem<NI, G, ILP>::pad;
-    static_assert(NI % 32 == 0 && JT % (4 * G) == 0 && ILP <= 4, "shape");
+template <int NW, int ILP, int TC>
+__global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+    constexpr int NT = NW * 32;
+    constexpr int TILE = 32 * ILP;  // particles per i tile
+    static_assert(ILP <= 4, "queue counts are packed in one 32-bit word");
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    // j tile, structure of arrays so one 16-byte load gives 4 consecutive j
-    float *s_x = reinterpret_cast<float *>(smem_raw);  // xh   [JP]
-    float *s_y = s_x + JP;                              // yh   [JP]
-    float *s_b = s_y + JP;                              // xh^2+yh^2 [JP]
-    float4 *s_pb = reinterpret_cast<float4 *>(s_b + JP);  // (xl, yl, q, -) [JP]
-    float4 *s_cold = s_pb + JP;                                   // [ILP][NI]
-    int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * NI);  // [NW][ILP][32]
-    float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);  // [ILP][NT] Kahan sums
-    double2 *s_red = reinterpret_cast<double2 *>(s_acc + ILP * NT);        // [ILP*NI]
-    double2 *s_therm = s_red + ILP * NI;                                    // [NT]
+    float4 *s_x4 = reinterpret_cast<float4 *>(smem_raw);  // [TC] xh of 4 j
+    float4 *s_y4 = s_x4 + TC;                              // [TC] yh
+    float4 *s_b4 = s_y4 + TC;                              // [TC] xh^2 + yh^2
+    float4 *s_pb = s_b4 + TC;                              // [4*TC] (xl, yl, q, global j)
+    float4 *s_cold = s_pb + 4 * TC;                        // [ILP][32]
+    int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * 32);           // [NW][ILP][32]
+    float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);    // [NW][ILP][32]
+    double2 *s_red = reinterpret_cast<double2 *>(s_acc + NW * ILP * 32);   // [TILE]
+    double2 *s_therm = s_red + TILE;                                       // [NT]
 
     cg::cluster_group cl = cg::this_cluster();
     const int S = (int)cl.num_blocks();
     const int rank = (int)cl.block_rank();
     const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
-    const int lane = tid & 31;
-    const int t = tid % NI, g = tid / NI;
+    const int lane = tid & 31, warp = tid >> 5;
     const int n = P.c.n, n_pad = P.c.n_pad;
     const int st = (P.mode == kModeForceOnly) ? 1 : P.stage;
     const int b = (st - 1) & 1;
     const float4 *__restrict__ pa = P.c.pa[b];
     const float4 *__restrict__ pb = P.c.pb[b];
-    int2 *my_queue = s_queue + (tid >> 5) * ILP * 32;
+    int2 *my_queue = s_queue + warp * ILP * 32;
+    float4 *my_acc = s_acc + warp * ILP * 32;
 
-    // This CTA finalises particles [rank*chunk, (rank+1)*chunk) of the tile
-    // (one per thread).  The FP64 thermal kick of that particle is computed
-    // now, so the FP64 pipe works while the other warps run the FP32 loop.
-    const int chunk = (NI * ILP + S - 1) / S;
+    // This CTA finalises particles [rank*chunk, (rank+1)*chunk) of the tile.
+    // Their FP64 thermal kicks are computed now, so the FP64 pipe works while
+    // the other warps run the FP32 loop.
+    const int fchunk = (TILE + S - 1) / S;
     int fin_e = -1;
-    if (tid < chunk) {
-        const int e = rank * chunk + tid;
-        if (e < NI * ILP && tile * NI * ILP + e < n) fin_e = e;
+    if (tid < fchunk) {
+        const int e = rank * fchunk + tid;
+        if (e < TILE && tile * TILE + e < n) fin_e = e;
     }
-    if (fin_e >= 0) s_therm[tid] = stage_thermal(P, tile * NI * ILP + fin_e);
+    if (fin_e >= 0) s_therm[tid] = stage_thermal(P, tile * TILE + fin_e);
 
-    // i side, duplicated into both halves of a packed pair: the packed FMAs
-    // below evaluate two consecutive j against one i
+    // every warp owns the same TILE particles: lane l, slot k -> i = tile*TILE + k*32 + l.
+    // i side duplicated into both halves of a packed pair: the packed FMAs
+    // evaluate two consecutive j against one i
     float2 mx2[ILP], my2[ILP], nu2[ILP];
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
-        const int i = tile * NI * ILP + k * NI + t;
+        const int i = tile * TILE + k * 32 + lane;
         float ax = 0.0f, ay = 0.0f, nu = INFINITY;
         float4 cold = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         if (i < n) {
@@ -224,72 +221,72 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
         mx2[k] = make_float2(-2.0f * ax, -2.0f * ax);
         my2[k] = make_float2(-2.0f * ay, -2.0f * ay);
         nu2[k] = make_float2(nu, nu);
-        if (g == 0) s_cold[k * NI + t] = cold;
-        s_acc[k * NT + tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (warp == 0) s_cold[k * 32 + lane] = cold;
+        my_acc[k * 32 + lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 
-    const int per = ((n_pad + S - 1) / S + 63) & ~63;
-    const int j0 = rank * per;
-    const int j1 = min(n_pad, j0 + per);
-    // queue fill per slot, 8 bits per slot (warp-uniform)
-    uint32_t qn = 0u;
-    __syncthreads();  // s_cold complete
+    // j chunks (4 consecutive j) are dealt round-robin: chunk c belongs to
+    // rank c % S and, within this CTA, to warp (c / S) % NW.  Every warp thus
+    // samples the whole cloud evenly, whatever the spatial order.
+    const int nch_all = n_pad >> 2;
+    const int my_nch = (nch_all - rank + S - 1) / S;  // chunks of this rank
+    uint32_t qn = 0u;  // queue fill per slot, 8 bits per slot (warp-uniform)
 
     // Run the precise path on the queued entries of slot K, then empty it.
-    auto flush = [&](auto kc, int jt) {
+    auto flush = [&](auto kc) {
         constexpr int K = decltype(kc)::value;
         __syncwarp();
         const int fill = (int)((qn >> (8 * K)) & 0xFFu);
         const int2 ent = (lane < fill) ? my_queue[K * 32 + lane] : make_int2(0, 0);
         uint32_t mask = warp_transpose32((uint32_t)ent.y);
         if (mask) {
-            const float4 c4 = s_cold[K * NI + t];
+            const float4 c4 = s_cold[K * 32 + lane];
             PairCtx ic;
             ic.xl = c4.x;
             ic.yl = c4.y;
             ic.qc = c4.z;
             ic.ii = __float_as_int(c4.w);
             const float xh = -0.5f * mx2[K].x, yh = -0.5f * my2[K].x;
-            float4 acc = s_acc[K * NT + tid];
+            float4 acc = my_acc[K * 32 + lane];
             do {
                 const int e = __ffs(mask) - 1;
                 mask &= mask - 1u;
-                const int jj = my_queue[K * 32 + e].x;
-                const float4 Aj = make_float4(s_x[jj], s_y[jj], 0.0f, s_pb[jj].z);
-                precise_pair(P, E, b, xh, yh, ic, Aj, s_pb[jj], jt + jj, acc.x, acc.y, acc.z,
-                             acc.w);
+                const int jj = my_queue[K * 32 + e].x;  // index into the tile's j
+                const float4 Bj = s_pb[jj];
+                const float xj = reinterpret_cast<const float *>(s_x4)[jj];
+                const float yj = reinterpret_cast<const float *>(s_y4)[jj];
+                precise_pair(P, E, b, xh, yh, ic, make_float4(xj, yj, 0.0f, Bj.z), Bj,
+                             __float_as_int(Bj.w), acc.x, acc.y, acc.z, acc.w);
             } while (mask);
-            s_acc[K * NT + tid] = acc;
+            my_acc[K * 32 + lane] = acc;
         }
         __syncwarp();
         qn &= ~(0xFFu << (8 * K));
     };
 
-    for (int jt = j0; jt < j1; jt += JT) {
-        const int cnt = min(JT, j1 - jt);
-        const int nch = (cnt + 3) >> 2;          // 4-j chunks in this tile
+    __syncthreads();  // s_cold complete
+    for (int q0 = 0; q0 < my_nch; q0 += TC) {
+        const int tcn = min(TC, my_nch - q0);
         __syncthreads();
-        for (int e = tid; e < 4 * ((nch + G - 1) / G) * G; e += NT) {
-            if (e < cnt) {
-                const float4 A = pa[jt + e];
-                s_x[e] = A.x;
-                s_y[e] = A.y;
-                s_b[e] = A.z;
-                const float4 B = pb[jt + e];
-                s_pb[e] = make_float4(B.x, B.y, A.w, 0.0f);
-            } else {  // padding j: never passes the filter
-                s_x[e] = kPadPosition;
-                s_y[e] = kPadPosition;
-                s_b[e] = INFINITY;
-                s_pb[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int e = tid; e < tcn; e += NT) {
+            const int jb = 4 * ((q0 + e) * S + rank);  // first j of the chunk
+            float xs[4], ys[4], bs[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const float4 A = pa[jb + u];
+                const float4 B = pb[jb + u];
+                xs[u] = A.x;
+                ys[u] = A.y;
+                bs[u] = A.z;
+                s_pb[4 * e + u] = make_float4(B.x, B.y, A.w, __int_as_float(jb + u));
             }
+            s_x4[e] = make_float4(xs[0], xs[1], xs[2], xs[3]);
+            s_y4[e] = make_float4(ys[0], ys[1], ys[2], ys[3]);
+            s_b4[e] = make_float4(bs[0], bs[1], bs[2], bs[3]);
         }
         __syncthreads();
-        const float4 *x4 = reinterpret_cast<const float4 *>(s_x);
-        const float4 *y4 = reinterpret_cast<const float4 *>(s_y);
-        const float4 *b4 = reinterpret_cast<const float4 *>(s_b);
-        for (int c = g; c < nch; c += G) {
-            const float4 X = x4[c], Y = y4[c], Bq = b4[c];
+        for (int c = warp; c < tcn; c += NW) {
+            const float4 X = s_x4[c], Y = s_y4[c], Bq = s_b4[c];
             const float2 X01 = make_float2(X.x, X.y), X23 = make_float2(X.z, X.w);
             const float2 Y01 = make_float2(Y.x, Y.y), Y23 = make_float2(Y.z, Y.w);
             const float2 B01 = make_float2(Bq.x, Bq.y), B23 = make_float2(Bq.z, Bq.w);
@@ -318,27 +315,26 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
                             const int fill = (int)((qn >> (8 * k)) & 0xFFu);
                             if (lane == 0) my_queue[k * 32 + fill] = make_int2(4 * c + u, (int)bal);
                             qn += 1u << (8 * k);
-                            if (fill == 31) flush(kc, jt);
+                            if (fill == 31) flush(kc);
                         }
                     });
                 }
             }
         }
-        // the queued j index into this tile: drain before it is overwritten
+        // queued entries index into this tile: drain before it is overwritten
         static_for<ILP>([&](auto kc) {
-            if ((qn >> (8 * decltype(kc)::value)) & 0xFFu) flush(kc, jt);
+            if ((qn >> (8 * decltype(kc)::value)) & 0xFFu) flush(kc);
         });
     }
 
-    // combine the G groups (fixed order, FP64; Kahan sum = s - c), then the
+    // combine the NW warps (fixed order, FP64; Kahan sum = s - c), then the
     // S cluster ranks
     __syncthreads();
-    for (int e = tid; e < ILP * NI; e += NT) {
-        const int k = e / NI, tt = e % NI;
+    for (int e = tid; e < TILE; e += NT) {
         double fx = 0.0, fy = 0.0;
 #pragma unroll
-        for (int gg = 0; gg < G; gg++) {
-            const float4 v = s_acc[k * NT + gg * NI + tt];
+        for (int w = 0; w < NW; w++) {
+            const float4 v = s_acc[w * ILP * 32 + e];
             fx += (double)v.x - (double)v.z;
             fy += (double)v.y - (double)v.w;
         }
@@ -346,7 +342,7 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp32c(const StageParams 
     }
     cl.sync();
     if (fin_e >= 0) {
-        const int i = tile * NI * ILP + fin_e;
+        const int i = tile * TILE + fin_e;
         double fx = 0.0, fy = 0.0;
         for (int r = 0; r < S; r++) {
             const double2 v = *cl.map_shared_rank(s_red + fin_e, r);
