@@ -93,7 +93,7 @@ struct Fp32cSmem {
     static constexpr size_t cold = (size_t)ILP * 32 * sizeof(float4);
     static constexpr size_t queue = (size_t)NW * ILP * 32 * sizeof(int2);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
-    static constexpr size_t red = (size_t)ILP * 32 * sizeof(double2);
+    static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
     static constexpr size_t therm = (size_t)NW * 32 * sizeof(double2);
     static constexpr size_t bytes = tile + cold + queue + acc + red + therm;
 };
@@ -173,8 +173,8 @@ __global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams
     float4 *s_cold = s_pb + 4 * TC;                        // [ILP][32]
     int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * 32);           // [NW][ILP][32]
     float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);    // [NW][ILP][32]
-    double2 *s_red = reinterpret_cast<double2 *>(s_acc + NW * ILP * 32);   // [TILE]
-    double2 *s_therm = s_red + TILE;                                       // [NT]
+    float4 *s_red = s_acc + NW * ILP * 32;                                 // [TILE]
+    double2 *s_therm = reinterpret_cast<double2 *>(s_red + TILE);          // [NT]
 
     cg::cluster_group cl = cg::this_cluster();
     const int S = (int)cl.num_blocks();
@@ -327,27 +327,30 @@ __global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams
         });
     }
 
-    // combine the NW warps (fixed order, FP64; Kahan sum = s - c), then the
-    // S cluster ranks
+    // combine the NW warps in fixed order with a compensated FP32 sum (each
+    // warp's Kahan pair (s, c) stands for s - c); FP64 only once per particle
+    // below (FP64 runs at 1/64 of the FP32 rate here)
     __syncthreads();
     for (int e = tid; e < TILE; e += NT) {
-        double fx = 0.0, fy = 0.0;
+        float sx = 0.0f, cx = 0.0f, sy = 0.0f, cy = 0.0f;
 #pragma unroll
         for (int w = 0; w < NW; w++) {
             const float4 v = s_acc[w * ILP * 32 + e];
-            fx += (double)v.x - (double)v.z;
-            fy += (double)v.y - (double)v.w;
+            kahan_add(sx, cx, v.x);
+            kahan_add(sx, cx, -v.z);
+            kahan_add(sy, cy, v.y);
+            kahan_add(sy, cy, -v.w);
         }
-        s_red[e] = make_double2(fx, fy);
+        s_red[e] = make_float4(sx, sy, cx, cy);
     }
     cl.sync();
     if (fin_e >= 0) {
         const int i = tile * TILE + fin_e;
         double fx = 0.0, fy = 0.0;
         for (int r = 0; r < S; r++) {
-            const double2 v = *cl.map_shared_rank(s_red + fin_e, r);
-            fx += v.x;
-            fy += v.y;
+            const float4 v = *cl.map_shared_rank(s_red + fin_e, r);
+            fx += (double)v.x - (double)v.z;
+            fy += (double)v.y - (double)v.w;
         }
         stage_epilogue(P, i, fx, fy, s_therm[tid]);
     }
