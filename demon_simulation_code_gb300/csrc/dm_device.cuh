@@ -88,34 +88,87 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
     }
 }
 
-// 53-bit uniform strictly inside (0, 1).
-__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
-    const unsigned long long v = ((unsigned long long)a << 21) ^ ((unsigned long long)b >> 11);
-    return __dmul_rn(__dadd_rn((double)v, 0.5), 1.0 / 9007199254740992.0);
+// Thermal kick arithmetic: FP32 Box-Muller built only from correctly rounded
+// IEEE single operations (add, mul, fma, div, sqrt) in a fixed order, so the
+// CPU oracle reproduces it bit for bit (oracle/demon_oracle.c).  The kick is
+// noise of relative size ~1e-5 of the forces it is added to; FP32 (rather
+// than FP64, which runs at 1/64 of the FP32 rate on this GPU) loses nothing.
+//
+// u in (0, 1): 24 random bits, (k + 0.5) * 2^-24.
+__device__ __forceinline__ float u24(uint32_t w) {
+    return __fmul_rn(__fadd_rn((float)(w >> 8), 0.5f), 5.9604644775390625e-8f);
+}
+
+// ln(u), u in (0, 1]: u = 2^e m with m in [sqrt(1/2), sqrt(2)),
+// ln m = 2 atanh(s), s = (m-1)/(m+1), atanh by its odd series to s^9
+// (|s| < 0.1716: truncation < 2e-9).
+__device__ __forceinline__ float thermal_log(float u) {
+    const uint32_t bits = __float_as_uint(u);
+    int e = (int)(bits >> 23) - 127;
+    float m = __uint_as_float((bits & 0x007FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) {
+        m = __fmul_rn(m, 0.5f);
+        e += 1;
+    }
+    const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+    const float s2 = __fmul_rn(s, s);
+    float p = __fmaf_rn(s2, 0.111111111f, 0.142857143f);
+    p = __fmaf_rn(s2, p, 0.2f);
+    p = __fmaf_rn(s2, p, 0.333333333f);
+    p = __fmaf_rn(s2, p, 1.0f);
+    const float lnm = __fmul_rn(__fmul_rn(2.0f, s), p);
+    return __fmaf_rn((float)e, 0.693147181f, lnm);
+}
+
+// sin and cos of 2 pi u, u in [0, 1): quadrant q = floor(4u), a = (4u - q) pi/2
+// in [0, pi/2), Taylor polynomials to a^13 (sin) and a^14 (cos), truncation
+// < 7e-10, then the exact quadrant rotation.
+__device__ __forceinline__ void thermal_sincos(float u, float &sn, float &cs) {
+    const float r = __fmul_rn(u, 4.0f);
+    const float qf = floorf(r);
+    const int q = (int)qf;
+    const float a = __fmul_rn(__fsub_rn(r, qf), 1.57079633f);
+    const float a2 = __fmul_rn(a, a);
+    float ps = __fmaf_rn(a2, 1.60590438e-10f, -2.50521084e-8f);
+    ps = __fmaf_rn(a2, ps, 2.75573192e-6f);
+    ps = __fmaf_rn(a2, ps, -1.98412698e-4f);
+    ps = __fmaf_rn(a2, ps, 8.33333333e-3f);
+    ps = __fmaf_rn(a2, ps, -1.66666667e-1f);
+    ps = __fmaf_rn(a2, ps, 1.0f);
+    const float sa = __fmul_rn(a, ps);
+    float pc = __fmaf_rn(a2, -1.14707456e-11f, 2.08767570e-9f);
+    pc = __fmaf_rn(a2, pc, -2.75573192e-7f);
+    pc = __fmaf_rn(a2, pc, 2.48015873e-5f);
+    pc = __fmaf_rn(a2, pc, -1.38888889e-3f);
+    pc = __fmaf_rn(a2, pc, 4.16666667e-2f);
+    pc = __fmaf_rn(a2, pc, -0.5f);
+    const float ca = __fmaf_rn(a2, pc, 1.0f);
+    switch (q & 3) {
+        case 0: sn = sa; cs = ca; break;
+        case 1: sn = ca; cs = -sa; break;
+        case 2: sn = -sa; cs = -ca; break;
+        default: sn = -ca; cs = sa; break;
+    }
 }
 
 // Thermal kick for particle i at (step, stage).  Mode 0 is the reference's
-// form heatVal*U*(cos t, sin t) (ThermalForce.cpp:118-140) with counter-based
-// uniforms; mode 1 is a Gaussian of standard deviation `heat` per axis.
+// form heatVal*U*(cos t, sin t), t ~ U(0, 2pi) (ThermalForce.cpp:118-140)
+// with counter-based uniforms; mode 1 is a Gaussian of standard deviation
+// `heat` per axis (Box-Muller).
 __device__ __forceinline__ void thermal_kick(const ForceParams &f, uint32_t i,
                                              unsigned long long step, int stage,
                                              double &tx, double &ty) {
     uint32_t c[4] = {i, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)stage};
     philox4x32_10(c, (uint32_t)f.seed, (uint32_t)(f.seed >> 32));
-    const double u1 = u53(c[0], c[1]);
-    const double u2 = u53(c[2], c[3]);
-    const double th = __dmul_rn(u2, 2.0 * 3.14159265358979323846);
-    double s, co;
-    sincos(th, &s, &co);
-    if (f.thermal_mode == 0) {
-        const double a = __dmul_rn(u1, f.heat);
-        tx = __dmul_rn(a, co);
-        ty = __dmul_rn(a, s);
-    } else {
-        const double rad = sqrt(__dmul_rn(-2.0, log(u1)));
-        tx = __dmul_rn(f.heat, __dmul_rn(rad, co));
-        ty = __dmul_rn(f.heat, __dmul_rn(rad, s));
-    }
+    const float u1 = u24(c[0]);
+    const float u2 = u24(c[1]);
+    float sn, cs;
+    thermal_sincos(u2, sn, cs);
+    float amp;
+    if (f.thermal_mode == 0) amp = u1;
+    else amp = __fsqrt_rn(__fmul_rn(-2.0f, thermal_log(u1)));
+    tx = __dmul_rn(f.heat, (double)__fmul_rn(amp, cs));
+    ty = __dmul_rn(f.heat, (double)__fmul_rn(amp, sn));
 }
 
 // RNG step index of the running stage.  Stage 1 reads slot 0 and copies it

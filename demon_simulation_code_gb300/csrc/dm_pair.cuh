@@ -94,8 +94,7 @@ struct Fp32cSmem {
     static constexpr size_t queue = (size_t)NW * ILP * 32 * sizeof(int2);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
-    static constexpr size_t therm = (size_t)NW * 32 * sizeof(double2);
-    static constexpr size_t bytes = tile + cold + queue + acc + red + therm;
+    static constexpr size_t bytes = tile + cold + queue + acc + red;
 };
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
@@ -174,7 +173,6 @@ __global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams
     int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * 32);           // [NW][ILP][32]
     float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);    // [NW][ILP][32]
     float4 *s_red = s_acc + NW * ILP * 32;                                 // [TILE]
-    double2 *s_therm = reinterpret_cast<double2 *>(s_red + TILE);          // [NT]
 
     cg::cluster_group cl = cg::this_cluster();
     const int S = (int)cl.num_blocks();
@@ -190,16 +188,15 @@ __global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams
     int2 *my_queue = s_queue + warp * ILP * 32;
     float4 *my_acc = s_acc + warp * ILP * 32;
 
-    // This CTA finalises particles [rank*chunk, (rank+1)*chunk) of the tile.
-    // Their FP64 thermal kicks are computed now, so the FP64 pipe works while
-    // the other warps run the FP32 loop.
-    const int fchunk = (TILE + S - 1) / S;
+    // This CTA finalises particles [rank*fchunk, (rank+1)*fchunk) of the tile,
+    // in whole warps: an FP64 warp instruction costs the same with 1 or 32
+    // active lanes, so the FP64 epilogue runs on as few warps as possible.
+    const int fchunk = max(32, (TILE + S - 1) / S);
     int fin_e = -1;
     if (tid < fchunk) {
         const int e = rank * fchunk + tid;
         if (e < TILE && tile * TILE + e < n) fin_e = e;
     }
-    if (fin_e >= 0) s_therm[tid] = stage_thermal(P, tile * TILE + fin_e);
 
     // every warp owns the same TILE particles: lane l, slot k -> i = tile*TILE + k*32 + l.
     // i side duplicated into both halves of a packed pair: the packed FMAs
@@ -352,7 +349,7 @@ __global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams
             fx += (double)v.x - (double)v.z;
             fy += (double)v.y - (double)v.w;
         }
-        stage_epilogue(P, i, fx, fy, s_therm[tid]);
+        stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
     }
     stage_step_advance(P);
     cl.sync();

@@ -220,10 +220,61 @@ void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* 53-bit uniform strictly inside (0, 1) from two 32-bit words. */
-static inline double u53(uint32_t a, uint32_t b) {
-    const uint64_t v = ((uint64_t)a << 21) ^ ((uint64_t)b >> 11);
-    return ((double)v + 0.5) * (1.0 / 9007199254740992.0);
+/* Thermal kick arithmetic: FP32 Box-Muller from correctly rounded IEEE
+ * single operations in a fixed order (this file is built with
+ * -ffp-contract=off, fmaf is the correctly rounded fused multiply-add), the
+ * same sequence as the CUDA path, so both give identical bits. */
+static inline float u24(uint32_t w) {
+    return ((float)(w >> 8) + 0.5f) * 5.9604644775390625e-8f;
+}
+
+static float thermal_log(float u) {
+    uint32_t bits;
+    memcpy(&bits, &u, 4);
+    int e = (int)(bits >> 23) - 127;
+    const uint32_t mb = (bits & 0x007FFFFFu) | 0x3F800000u;
+    float m;
+    memcpy(&m, &mb, 4);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = fmaf(s2, 0.111111111f, 0.142857143f);
+    p = fmaf(s2, p, 0.2f);
+    p = fmaf(s2, p, 0.333333333f);
+    p = fmaf(s2, p, 1.0f);
+    const float lnm = (2.0f * s) * p;
+    return fmaf((float)e, 0.693147181f, lnm);
+}
+
+static void thermal_sincos(float u, float *sn, float *cs) {
+    const float r = u * 4.0f;
+    const float qf = floorf(r);
+    const int q = (int)qf;
+    const float a = (r - qf) * 1.57079633f;
+    const float a2 = a * a;
+    float ps = fmaf(a2, 1.60590438e-10f, -2.50521084e-8f);
+    ps = fmaf(a2, ps, 2.75573192e-6f);
+    ps = fmaf(a2, ps, -1.98412698e-4f);
+    ps = fmaf(a2, ps, 8.33333333e-3f);
+    ps = fmaf(a2, ps, -1.66666667e-1f);
+    ps = fmaf(a2, ps, 1.0f);
+    const float sa = a * ps;
+    float pc = fmaf(a2, -1.14707456e-11f, 2.08767570e-9f);
+    pc = fmaf(a2, pc, -2.75573192e-7f);
+    pc = fmaf(a2, pc, 2.48015873e-5f);
+    pc = fmaf(a2, pc, -1.38888889e-3f);
+    pc = fmaf(a2, pc, 4.16666667e-2f);
+    pc = fmaf(a2, pc, -0.5f);
+    const float ca = fmaf(a2, pc, 1.0f);
+    switch (q & 3) {
+        case 0: *sn = sa; *cs = ca; break;
+        case 1: *sn = ca; *cs = -sa; break;
+        case 2: *sn = -sa; *cs = -ca; break;
+        default: *sn = -ca; *cs = sa; break;
+    }
 }
 
 void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
@@ -232,20 +283,15 @@ void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
     const uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
     uint32_t o[4];
     or_philox4x32_10(ctr, key, o);
-    const double u1 = u53(o[0], o[1]);
-    const double u2 = u53(o[2], o[3]);
-    const double th = u2 * (2.0 * M_PI);
-    if (p->thermal_mode == 0) {
-        /* ThermalForce::force (ThermalForce.cpp:118-122): heatVal*U*(cos, sin) */
-        const double a = u1 * p->heat;
-        *tx = a * cos(th);
-        *ty = a * sin(th);
-    } else {
-        /* Gaussian kick, sigma = heat per axis (Box-Muller) */
-        const double rad = sqrt(-2.0 * log(u1));
-        *tx = p->heat * (rad * cos(th));
-        *ty = p->heat * (rad * sin(th));
-    }
+    const float u1 = u24(o[0]);
+    const float u2 = u24(o[1]);
+    float sn, cs;
+    thermal_sincos(u2, &sn, &cs);
+    /* mode 0: ThermalForce::force (ThermalForce.cpp:118-122), heatVal*U*(cos, sin);
+     * mode 1: Gaussian, sigma = heat per axis (Box-Muller) */
+    const float amp = (p->thermal_mode == 0) ? u1 : sqrtf(-2.0f * thermal_log(u1));
+    *tx = p->heat * (double)(amp * cs);
+    *ty = p->heat * (double)(amp * sn);
 }
 
 /* ---------------------------------------------------------------------------

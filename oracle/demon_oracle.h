@@ -68,7 +68,8 @@ void or_shielded_coulomb_omp(int n, const double *x, const double *y,
 
 /* Counter-based thermal kick for particle i at (step, stage): writes the
  * force (not +=).  Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) keyed by
- * seed, counter (i, step lo, step hi, stage); two 53-bit uniforms; mode 0 is
+ * seed, counter (i, step lo, step hi, stage); two 24-bit uniforms and FP32
+ * Box-Muller arithmetic shared bit for bit with the CUDA path; mode 0 is
  * the reference's form (ThermalForce.cpp:118-140), mode 1 Box-Muller. */
 void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
                     double *tx, double *ty);
