@@ -254,6 +254,7 @@ def run_gb300(args, world, rank, local):
         step_ms[:] = ms
         return sum(ms) / 1e3
 
+    tuned = cloud.autotune(args.precision)  # autotuner: variant x split on this cloud
     # warm-up (untimed)
     cloud.step(max(args.warmup, 3), w.dt, args.precision)
     torch.cuda.synchronize()
@@ -342,6 +343,7 @@ def run_gb300(args, world, rank, local):
             "dtype": "f32" if args.precision == "fp32c" else "f64",
             "data": "synthetic (seeded generator, demon_simulation_code_gb300/workloads.py)",
             "config": config_of(w, args),
+            "tuning": {"variant": tuned[0], "split": tuned[1]},
             "fp64_value": fp64_value,
             "fp32c_over_fp64": (value / world / fp64_value) if fp64_value else None,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * n,

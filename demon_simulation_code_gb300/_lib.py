@@ -61,6 +61,11 @@ SIGNATURES = {
     "dm_ctx_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dm_ctx_profile_read": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_longlong), _dp]),
     "dm_probe_peak": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "dm_ctx_set_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dm_kernel_variants": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "dm_cloud_set_kernel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
+    "dm_cloud_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
+                                         ctypes.POINTER(ctypes.c_int)]),
     "dm_cloud_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp,
                                        ctypes.POINTER(ctypes.c_void_p)]),
     "dm_cloud_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -114,6 +119,12 @@ def last_error(ctx) -> str:
 def check(rc: int, ctx=None) -> None:
     if rc != DM_OK:
         raise DemonError(rc, last_error(ctx))
+
+
+def kernel_variants() -> list[str]:
+    buf = ctypes.create_string_buffer(4096)
+    check(load().dm_kernel_variants(buf, len(buf)))
+    return buf.value.decode().split(";")
 
 
 def ptr(a: np.ndarray):

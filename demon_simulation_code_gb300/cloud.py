@@ -63,6 +63,9 @@ class Context:
                                            ctypes.byref(pairs)), self.h)
         return ms.value, n.value, pairs.value
 
+    def set_autotune(self, enable: bool):
+        check(self.lib.dm_ctx_set_autotune(self.h, int(enable)), self.h)
+
     def probe_peak(self, kind: str = "fp32") -> float:
         v = ctypes.c_double()
         check(self.lib.dm_probe_peak(self.h, 0 if kind == "fp32" else 1, ctypes.byref(v)), self.h)
@@ -157,6 +160,15 @@ class DeviceCloud:
         out = np.zeros(5)
         self._chk(self.lib.dm_cloud_diagnostics(self.h, ptr(out)))
         return out
+
+    def autotune(self, precision="fp32c"):
+        buf = ctypes.create_string_buffer(128)
+        split = ctypes.c_int()
+        self._chk(self.lib.dm_cloud_autotune(self.h, _prec(precision), buf, len(buf), ctypes.byref(split)))
+        return buf.value.decode(), split.value
+
+    def set_kernel(self, variant: str, split: int = 0):
+        self._chk(self.lib.dm_cloud_set_kernel(self.h, variant.encode(), int(split)))
 
     def set_reorder_interval(self, steps: int):
         self._chk(self.lib.dm_cloud_set_reorder_interval(self.h, int(steps)))

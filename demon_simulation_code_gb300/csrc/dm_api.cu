@@ -28,8 +28,8 @@ namespace {
 
 std::string g_create_error;
 
-// FP32C: 8 warps sharing one 128-particle i tile (4 per lane), j tiles of
-// 256 4-j chunks
+// FP32C default shape: 8 warps sharing one 128-particle i tile (4 per
+// lane), j tiles of 256 4-j chunks; the autotuner may pick another variant.
 constexpr int kNW32 = 8, kILP32 = 4, kTC32 = 256;
 // FP64: 2 j-groups x 128 i-lanes, 2 particles per lane, 512-particle j tiles
 constexpr int kNI64 = 128, kG64 = 2, kILP64 = 2, kJT64 = 512;
@@ -44,6 +44,8 @@ struct dm_ctx {
     int num_sms = 0;
     std::string err;
     bool prof = false;
+    bool autotune = true;
+    std::map<long long, std::pair<int, int>> tune_cache;  // (n, precision) -> (variant, split)
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
     size_t prof_used = 0;
     double prof_pairs = 0.0;
@@ -83,6 +85,9 @@ struct dm_cloud {
     unsigned int *d_min = nullptr;
     float *d_dmin = nullptr;
     int split[2] = {0, 0};  // cluster size per precision (0 = not chosen yet)
+    int tuned_variant[2] = {-1, -1};  // per precision: index into kVariants
+    float4 *partial = nullptr;         // [partial_cap][n_pad] non-cluster partial sums
+    int partial_cap = 0;
     SortScratch sort{};
     int sort_blocks = 0;
     int reorder_interval = 4;   // steps between Morton re-sorts (0 = never)
@@ -94,6 +99,9 @@ struct dm_cloud {
     void drop_graphs() {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
         graphs.clear();
+    }
+    ~dm_cloud() {
+        if (partial) cudaFree(partial);
     }
 };
 
@@ -161,70 +169,117 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     return P;
 }
 
-struct KernelShape {
-    const void *fn;
-    int nt;      // threads per CTA
-    int tile;    // particles per i tile
-    int groups;  // j groups per CTA
+// ---------------------------------------------------------------------------
+// Kernel variants and the autotuner
+// ---------------------------------------------------------------------------
+struct Variant {
+    const char *name;
+    int precision;
+    bool cluster;  // reduce through a thread-block cluster (else global partials + stage_finish)
+    int nt;        // threads per CTA
+    int tile;      // particles per i tile
     size_t smem;
+    const void *fn;
+    cudaError_t (*launch)(const cudaLaunchConfig_t *, const StageParams &);
 };
 
-KernelShape shape_of(int precision) {
-    if (precision == DM_FP32C)
-        return {(const void *)pair_stage_fp32c<kNW32, kILP32, kTC32>, kNW32 * 32, 32 * kILP32, 1,
-                Fp32cSmem<kNW32, kILP32, kTC32>::bytes};
-    return {(const void *)pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, kNI64 * kG64,
-            kNI64 * kILP64, kG64, Fp64Smem<kNI64, kG64, kILP64>::bytes(kJT64)};
+template <int NW, int ILP, int TC, bool CL>
+cudaError_t launch_fp32c(const cudaLaunchConfig_t *cfg, const StageParams &P) {
+    return cudaLaunchKernelEx(cfg, pair_stage_fp32c<NW, ILP, TC, CL>, P, exp_consts());
 }
+template <int NI, int G, int ILP, int JT>
+cudaError_t launch_fp64(const cudaLaunchConfig_t *cfg, const StageParams &P) {
+    return cudaLaunchKernelEx(cfg, pair_stage_fp64<NI, G, ILP, JT>, P);
+}
+
+#define DM_FP32C_VARIANT(NW, ILP, TC, CL)                                                        \
+    {"fp32c<" #NW "," #ILP "," #TC "," #CL ">", DM_FP32C, CL, NW * 32, 32 * ILP,                  \
+     Fp32cSmem<NW, ILP, TC>::bytes, (const void *)pair_stage_fp32c<NW, ILP, TC, CL>,              \
+     launch_fp32c<NW, ILP, TC, CL>}
+
+const Variant kVariants[] = {
+    DM_FP32C_VARIANT(8, 4, 256, true),
+    DM_FP32C_VARIANT(8, 4, 256, false),
+    DM_FP32C_VARIANT(4, 4, 256, true),
+    DM_FP32C_VARIANT(4, 4, 256, false),
+    DM_FP32C_VARIANT(16, 4, 256, false),
+    DM_FP32C_VARIANT(8, 2, 256, false),
+    {"fp64<128,2,2,512>", DM_FP64, true, kNI64 * kG64, kNI64 * kILP64,
+     Fp64Smem<kNI64, kG64, kILP64>::bytes(kJT64),
+     (const void *)pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, launch_fp64<kNI64, kG64, kILP64, kJT64>},
+};
+constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+constexpr int kDefaultVariant32 = 0;
+constexpr int kDefaultVariant64 = kNumVariants - 1;
+constexpr int kMaxSplitGlobal = 64;
 
 int ensure_kernel_attrs(dm_ctx *ctx) {
     static bool done[64] = {false};
     int dev = ctx->device;
     if (dev < 0 || dev >= 64) dev = 0;
     if (done[dev]) return DM_OK;
-    for (int prec : {DM_FP64, DM_FP32C}) {
-        const KernelShape k = shape_of(prec);
-        DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    for (int v = 0; v < kNumVariants; v++) {
+        const Variant &k = kVariants[v];
+        if (k.cluster)
+            DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
     }
     done[dev] = true;
     return DM_OK;
 }
 
-// j split (cluster size S) for a cloud.  All CTAs of a launch do equal work
-// (1/S of a tile), so the launch takes as long as its busiest SM: with X
-// co-resident clusters of size S (the device's own count, GPC packing
-// included) the tiles run in ceil(ntiles / X) cluster waves, and within a
-// wave the busiest SM holds ceil(CTAs_in_wave / num_sms) CTAs.  Cost =
-// sum over waves of that count / S; on ties (within 2%) the larger S wins:
-// more co-resident CTAs hide latency better, which the model ignores.
-int pick_split(dm_ctx *ctx, int precision, int n, int n_pad, int *out) {
-    const KernelShape k = shape_of(precision);
-    const int ntiles = (n + k.tile - 1) / k.tile;
-    int best_s = 1;
-    double best_cost = 1e300;
-    for (int S = 1; S <= 16; S++) {
-        if (S > 1 && n_pad / S < 64 * k.groups) break;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(ntiles * S, 1, 1);
-        cfg.blockDim = dim3(k.nt, 1, 1);
-        cfg.dynamicSmemBytes = k.smem;
-        cudaLaunchAttribute attr[1];
+int variant_groups(const Variant &k) { return k.precision == DM_FP64 ? kG64 : k.nt / 32; }
+
+cudaLaunchConfig_t make_cfg(dm_ctx *ctx, const Variant &k, int ntiles, int S, cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ntiles * S, 1, 1);
+    cfg.blockDim = dim3(k.nt, 1, 1);
+    cfg.dynamicSmemBytes = k.smem;
+    cfg.stream = ctx->stream;
+    if (k.cluster) {
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = S;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        int nc = 0;
-        cudaError_t e = cudaOccupancyMaxActiveClusters(&nc, k.fn, &cfg);
-        if (e != cudaSuccess || nc <= 0) {
-            cudaGetLastError();
-            continue;
+    }
+    return cfg;
+}
+
+// j split S for a variant from a cost model: all CTAs do equal work (1/S of a
+// tile), so a launch takes as long as its busiest SM.  With X co-resident
+// clusters (or CTAs) the tiles run in ceil(ntiles / X) waves and within a
+// wave the busiest SM holds ceil(CTAs_in_wave / num_sms) CTAs.  Cost = sum
+// over waves of that count / S; on ties (within 2%) the larger S wins, since
+// more co-resident CTAs hide latency better.
+int model_split(dm_ctx *ctx, const Variant &k, int n, int n_pad) {
+    const int ntiles = (n + k.tile - 1) / k.tile;
+    const int smax = k.cluster ? 16 : kMaxSplitGlobal;
+    int best_s = 1;
+    double best_cost = 1e300;
+    for (int S = 1; S <= smax; S++) {
+        if (S > 1 && n_pad / S < 64 * variant_groups(k)) break;
+        int slots = 0;
+        if (k.cluster) {
+            cudaLaunchAttribute attr[1];
+            cudaLaunchConfig_t cfg = make_cfg(ctx, k, ntiles, S, attr);
+            if (cudaOccupancyMaxActiveClusters(&slots, k.fn, &cfg) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+        } else {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.nt, k.smem) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            slots = per_sm * ctx->num_sms / S;  // co-resident "tiles"
         }
+        if (slots <= 0) continue;
         double cost = 0.0;
-        for (int left = ntiles; left > 0; left -= nc) {
-            const int in_wave = std::min(left, nc) * S;
+        for (int left = ntiles; left > 0; left -= slots) {
+            const int in_wave = std::min(left, slots) * S;
             cost += (double)((in_wave + ctx->num_sms - 1) / ctx->num_sms) / S;
         }
         if (cost <= best_cost * 1.02) {
@@ -232,21 +287,57 @@ int pick_split(dm_ctx *ctx, int precision, int n, int n_pad, int *out) {
             best_s = S;
         }
     }
-    *out = best_s;
+    return best_s;
+}
+
+int ensure_partial(dm_cloud *c, int S) {
+    if (S <= c->partial_cap) return DM_OK;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (c->partial) cudaFree(c->partial);
+    c->partial = nullptr;
+    c->partial_cap = 0;
+    cudaError_t e = cudaMalloc((void **)&c->partial, (size_t)S * c->n_pad * sizeof(float4));
+    if (e != cudaSuccess)
+        return ctx->fail(DM_ERR_NOMEM, "partial-sum buffer (%d x %d): %s", S, c->n_pad, cudaGetErrorString(e));
+    c->partial_cap = S;
+    c->drop_graphs();
     return DM_OK;
 }
 
-// One launch of the fused pair + stage kernel.
+// One stage: the pair kernel (+ stage_finish for non-cluster variants).
+int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, const double *dt_dev) {
+    dm_ctx *ctx = c->ctx;
+    const Variant &k = kVariants[vi];
+    StageParams P = make_stage_params(c, stage, mode, dt, dt_dev);
+    P.split = S;
+    P.partial = c->partial;
+    const int ntiles = (c->n + k.tile - 1) / k.tile;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = make_cfg(ctx, k, ntiles, S, attr);
+    DM_CUDA(ctx, k.launch(&cfg, P));
+    if (!k.cluster) {
+        stage_finish<<<(c->n + 127) / 128, 128, 0, ctx->stream>>>(P);
+        DM_CUDA(ctx, cudaGetLastError());
+    }
+    return DM_OK;
+}
+
+int tune_precision(dm_cloud *c, int precision);
+
+// One launch of the fused pair + stage kernel(s) with the cloud's tuned
+// variant and split.
 int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, const double *dt_dev) {
     dm_ctx *ctx = c->ctx;
     int rc = ensure_kernel_attrs(ctx);
     if (rc) return rc;
-    int &S = c->split[precision == DM_FP32C ? 1 : 0];
-    if (S <= 0) {
-        rc = pick_split(ctx, precision, c->n, c->n_pad, &S);
+    const int pi = precision == DM_FP32C ? 1 : 0;
+    if (c->tuned_variant[pi] < 0) {
+        rc = tune_precision(c, precision);
         if (rc) return rc;
     }
-    const StageParams P = make_stage_params(c, stage, mode, dt, dt_dev);
+    const int vi = c->tuned_variant[pi];
+    const int S = c->split[pi];
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ctx->prof) {
         if (ctx->prof_used == ctx->prof_events.size()) {
@@ -260,29 +351,97 @@ int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, con
         ctx->prof_used++;
         DM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
     }
-    const KernelShape k = shape_of(precision);
-    const int ntiles = (c->n + k.tile - 1) / k.tile;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(ntiles * S, 1, 1);
-    cfg.blockDim = dim3(k.nt, 1, 1);
-    cfg.dynamicSmemBytes = k.smem;
-    cfg.stream = ctx->stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = S;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (precision == DM_FP32C)
-        DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, pair_stage_fp32c<kNW32, kILP32, kTC32>, P, exp_consts()));
-    else
-        DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, P));
+    rc = launch_variant(c, vi, S, stage, mode, dt, dt_dev);
+    if (rc) return rc;
     if (ctx->prof) {
         DM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
         ctx->prof_launches++;
         ctx->prof_pairs += (double)c->n * (double)(c->n - 1);
     }
+    return DM_OK;
+}
+
+// Autotuner: times every variant of this precision over a set of splits on
+// THIS cloud (force-only launches: no state changes), keeps the fastest.
+// Results are cached per (precision, n) in the context.  When disabled, the
+// default variant and the cost-model split are used.
+int tune_precision(dm_cloud *c, int precision) {
+    dm_ctx *ctx = c->ctx;
+    const int pi = precision == DM_FP32C ? 1 : 0;
+    const long long key = ((long long)c->n << 1) | pi;
+    auto hit = ctx->tune_cache.find(key);
+    if (hit != ctx->tune_cache.end()) {
+        c->tuned_variant[pi] = hit->second.first;
+        c->split[pi] = hit->second.second;
+        if (!kVariants[c->tuned_variant[pi]].cluster) return ensure_partial(c, c->split[pi]);
+        return DM_OK;
+    }
+    const int defv = precision == DM_FP32C ? kDefaultVariant32 : kDefaultVariant64;
+    int best_v = defv, best_s = model_split(ctx, kVariants[defv], c->n, c->n_pad);
+    if (ctx->autotune) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        DM_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return ctx->fail(DM_ERR_STATE, "autotuning needs an uncaptured stream (run one step first)");
+        cudaEvent_t a, b;
+        DM_CUDA(ctx, cudaEventCreate(&a));
+        DM_CUDA(ctx, cudaEventCreate(&b));
+        float best_ms = 1e30f;
+        const bool big = (double)c->n * c->n > 4e9;  // ~64k particles: keep tuning short
+        for (int vi = 0; vi < kNumVariants; vi++) {
+            const Variant &k = kVariants[vi];
+            if (k.precision != precision) continue;
+            const int sm = model_split(ctx, k, c->n, c->n_pad);
+            std::vector<int> cands = {sm};
+            const int extra_c[] = {1, 2, 3, 4, 6, 8, 12, 16};
+            const int extra_g[] = {1, 2, 4, 8, 12, 16, 24, 32, 48, 64};
+            if (!big) {
+                if (k.cluster) cands.insert(cands.end(), std::begin(extra_c), std::end(extra_c));
+                else cands.insert(cands.end(), std::begin(extra_g), std::end(extra_g));
+            }
+            std::sort(cands.begin(), cands.end());
+            cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+            for (int S : cands) {
+                if (S > 1 && c->n_pad / S < 64 * variant_groups(k)) continue;
+                if (k.cluster) {
+                    int nc = 0;
+                    cudaLaunchAttribute attr[1];
+                    cudaLaunchConfig_t cfg = make_cfg(ctx, k, (c->n + k.tile - 1) / k.tile, S, attr);
+                    if (cudaOccupancyMaxActiveClusters(&nc, k.fn, &cfg) != cudaSuccess || nc <= 0) {
+                        cudaGetLastError();
+                        continue;
+                    }
+                } else {
+                    int rc = ensure_partial(c, S);
+                    if (rc) return rc;
+                }
+                int rc = launch_variant(c, vi, S, 1, kModeForceOnly, 0.0, nullptr);  // warm-up
+                if (rc) return rc;
+                const int reps = big ? 1 : 3;
+                DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
+                for (int r = 0; r < reps; r++) {
+                    rc = launch_variant(c, vi, S, 1, kModeForceOnly, 0.0, nullptr);
+                    if (rc) return rc;
+                }
+                DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
+                DM_CUDA(ctx, cudaEventSynchronize(b));
+                float ms = 0.0f;
+                DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+                ms /= reps;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best_v = vi;
+                    best_s = S;
+                }
+            }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    c->tuned_variant[pi] = best_v;
+    c->split[pi] = best_s;
+    ctx->tune_cache[key] = {best_v, best_s};
+    if (!kVariants[best_v].cluster) return ensure_partial(c, best_s);
     return DM_OK;
 }
 
@@ -815,6 +974,74 @@ int dm_cloud_diagnostics(dm_cloud *c, double out[5]) {
     for (int k = 0; k < 5; k++) out[k] = 0.0;
     for (int b = 0; b < blocks; b++)
         for (int k = 0; k < 5; k++) out[k] += h[(size_t)b * 5 + k];
+    return DM_OK;
+}
+
+int dm_ctx_set_autotune(dm_ctx *ctx, int enable) {
+    if (!ctx) return DM_ERR_ARG;
+    ctx->autotune = enable != 0;
+    ctx->tune_cache.clear();
+    return DM_OK;
+}
+
+int dm_cloud_autotune(dm_cloud *c, int precision, char *variant, size_t len, int *split) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    if (precision != DM_FP64 && precision != DM_FP32C) return ctx->fail(DM_ERR_ARG, "bad precision %d", precision);
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = ensure_kernel_attrs(ctx);
+    if (rc) return rc;
+    const int pi = precision == DM_FP32C ? 1 : 0;
+    if (c->tuned_variant[pi] < 0) {
+        rc = tune_precision(c, precision);
+        if (rc) return rc;
+    }
+    if (variant && len) snprintf(variant, len, "%s", kVariants[c->tuned_variant[pi]].name);
+    if (split) *split = c->split[pi];
+    return DM_OK;
+}
+
+int dm_kernel_variants(char *buf, size_t len) {
+    if (!buf || len == 0) return DM_ERR_ARG;
+    std::string out;
+    for (int v = 0; v < kNumVariants; v++) {
+        if (v) out += ";";
+        out += kVariants[v].name;
+    }
+    snprintf(buf, len, "%s", out.c_str());
+    return DM_OK;
+}
+
+int dm_cloud_set_kernel(dm_cloud *c, const char *variant, int split) {
+    if (!c || !variant) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    int vi = -1;
+    for (int v = 0; v < kNumVariants; v++)
+        if (std::strcmp(kVariants[v].name, variant) == 0) vi = v;
+    if (vi < 0) return ctx->fail(DM_ERR_ARG, "unknown kernel variant '%s'", variant);
+    const Variant &k = kVariants[vi];
+    const int smax = k.cluster ? 16 : kMaxSplitGlobal;
+    if (split < 0 || split > smax) return ctx->fail(DM_ERR_ARG, "split %d outside [0, %d]", split, smax);
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = ensure_kernel_attrs(ctx);
+    if (rc) return rc;
+    if (split == 0) split = model_split(ctx, k, c->n, c->n_pad);
+    if (k.cluster) {
+        int nc = 0;
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = make_cfg(ctx, k, (c->n + k.tile - 1) / k.tile, split, attr);
+        if (cudaOccupancyMaxActiveClusters(&nc, k.fn, &cfg) != cudaSuccess || nc <= 0) {
+            cudaGetLastError();
+            return ctx->fail(DM_ERR_UNSUPPORTED, "cluster of %d CTAs of %s cannot be scheduled", split, k.name);
+        }
+    } else {
+        rc = ensure_partial(c, split);
+        if (rc) return rc;
+    }
+    const int pi = k.precision == DM_FP32C ? 1 : 0;
+    c->tuned_variant[pi] = vi;
+    c->split[pi] = split;
+    c->drop_graphs();
     return DM_OK;
 }
 

@@ -159,8 +159,13 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
     kahan_add(sy, cy, s * dy);
 }
 
-template <int NW, int ILP, int TC>
-__global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+// CL = true: the S ranks of a tile form a thread-block cluster, combine
+// through distributed shared memory and run the stage epilogue in the same
+// launch.  CL = false: plain blocks; each writes its partial sums to global
+// memory and stage_finish (below) completes the stage.
+template <int NW, int ILP, int TC, bool CL>
+__global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
+    pair_stage_fp32c(const StageParams P, const ExpConsts E) {
     constexpr int NT = NW * 32;
     constexpr int TILE = 32 * ILP;  // particles per i tile
     static_assert(ILP <= 4, "queue counts are packed in one 32-bit word");
@@ -174,9 +179,8 @@ __global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams
     float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);    // [NW][ILP][32]
     float4 *s_red = s_acc + NW * ILP * 32;                                 // [TILE]
 
-    cg::cluster_group cl = cg::this_cluster();
-    const int S = (int)cl.num_blocks();
-    const int rank = (int)cl.block_rank();
+    const int S = CL ? (int)cg::this_cluster().num_blocks() : P.split;
+    const int rank = CL ? (int)cg::this_cluster().block_rank() : (int)(blockIdx.x % P.split);
     const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
@@ -338,21 +342,42 @@ __global__ void __launch_bounds__(NW * 32, 3) pair_stage_fp32c(const StageParams
             kahan_add(sy, cy, v.y);
             kahan_add(sy, cy, -v.w);
         }
-        s_red[e] = make_float4(sx, sy, cx, cy);
+        if constexpr (CL) s_red[e] = make_float4(sx, sy, cx, cy);
+        else if (tile * TILE + e < n) P.partial[(size_t)rank * n_pad + tile * TILE + e] = make_float4(sx, sy, cx, cy);
     }
-    cl.sync();
-    if (fin_e >= 0) {
-        const int i = tile * TILE + fin_e;
+    if constexpr (CL) {
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();
+        if (fin_e >= 0) {
+            const int i = tile * TILE + fin_e;
+            double fx = 0.0, fy = 0.0;
+            for (int r = 0; r < S; r++) {
+                const float4 v = *cl.map_shared_rank(s_red + fin_e, r);
+                fx += (double)v.x - (double)v.z;
+                fy += (double)v.y - (double)v.w;
+            }
+            stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
+        }
+        stage_step_advance(P);
+        cl.sync();
+    }
+}
+
+// Completes a stage after a non-cluster pair launch: per particle, the
+// split partial sums in rank order (FP64), then the stage epilogue.  One
+// particle per thread: the FP64 work runs in full warps on every SM.
+static __global__ void __launch_bounds__(128) stage_finish(const StageParams P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.c.n) {
         double fx = 0.0, fy = 0.0;
-        for (int r = 0; r < S; r++) {
-            const float4 v = *cl.map_shared_rank(s_red + fin_e, r);
+        for (int r = 0; r < P.split; r++) {
+            const float4 v = P.partial[(size_t)r * P.c.n_pad + i];
             fx += (double)v.x - (double)v.z;
             fy += (double)v.y - (double)v.w;
         }
         stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
     }
     stage_step_advance(P);
-    cl.sync();
 }
 
 // ---------------------------------------------------------------------------

@@ -113,6 +113,14 @@ int dm_last_error(const dm_ctx *ctx, char *buf, size_t len);
 int dm_ctx_profile_enable(dm_ctx *ctx, int enable);
 int dm_ctx_profile_read(dm_ctx *ctx, double *total_ms, long long *launches, double *pairs);
 
+/* Autotuning of the pair kernels (default on).  On a cloud's first step (or
+ * dm_cloud_autotune) every compiled kernel variant of the precision is timed
+ * on that cloud over a set of j splits (force-only launches, no state
+ * change) and the fastest is kept; results are cached per (n, precision) in
+ * the context.  Off: a fixed default variant with a cost-model split.  No
+ * reference counterpart. */
+int dm_ctx_set_autotune(dm_ctx *ctx, int enable);
+
 /* Measures this GPU's FP32 FMA (kind 0) or FP64 FMA (kind 1) throughput
  * [TFLOP/s] with a dependent-chain-free FMA loop; used as the roofline peak. */
 int dm_probe_peak(dm_ctx *ctx, int kind, double *tflops);
@@ -183,6 +191,17 @@ int dm_cloud_modify_timestep(dm_cloud *cloud, double init_dt, float *min_dist,
  * Yukawa potential energy (pairs with kappa*r < 10), out[2] confinement
  * potential energy, out[3..4] momentum.  No reference counterpart. */
 int dm_cloud_diagnostics(dm_cloud *cloud, double out[5]);
+
+/* Runs (or reuses) the autotuner for `precision` and reports the chosen
+ * kernel variant name and j split. */
+int dm_cloud_autotune(dm_cloud *cloud, int precision, char *variant, size_t len, int *split);
+
+/* Names of the compiled pair-kernel variants, ';'-separated. */
+int dm_kernel_variants(char *buf, size_t len);
+
+/* Pins the cloud to one kernel variant (by name) and j split (0 = cost
+ * model) instead of the autotuner's choice, for its precision. */
+int dm_cloud_set_kernel(dm_cloud *cloud, const char *variant, int split);
 
 /* The device keeps the cloud in Morton (space-filling-curve) order so each
  * warp's particles are spatially compact and the pair kernels' cutoff test

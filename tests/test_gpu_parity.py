@@ -288,3 +288,38 @@ def test_reorder_interval_does_not_change_fp64_results_beyond_rounding(gpu_ctx):
     for o in outs[1:]:
         for a, b in zip(o, outs[0]):
             assert rel(a, b) < 1e-13
+
+
+def _variants(prec):
+    from demon_simulation_code_gb300 import _lib
+
+    return [v for v in _lib.kernel_variants() if v.startswith(prec + "<")]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_every_kernel_variant_and_split_is_correct(gpu_ctx, oracle_lib, prec):
+    """The autotuner may pick any variant/split: every one must pass parity."""
+    c0 = W.disk_cloud(3000, 2.5e-3, 21)
+    rx, ry = oracle_lib.forces(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m,
+                               oracle.make_params(**c0.params()))
+    names = _variants(prec)
+    assert names
+    for name in names:
+        for split in (1, 2, 3, 5, 8, 16, 0):
+            c = DeviceCloud.from_cloud(gpu_ctx, c0)
+            try:
+                c.set_kernel(name, split)
+            except Exception:  # e.g. a cluster size the device cannot schedule
+                continue
+            fx, fy = c.eval_forces(prec)
+            assert e_F(fx, fy, rx, ry) <= TOL[prec], (name, split)
+            c.step(2, 1e-4, prec)  # stage path through the same variant
+            assert np.all(np.isfinite(c.download()[0]))
+
+
+def test_autotuner_reports_a_variant(gpu_ctx):
+    c = DeviceCloud.from_cloud(gpu_ctx, W.disk_cloud(4096, 4e-3, 2))
+    name, split = c.autotune("fp32c")
+    assert name.startswith("fp32c<") and split >= 1
+    name64, split64 = c.autotune("fp64")
+    assert name64.startswith("fp64<") and split64 >= 1
