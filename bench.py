@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel", default=None, help="pin a kernel variant (skips the autotuner)")
+    ap.add_argument("--split", type=int, default=0, help="j split for --kernel (0 = cost model)")
     return ap.parse_args()
 
 
@@ -254,6 +256,8 @@ def run_gb300(args, world, rank, local):
         step_ms[:] = ms
         return sum(ms) / 1e3
 
+    if args.kernel:
+        cloud.set_kernel(args.kernel, args.split)
     tuned = cloud.autotune(args.precision)  # autotuner: variant x split on this cloud
     # warm-up (untimed)
     cloud.step(max(args.warmup, 3), w.dt, args.precision)
@@ -263,8 +267,10 @@ def run_gb300(args, world, rank, local):
     ctx.profile(True)
     barrier()
     torch.cuda.synchronize()
+    l0 = ctx.launch_count()
     with ClockSampler(local) as clk:
         elapsed = timed_steps(args.precision, args.steps)
+    launches_timed = ctx.launch_count() - l0
     pair_ms, launches, pairs_prof = ctx.profile_read()
     main_step_ms = list(step_ms)
     ctx.profile(False)
@@ -350,7 +356,7 @@ def run_gb300(args, world, rank, local):
                     "d2h_bytes_per_step": 4 * 8 * n, "steps": args.e2e_steps},
             "step_ms_percentiles": {p: float(np.percentile(main_step_ms, q))
                                     for p, q in (("p10", 10), ("p50", 50), ("p90", 90), ("max", 100))},
-            "gpu_launches": 4 * args.steps,
+            "gpu_launches": launches_timed,
             "roofline": {"bound": "fp32-pipe", "kernel": kname, "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "traffic": traffic,

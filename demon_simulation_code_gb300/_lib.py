@@ -59,6 +59,7 @@ SIGNATURES = {
     "dm_ctx_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "dm_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "dm_ctx_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dm_ctx_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "dm_ctx_profile_read": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_longlong), _dp]),
     "dm_probe_peak": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "dm_ctx_set_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

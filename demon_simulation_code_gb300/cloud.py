@@ -52,6 +52,11 @@ class Context:
     def synchronize(self):
         check(self.lib.dm_ctx_synchronize(self.h), self.h)
 
+    def launch_count(self) -> int:
+        v = ctypes.c_longlong()
+        check(self.lib.dm_ctx_launch_count(self.h, ctypes.byref(v)), self.h)
+        return v.value
+
     def profile(self, enable: bool):
         check(self.lib.dm_ctx_profile_enable(self.h, int(enable)), self.h)
 

@@ -45,6 +45,7 @@ struct dm_ctx {
     std::string err;
     bool prof = false;
     bool autotune = true;
+    long long launches = 0;  // kernels this library has launched on the context
     std::map<long long, std::pair<int, int>> tune_cache;  // (n, precision) -> (variant, split)
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
     size_t prof_used = 0;
@@ -93,6 +94,7 @@ struct dm_cloud {
     int reorder_interval = 4;   // steps between Morton re-sorts (0 = never)
     bool order_dirty = true;    // re-sort before the next step
     unsigned long long host_steps = 0;  // RK4 steps enqueued so far
+    long long graph_launches = 0;       // kernels in one replay of the step graph
     std::map<GraphKey, cudaGraphExec_t> graphs;
     cudaStream_t graph_stream = nullptr;  // stream the graphs were built for
 
@@ -316,9 +318,11 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = make_cfg(ctx, k, ntiles, S, attr);
     DM_CUDA(ctx, k.launch(&cfg, P));
+    ctx->launches++;
     if (!k.cluster) {
         stage_finish<<<(c->n + 127) / 128, 128, 0, ctx->stream>>>(P);
         DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches++;
     }
     return DM_OK;
 }
@@ -481,6 +485,7 @@ int reorder(dm_cloud *c) {
     permute_commit<<<grid, 256, 0, s>>>(c->d, z);
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
     DM_CUDA(ctx, cudaGetLastError());
+    ctx->launches += 5 + 3 * (kSortBits / kSortDigitBits);
     c->order_dirty = false;
     return DM_OK;
 }
@@ -522,10 +527,13 @@ int run_steps(dm_cloud *c, int nsteps, double dt, int precision) {
     if (it == c->graphs.end()) {
         cudaGraph_t g = nullptr;
         const unsigned long long saved = c->host_steps;
+        const long long saved_launches = ctx->launches;
         DM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         int rc = enqueue_steps(c, kGraphSteps, dt, precision);
         cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
         c->host_steps = saved;  // capture recorded the steps, it did not run them
+        c->graph_launches = ctx->launches - saved_launches;
+        ctx->launches = saved_launches;
         if (rc) {
             if (g) cudaGraphDestroy(g);
             return rc;
@@ -541,6 +549,7 @@ int run_steps(dm_cloud *c, int nsteps, double dt, int precision) {
     for (int r = 0; r < reps; r++) {
         DM_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
         c->host_steps += kGraphSteps;
+        ctx->launches += c->graph_launches;
     }
     return enqueue_steps(c, nsteps - reps * kGraphSteps, dt, precision);
 }
@@ -622,6 +631,12 @@ int dm_last_error(const dm_ctx *ctx, char *buf, size_t len) {
     if (!buf || len == 0) return DM_ERR_ARG;
     const std::string &s = ctx ? ctx->err : g_create_error;
     snprintf(buf, len, "%s", s.c_str());
+    return DM_OK;
+}
+
+int dm_ctx_launch_count(dm_ctx *ctx, long long *count) {
+    if (!ctx || !count) return DM_ERR_ARG;
+    *count = ctx->launches;
     return DM_OK;
 }
 
@@ -797,6 +812,7 @@ int dm_cloud_upload(dm_cloud *c, const double *x, const double *y, const double 
     set_identity<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->d.orig, c->n);
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
     DM_CUDA(ctx, cudaGetLastError());
+    ctx->launches += 3;
     c->order_dirty = true;
     return DM_OK;
 }
@@ -810,6 +826,7 @@ int dm_cloud_download(dm_cloud *c, double *x, double *y, double *vx, double *vy)
     scatter_to_caller<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(
         c->d.orig, c->n, c->d.x, c->d.y, c->d.vx, c->d.vy, st[0], st[1], st[2], st[3]);
     DM_CUDA(ctx, cudaGetLastError());
+    ctx->launches++;
     if (x) DM_CUDA(ctx, cudaMemcpyAsync(x, st[0], bytes, cudaMemcpyDeviceToHost, ctx->stream));
     if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, st[1], bytes, cudaMemcpyDeviceToHost, ctx->stream));
     if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, st[2], bytes, cudaMemcpyDeviceToHost, ctx->stream));

@@ -111,6 +111,9 @@ int dm_last_error(const dm_ctx *ctx, char *buf, size_t len);
  * summed duration [ms], the launch count and the ordered pairs those
  * launches covered, then resets the counters. */
 int dm_ctx_profile_enable(dm_ctx *ctx, int enable);
+/* Kernels this library has launched on the context so far (graph replays
+ * count every kernel node). */
+int dm_ctx_launch_count(dm_ctx *ctx, long long *count);
 int dm_ctx_profile_read(dm_ctx *ctx, double *total_ms, long long *launches, double *pairs);
 
 /* Autotuning of the pair kernels (default on).  On a cloud's first step (or
