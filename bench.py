@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--batch-steps", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", default=None, help="pin a kernel variant (skips the autotuner)")
     ap.add_argument("--split", type=int, default=0, help="j split for --kernel (0 = cost model)")
@@ -332,6 +333,29 @@ def run_gb300(args, world, rank, local):
     kname = "pair_stage_fp32c" if args.precision == "fp32c" else "pair_stage_fp64"
     traffic = traffic_from_profiles(kname, w.name)
 
+    # batched workload (256 clouds of uneven N, one persistent launch per stage)
+    batch = None
+    if args.batch_steps > 0:
+        from demon_simulation_code_gb300 import DeviceBatch
+
+        wb = W.batch256()
+        bt = DeviceBatch(ctx, wb.clouds)
+        bt.step(4, wb.dt)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        bt.step(args.batch_steps, wb.dt)
+        b.record(stream)
+        torch.cuda.synchronize()
+        el = a.elapsed_time(b) / 1e3
+        name, nitems, grid = bt.info()
+        batch = {"workload": wb.name, "value": 4.0 * wb.pairs_per_eval * args.batch_steps / el,
+                 "unit": UNIT, "steps": args.batch_steps, "ms_per_step": el / args.batch_steps * 1e3,
+                 "variant": name, "work_items": nitems, "persistent_grid": grid,
+                 "graph_captured": args.batch_steps >= 16}
+        bt.close()
+
     cpu = None
     if rank == 0 and not args.no_cpu and args.cpu_steps > 0:
         threads = cpu_threads()
@@ -364,6 +388,7 @@ def run_gb300(args, world, rank, local):
                          "avg_launch_us": avg_launch_s * 1e6,
                          "peak_source": "in-run FP32 FMA probe (dm_probe_peak); "
                                         "MEASURED_PEAKS.json has no FP32 figure"},
+            "batch": batch,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

@@ -6,4 +6,4 @@ include/demon_gb300.h).  This package holds its ctypes binding
 workloads (``workloads``) and the build script (``build``).
 """
 from ._lib import DM_FP32C, DM_FP64, DemonError, force_params, load  # noqa: F401
-from .cloud import Context, DeviceCloud  # noqa: F401
+from .cloud import Context, DeviceBatch, DeviceCloud  # noqa: F401

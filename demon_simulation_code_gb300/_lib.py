@@ -88,6 +88,16 @@ SIGNATURES = {
     "dm_cloud_set_reorder_interval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dm_cloud_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dm_cloud_get_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "dm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp, _dp,
+                                       _dp, _dp, _dp, _dp, ctypes.POINTER(ForceParams),
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "dm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dm_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int]),
+    "dm_batch_eval_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
+    "dm_batch_download": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+    "dm_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
+                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "dm_batch_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dm_diagnostics_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.POINTER(ForceParams),

@@ -185,3 +185,60 @@ class DeviceCloud:
         v = ctypes.c_uint64()
         self._chk(self.lib.dm_cloud_get_step_counter(self.h, ctypes.byref(v)))
         return v.value
+
+
+class DeviceBatch:
+    """Many independent clouds advanced together (dm_batch)."""
+
+    def __init__(self, ctx: Context, clouds):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.ns = [int(c.n) for c in clouds]
+        cat = [np.ascontiguousarray(np.concatenate([getattr(c, k) for c in clouds]), dtype=np.float64)
+               for k in ("x", "y", "vx", "vy", "q", "m")]
+        params = (_lib.ForceParams * len(clouds))(*[_lib.force_params(**c.params()) for c in clouds])
+        nn = (ctypes.c_int * len(clouds))(*self.ns)
+        h = ctypes.c_void_p()
+        check(self.lib.dm_batch_create(ctx.h, len(clouds), nn, *(ptr(a) for a in cat), params,
+                                       ctypes.byref(h)), ctx.h)
+        self.h = h
+        self.total = sum(self.ns)
+
+    def close(self):
+        if self.h:
+            self.lib.dm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, nsteps: int, dt: float, precision="fp32c"):
+        check(self.lib.dm_batch_step(self.h, int(nsteps), float(dt), _prec(precision)), self.ctx.h)
+
+    def eval_forces(self, precision="fp32c"):
+        fx = np.empty(self.total)
+        fy = np.empty(self.total)
+        check(self.lib.dm_batch_eval_forces(self.h, _prec(precision), ptr(fx), ptr(fy)), self.ctx.h)
+        return fx, fy
+
+    def download(self):
+        out = [np.empty(self.total) for _ in range(4)]
+        check(self.lib.dm_batch_download(self.h, *(ptr(v) for v in out)), self.ctx.h)
+        return tuple(out)
+
+    def split(self, arr):
+        """Splits a concatenated array into per-cloud arrays."""
+        return np.split(arr, np.cumsum(self.ns)[:-1])
+
+    def info(self):
+        buf = ctypes.create_string_buffer(128)
+        ni = ctypes.c_int()
+        g = ctypes.c_int()
+        check(self.lib.dm_batch_info(self.h, buf, len(buf), ctypes.byref(ni), ctypes.byref(g)), self.ctx.h)
+        return buf.value.decode(), ni.value, g.value
+
+    def set_step_counter(self, step: int):
+        check(self.lib.dm_batch_set_step_counter(self.h, int(step)), self.ctx.h)

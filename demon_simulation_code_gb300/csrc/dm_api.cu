@@ -19,6 +19,7 @@
 #include "dm_misc.cuh"
 #include "dm_pair.cuh"
 #include "dm_sort.cuh"
+#include "dm_batch.cuh"
 
 using namespace dm;
 
@@ -1089,6 +1090,451 @@ int dm_cloud_get_step_counter(dm_cloud *c, uint64_t *step) {
     DM_CUDA(ctx, cudaMemcpyAsync(&v, c->d.step_ctr, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
     DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     *step = v;
+    return DM_OK;
+}
+
+
+// ===========================================================================
+// Batched clouds
+// ===========================================================================
+}  // extern "C"
+
+namespace {
+
+struct BatchVariant {
+    const char *name;
+    int nt, tile;
+    size_t smem;
+    const void *fn;
+    cudaError_t (*launch)(dim3, dim3, size_t, cudaStream_t, const StageParams &, const BatchCloud *,
+                          const int2 *, int, unsigned int *);
+};
+
+template <int NW, int ILP, int TC>
+cudaError_t launch_batch(dim3 g, dim3 b, size_t smem, cudaStream_t s, const StageParams &P,
+                         const BatchCloud *desc, const int2 *items, int nitems, unsigned int *ctr) {
+    batch_stage_fp32c<NW, ILP, TC><<<g, b, smem, s>>>(P, desc, items, nitems, ctr, exp_consts());
+    return cudaGetLastError();
+}
+
+#define DM_BATCH_VARIANT(NW, ILP, TC)                                                            \
+    {"batch_fp32c<" #NW "," #ILP "," #TC ">", NW * 32, 32 * ILP, Fp32cSmem<NW, ILP, TC>::bytes,  \
+     (const void *)batch_stage_fp32c<NW, ILP, TC>, launch_batch<NW, ILP, TC>}
+
+const BatchVariant kBatchVariants[] = {
+    DM_BATCH_VARIANT(8, 4, 256),
+    DM_BATCH_VARIANT(4, 4, 256),
+    DM_BATCH_VARIANT(8, 2, 256),
+    DM_BATCH_VARIANT(4, 2, 128),
+};
+constexpr int kNumBatchVariants = (int)(sizeof(kBatchVariants) / sizeof(kBatchVariants[0]));
+
+}  // namespace
+
+struct dm_batch {
+    dm_ctx *ctx = nullptr;
+    int nclouds = 0, total = 0, total_pad = 0;
+    void *block = nullptr;
+    CloudDev d{};
+    std::vector<BatchCloud> hdesc;
+    std::vector<int> hn;
+    BatchCloud *ddesc = nullptr;
+    int *dseg = nullptr;
+    unsigned int *dcounter = nullptr;  // [4] work-item counters, one per stage
+    int2 *ditems[kNumBatchVariants] = {nullptr};
+    int nitems[kNumBatchVariants] = {0};
+    int grid[kNumBatchVariants] = {0};
+    unsigned long long *dbbox = nullptr;
+    SortScratch sort{};
+    int sort_blocks = 0;
+    int mbits = 24;
+    double *d_fx = nullptr, *d_fy = nullptr;
+    int variant = -1;
+    int reorder_interval = 4;
+    bool order_dirty = true;
+    unsigned long long host_steps = 0;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    cudaStream_t graph_stream = nullptr;
+    std::vector<void *> extra;
+
+    void drop_graphs() {
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
+    ~dm_batch() {
+        drop_graphs();
+        for (void *p : extra) cudaFree(p);
+        if (block) cudaFree(block);
+    }
+};
+
+namespace {
+
+int batch_launch_stage(dm_batch *B, int stage, int mode, double dt) {
+    dm_ctx *ctx = B->ctx;
+    const BatchVariant &k = kBatchVariants[B->variant];
+    StageParams P{};
+    P.c = B->d;
+    P.stage = stage;
+    P.mode = mode;
+    P.dt = dt;
+    P.coulomb = B->d.coulomb;
+    P.fx_out = B->d_fx;
+    P.fy_out = B->d_fy;
+    const int slot = (mode == kModeForceOnly) ? 0 : stage - 1;
+    DM_CUDA(ctx, k.launch(dim3(B->grid[B->variant]), dim3(k.nt), k.smem, ctx->stream, P, B->ddesc,
+                          B->ditems[B->variant], B->nitems[B->variant], B->dcounter + slot));
+    ctx->launches++;
+    return DM_OK;
+}
+
+int batch_reorder(dm_batch *B) {
+    dm_ctx *ctx = B->ctx;
+    cudaStream_t s = ctx->stream;
+    const int n = B->total;
+    const int grid = (n + 255) / 256;
+    SortScratch &z = B->sort;
+    const size_t half = 2 * sizeof(unsigned long long);
+    for (int c = 0; c < B->nclouds; c++) {  // one memset pair would do; keep it simple and capturable
+        (void)c;
+    }
+    // min entries to all-ones, max entries to zero: bbox layout [cloud][4]
+    DM_CUDA(ctx, cudaMemsetAsync(B->dbbox, 0xFF, 4 * sizeof(unsigned long long) * B->nclouds, s));
+    (void)half;
+    batch_init_bbox_max<<<(B->nclouds + 127) / 128, 128, 0, s>>>(B->dbbox, B->nclouds);
+    batch_bbox<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbbox);
+    batch_keys<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbbox, B->mbits, z.keys[0], z.vals[0]);
+    int cur = 0;
+    int passes = 0;
+    const int bits = B->mbits + 32 - __builtin_clz((unsigned)std::max(B->nclouds - 1, 1));
+    for (int shift = 0; shift < bits; shift += kSortDigitBits) {
+        radix_hist<<<B->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], n, shift, z.hist);
+        radix_scan<<<1, 1024, 0, s>>>(z.hist, kSortBuckets * B->sort_blocks);
+        radix_scatter<<<B->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], z.vals[cur], z.keys[cur ^ 1],
+                                                               z.vals[cur ^ 1], n, shift, z.hist);
+        cur ^= 1;
+        passes++;
+    }
+    permute_gather<<<grid, 256, 0, s>>>(B->d, z.vals[cur], z);
+    permute_commit<<<grid, 256, 0, s>>>(B->d, z);
+    batch_init_positions<<<(B->total_pad + 255) / 256, 256, 0, s>>>(B->d, B->ddesc, B->dseg);
+    DM_CUDA(ctx, cudaGetLastError());
+    ctx->launches += 6 + 3 * passes;
+    B->order_dirty = false;
+    return DM_OK;
+}
+
+int batch_enqueue_steps(dm_batch *B, int nsteps, double dt) {
+    dm_ctx *ctx = B->ctx;
+    for (int s = 0; s < nsteps; s++) {
+        if (B->order_dirty || (B->reorder_interval > 0 && B->host_steps % (unsigned)B->reorder_interval == 0)) {
+            int rc = batch_reorder(B);
+            if (rc) return rc;
+        }
+        DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, 4 * sizeof(unsigned int), ctx->stream));
+        for (int st = 1; st <= 4; st++) {
+            int rc = batch_launch_stage(B, st, kModeStep, dt);
+            if (rc) return rc;
+        }
+        B->host_steps++;
+    }
+    return DM_OK;
+}
+
+int batch_tune(dm_batch *B) {
+    dm_ctx *ctx = B->ctx;
+    int rc = DM_OK;
+    for (int v = 0; v < kNumBatchVariants; v++) {
+        const BatchVariant &k = kBatchVariants[v];
+        DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
+        int per_sm = 0;
+        DM_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.nt, k.smem));
+        B->grid[v] = std::max(1, per_sm) * ctx->num_sms;
+        // work items (cloud, tile), largest clouds first
+        std::vector<int2> items;
+        std::vector<int> order(B->nclouds);
+        for (int c = 0; c < B->nclouds; c++) order[c] = c;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return B->hn[a] > B->hn[b]; });
+        for (int c : order)
+            for (int t = 0; t * k.tile < B->hn[c]; t++) items.push_back(make_int2(c, t));
+        B->nitems[v] = (int)items.size();
+        if (!B->ditems[v]) {
+            DM_CUDA(ctx, cudaMalloc((void **)&B->ditems[v], items.size() * sizeof(int2)));
+            B->extra.push_back(B->ditems[v]);
+        }
+        DM_CUDA(ctx, cudaMemcpyAsync(B->ditems[v], items.data(), items.size() * sizeof(int2),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+    }
+    int best = 0;
+    if (ctx->autotune) {
+        cudaEvent_t a, b;
+        DM_CUDA(ctx, cudaEventCreate(&a));
+        DM_CUDA(ctx, cudaEventCreate(&b));
+        float best_ms = 1e30f;
+        for (int v = 0; v < kNumBatchVariants; v++) {
+            B->variant = v;
+            DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
+            rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);  // warm-up
+            if (rc) return rc;
+            DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
+            DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
+            rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);
+            if (rc) return rc;
+            DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
+            DM_CUDA(ctx, cudaEventSynchronize(b));
+            float ms = 0.0f;
+            DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = v;
+            }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    B->variant = best;
+    return DM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, const double *y,
+                    const double *vx, const double *vy, const double *q, const double *m,
+                    const dm_force_params *params, dm_batch **out) {
+    if (!ctx || !out || nclouds < 1 || !n || !x || !y || !vx || !vy || !q || !m || !params)
+        return ctx ? ctx->fail(DM_ERR_ARG, "dm_batch_create: bad argument") : DM_ERR_ARG;
+    if (nclouds > 65536) return ctx->fail(DM_ERR_ARG, "dm_batch_create: at most 65536 clouds");
+    *out = nullptr;
+    long long total = 0;
+    for (int c = 0; c < nclouds; c++) {
+        if (n[c] < 1) return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d has n = %d", c, n[c]);
+        const long long kn = params[c].flags & ~(kConfinement | kDrag | kShieldedCoulomb | kThermal | kRectConfinement);
+        if (kn) return ctx->fail(DM_ERR_UNSUPPORTED, "dm_batch_create: unsupported force flags in cloud %d", c);
+        if ((params[c].flags & kShieldedCoulomb) && !(params[c].shielding > 0.0))
+            return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d shielding must be positive", c);
+        total += n[c];
+    }
+    if (total > (1LL << 30)) return ctx->fail(DM_ERR_ARG, "dm_batch_create: too many particles");
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    dm_batch *B = new dm_batch();
+    B->ctx = ctx;
+    B->nclouds = nclouds;
+    B->total = (int)total;
+    B->total_pad = ((int)total + 63) & ~63;
+    B->hn.assign(n, n + nclouds);
+    const int cbits = 32 - __builtin_clz((unsigned)std::max(nclouds - 1, 1));
+    B->mbits = std::min(24, (32 - cbits) & ~1);
+    const double coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);
+    const int np = B->total_pad;
+    const size_t nd = align256((size_t)np * sizeof(double));
+    const size_t nf4 = align256((size_t)np * sizeof(float4));
+    const size_t ni = align256((size_t)np * sizeof(int));
+    B->sort_blocks = (B->total + kSortPerBlock - 1) / kSortPerBlock;
+    const size_t nh = align256((size_t)kSortBuckets * B->sort_blocks * sizeof(uint32_t));
+    const size_t ndesc = align256((size_t)nclouds * sizeof(BatchCloud));
+    const size_t nbb = align256((size_t)nclouds * 4 * sizeof(unsigned long long));
+    const size_t bytes_total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ni * 7 + nh + ndesc + nbb + 1024;
+    cudaError_t e = cudaMalloc(&B->block, bytes_total);
+    if (e != cudaSuccess) {
+        delete B;
+        return ctx->fail(DM_ERR_NOMEM, "dm_batch_create: cudaMalloc(%zu): %s", bytes_total, cudaGetErrorString(e));
+    }
+    char *p = (char *)B->block;
+    auto takeD = [&]() { double *r = (double *)p; p += nd; return r; };
+    auto takeF4 = [&]() { float4 *r = (float4 *)p; p += nf4; return r; };
+    auto takeI = [&]() { int *r = (int *)p; p += ni; return r; };
+    CloudDev &d = B->d;
+    d.n = B->total;
+    d.n_pad = np;
+    d.coulomb = coulomb;
+    d.x = takeD(); d.y = takeD(); d.vx = takeD(); d.vy = takeD(); d.q = takeD(); d.m = takeD();
+    d.vxc = takeD(); d.vyc = takeD();
+    for (int k = 0; k < 4; k++) d.a1[k] = takeD();
+    for (int k = 0; k < 4; k++) d.a23[k] = takeD();
+    for (int b = 0; b < 2; b++) { d.px[b] = takeD(); d.py[b] = takeD(); }
+    B->d_fx = takeD();
+    B->d_fy = takeD();
+    for (int k = 0; k < 6; k++) B->sort.stage[k] = takeD();
+    for (int b = 0; b < 2; b++) { d.pa[b] = takeF4(); d.pb[b] = takeF4(); }
+    d.orig = takeI();
+    B->dseg = takeI();
+    B->sort.keys[0] = (uint32_t *)takeI();
+    B->sort.keys[1] = (uint32_t *)takeI();
+    B->sort.vals[0] = takeI();
+    B->sort.vals[1] = takeI();
+    B->sort.orig_stage = takeI();
+    B->sort.hist = (uint32_t *)p; p += nh;
+    B->ddesc = (BatchCloud *)p; p += ndesc;
+    B->dbbox = (unsigned long long *)p; p += nbb;
+    d.step_ctr = (unsigned long long *)p; p += 256;
+    d.err = (int *)p; p += 256;
+    B->dcounter = (unsigned int *)p; p += 256;
+    // host descriptors
+    B->hdesc.resize(nclouds);
+    std::vector<int> seg((size_t)B->total), orig((size_t)B->total);
+    int off = 0;
+    for (int c = 0; c < nclouds; c++) {
+        BatchCloud &bc = B->hdesc[c];
+        bc.off = off;
+        bc.n = n[c];
+        bc.pad_ = 0;
+        std::memcpy(&bc.f, &params[c], sizeof(ForceParams));
+        const double kappa = params[c].shielding;
+        bc.rc2 = (kappa > 0.0) ? (10.0 / kappa) * (10.0 / kappa) : 0.0;
+        bc.rc2_lo = (float)(bc.rc2 * (1.0 - 4e-6));
+        bc.rc2_hi = (float)(bc.rc2 * (1.0 + 4e-6));
+        bc.kappa_f = (float)kappa;
+        for (int i = 0; i < n[c]; i++) {
+            seg[off + i] = c;
+            orig[off + i] = off + i;
+        }
+        off += n[c];
+    }
+    cudaStream_t s = ctx->stream;
+    const size_t bt = (size_t)B->total * sizeof(double);
+    e = cudaMemsetAsync(B->block, 0, bytes_total, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.x, x, bt, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.y, y, bt, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.vx, vx, bt, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.vy, vy, bt, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.q, q, bt, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.m, m, bt, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B->dseg, seg.data(), seg.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.orig, orig.data(), orig.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(B->ddesc, B->hdesc.data(), nclouds * sizeof(BatchCloud), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        batch_init_positions<<<(np + 255) / 256, 256, 0, s>>>(d, B->ddesc, B->dseg);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        delete B;
+        return ctx->fail(DM_ERR_CUDA, "dm_batch_create: %s", cudaGetErrorString(e));
+    }
+    int rc = batch_tune(B);
+    if (rc) {
+        delete B;
+        return rc;
+    }
+    *out = B;
+    return DM_OK;
+}
+
+int dm_batch_destroy(dm_batch *B) {
+    if (!B) return DM_ERR_ARG;
+    cudaSetDevice(B->ctx->device);
+    cudaStreamSynchronize(B->ctx->stream);
+    delete B;
+    return DM_OK;
+}
+
+int dm_batch_step(dm_batch *B, int nsteps, double dt, int precision) {
+    if (!B) return DM_ERR_ARG;
+    dm_ctx *ctx = B->ctx;
+    if (precision != DM_FP32C)
+        return ctx->fail(DM_ERR_UNSUPPORTED, "batched clouds run the FP32C kernel; step FP64 clouds singly");
+    if (nsteps < 0 || !std::isfinite(dt)) return ctx->fail(DM_ERR_ARG, "dm_batch_step: bad nsteps/dt");
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (ctx->prof || nsteps < kGraphSteps) return batch_enqueue_steps(B, nsteps, dt);
+    if (B->graph_stream != ctx->stream) {
+        B->drop_graphs();
+        B->graph_stream = ctx->stream;
+    }
+    while (nsteps > 0 && (B->order_dirty || (B->reorder_interval > 0 && B->host_steps % kGraphSteps != 0))) {
+        int rc = batch_enqueue_steps(B, 1, dt);
+        if (rc) return rc;
+        nsteps--;
+    }
+    if (nsteps < kGraphSteps) return batch_enqueue_steps(B, nsteps, dt);
+    const GraphKey key{DM_FP32C, kGraphSteps, dt};
+    auto it = B->graphs.find(key);
+    static long long graph_launches_cache = 0;
+    if (it == B->graphs.end()) {
+        cudaGraph_t g = nullptr;
+        const unsigned long long saved = B->host_steps;
+        const long long sl = ctx->launches;
+        DM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = batch_enqueue_steps(B, kGraphSteps, dt);
+        cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+        B->host_steps = saved;
+        graph_launches_cache = ctx->launches - sl;
+        ctx->launches = sl;
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ec != cudaSuccess) return ctx->fail(DM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+        cudaGraphExec_t ge = nullptr;
+        ec = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ec != cudaSuccess) return ctx->fail(DM_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ec));
+        it = B->graphs.emplace(key, ge).first;
+    }
+    const int reps = nsteps / kGraphSteps;
+    for (int r = 0; r < reps; r++) {
+        DM_CUDA(ctx, cudaGraphLaunch(it->second, ctx->stream));
+        B->host_steps += kGraphSteps;
+        ctx->launches += graph_launches_cache;
+    }
+    return batch_enqueue_steps(B, nsteps - reps * kGraphSteps, dt);
+}
+
+int dm_batch_eval_forces(dm_batch *B, int precision, double *fx, double *fy) {
+    if (!B || !fx || !fy) return B ? B->ctx->fail(DM_ERR_ARG, "NULL output") : DM_ERR_ARG;
+    dm_ctx *ctx = B->ctx;
+    if (precision != DM_FP32C)
+        return ctx->fail(DM_ERR_UNSUPPORTED, "batched clouds run the FP32C kernel");
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
+    int rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);
+    if (rc) return rc;
+    const size_t bt = (size_t)B->total * sizeof(double);
+    DM_CUDA(ctx, cudaMemcpyAsync(fx, B->d_fx, bt, cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(fy, B->d_fy, bt, cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DM_OK;
+}
+
+int dm_batch_download(dm_batch *B, double *x, double *y, double *vx, double *vy) {
+    if (!B) return DM_ERR_ARG;
+    dm_ctx *ctx = B->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bt = (size_t)B->total * sizeof(double);
+    double **st = B->sort.stage;
+    scatter_to_caller<<<(B->total + 255) / 256, 256, 0, ctx->stream>>>(
+        B->d.orig, B->total, B->d.x, B->d.y, B->d.vx, B->d.vy, st[0], st[1], st[2], st[3]);
+    DM_CUDA(ctx, cudaGetLastError());
+    ctx->launches++;
+    if (x) DM_CUDA(ctx, cudaMemcpyAsync(x, st[0], bt, cudaMemcpyDeviceToHost, ctx->stream));
+    if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, st[1], bt, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, st[2], bt, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vy) DM_CUDA(ctx, cudaMemcpyAsync(vy, st[3], bt, cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int h = 0;
+    DM_CUDA(ctx, cudaMemcpy(&h, B->d.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        cudaMemset(B->d.err, 0, sizeof(int));
+        return ctx->fail(DM_ERR_NUMERIC, "non-finite particle position in the batch");
+    }
+    return DM_OK;
+}
+
+int dm_batch_info(dm_batch *B, char *variant, size_t len, int *nitems, int *grid) {
+    if (!B) return DM_ERR_ARG;
+    if (variant && len) snprintf(variant, len, "%s", kBatchVariants[B->variant].name);
+    if (nitems) *nitems = B->nitems[B->variant];
+    if (grid) *grid = B->grid[B->variant];
+    return DM_OK;
+}
+
+int dm_batch_set_step_counter(dm_batch *B, uint64_t step) {
+    if (!B) return DM_ERR_ARG;
+    dm_ctx *ctx = B->ctx;
+    unsigned long long v[2] = {step, step};
+    DM_CUDA(ctx, cudaMemcpy(B->d.step_ctr, v, sizeof(v), cudaMemcpyHostToDevice));
     return DM_OK;
 }
 

@@ -1,0 +1,149 @@
+// dm_batch.cuh -- many independent clouds of uneven size in one launch.
+//
+// The clouds are concatenated (caller order: cloud 0's particles, then cloud
+// 1's, ...) into one set of device arrays with no per-cloud padding; each
+// cloud keeps its own force parameters (kappa, charge, confinement, ...).
+// A stage is ONE persistent launch: every CTA repeatedly takes the next work
+// item -- (cloud, i-tile) -- from a global counter and runs the same FP32C
+// sweep as the single-cloud kernel over that cloud's j, then the stage
+// epilogue for the tile's particles.  Items are ordered by cost (largest
+// clouds first), so the dynamic hand-out is a longest-processing-time
+// schedule; since an item is computed entirely by one CTA, the result does
+// not depend on which CTA takes it (deterministic, no atomics on forces).
+#pragma once
+
+#include "dm_pair.cuh"
+#include "dm_sort.cuh"
+
+namespace dm {
+
+struct BatchCloud {
+    int off;        // first particle in the concatenated arrays
+    int n;
+    int pad_;
+    ForceParams f;
+    double rc2;
+    float rc2_lo, rc2_hi, kappa_f;
+};
+
+// A StageParams view of one cloud: pointers offset to the cloud's particles.
+__device__ __forceinline__ void batch_view(StageParams &V, const StageParams &P0, const BatchCloud &d) {
+    V = P0;
+    const int o = d.off;
+    CloudDev &c = V.c;
+    c.x += o; c.y += o; c.vx += o; c.vy += o; c.q += o; c.m += o;
+    c.vxc += o; c.vyc += o;
+    for (int k = 0; k < 4; k++) { c.a1[k] += o; c.a23[k] += o; }
+    for (int b = 0; b < 2; b++) { c.px[b] += o; c.py[b] += o; c.pa[b] += o; c.pb[b] += o; }
+    c.orig += o;  // values stay global caller indices (thermal counter, outputs)
+    c.n = d.n;
+    c.n_pad = d.n;
+    c.rc2 = d.rc2;
+    V.f = d.f;
+    V.rc2 = d.rc2;
+    V.rc2_lo = d.rc2_lo;
+    V.rc2_hi = d.rc2_hi;
+    V.kappa_f = d.kappa_f;
+}
+
+template <int NW, int ILP, int TC>
+__global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
+    batch_stage_fp32c(const StageParams P0, const BatchCloud *__restrict__ desc,
+                      const int2 *__restrict__ items, int nitems, unsigned int *counter,
+                      const ExpConsts E) {
+    constexpr int TILE = 32 * ILP;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ StageParams sV;
+    __shared__ int s_item;
+    float4 *s_red = reinterpret_cast<float4 *>(smem_raw) + Fp32cSmem<NW, ILP, TC>::red_offset;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems) break;
+        const int2 w = items[it];
+        if (tid == 0) batch_view(sV, P0, desc[w.x]);
+        __syncthreads();
+        const int tile = w.y;
+        fp32c_sweep<NW, ILP, TC>(sV, E, tile, 0, 1, smem_raw);
+        if (tid < TILE) {
+            const int i = tile * TILE + tid;
+            if (i < sV.c.n) {
+                const float4 v = s_red[tid];
+                stage_epilogue(sV, i, (double)v.x - (double)v.z, (double)v.y - (double)v.w,
+                               stage_thermal(sV, i));
+            }
+        }
+        __syncthreads();  // before the next item reuses shared memory
+    }
+    stage_step_advance(P0);
+}
+
+// --- per-cloud Morton order ------------------------------------------------
+
+// bbox rows are (min x, min y, max x, max y) in ordered bits: the min
+// entries start at all-ones (memset), the max entries at zero.
+static __global__ void batch_init_bbox_max(unsigned long long *bbox, int nclouds) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nclouds) {
+        bbox[4 * c + 2] = 0ull;
+        bbox[4 * c + 3] = 0ull;
+    }
+}
+
+static __global__ void batch_bbox(const double *__restrict__ x, const double *__restrict__ y, int n,
+                                  const int *__restrict__ seg, unsigned long long *bbox) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = x[i], b = y[i];
+    if (!(isfinite(a) && isfinite(b))) return;
+    unsigned long long *bb = bbox + 4 * seg[i];
+    atomicMin(&bb[0], ordered_bits(a));
+    atomicMin(&bb[1], ordered_bits(b));
+    atomicMax(&bb[2], ordered_bits(a));
+    atomicMax(&bb[3], ordered_bits(b));
+}
+
+// key = cloud index (high bits) | the top `mbits` bits of the 24-bit Morton
+// code within the cloud's box, so a stable sort keeps every cloud in its own
+// contiguous range.
+static __global__ void batch_keys(const double *__restrict__ x, const double *__restrict__ y, int n,
+                                  const int *__restrict__ seg, const unsigned long long *bbox,
+                                  int mbits, uint32_t *keys, int *vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int sg = seg[i];
+    const unsigned long long *bb = bbox + 4 * sg;
+    const double x0 = from_ordered_bits(bb[0]), y0 = from_ordered_bits(bb[1]);
+    const double x1 = from_ordered_bits(bb[2]), y1 = from_ordered_bits(bb[3]);
+    const double ext = fmax(x1 - x0, y1 - y0);
+    const double scale = (ext > 0.0 && isfinite(ext)) ? 4095.0 / ext : 0.0;
+    const double fx = (x[i] - x0) * scale, fy = (y[i] - y0) * scale;
+    const uint32_t qx = (fx > 0.0) ? (uint32_t)fmin(fx, 4095.0) : 0u;
+    const uint32_t qy = (fy > 0.0) ? (uint32_t)fmin(fy, 4095.0) : 0u;
+    const uint32_t morton = spread_bits12(qx) | (spread_bits12(qy) << 1);
+    keys[i] = ((uint32_t)sg << mbits) | (morton >> (24 - mbits));
+    vals[i] = i;
+}
+
+// Stage buffer 0 from the base positions, with each particle's own cloud's
+// filter bound.
+static __global__ void batch_init_positions(CloudDev c, const BatchCloud *__restrict__ desc,
+                                            const int *__restrict__ seg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c.n) {
+        CloudDev v = c;
+        v.rc2 = desc[seg[i]].rc2;
+        write_stage_position(v, 0, i, c.x[i], c.y[i]);
+    } else if (i < c.n_pad) {
+        for (int b = 0; b < 2; b++) {
+            c.px[b][i] = (double)kPadPosition;
+            c.py[b][i] = (double)kPadPosition;
+            c.pa[b][i] = make_float4(kPadPosition, kPadPosition, kPadPosition * kPadPosition, 0.0f);
+            c.pb[b][i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
+}  // namespace dm

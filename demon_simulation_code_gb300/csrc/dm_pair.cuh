@@ -95,6 +95,8 @@ struct Fp32cSmem {
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
     static constexpr size_t bytes = tile + cold + queue + acc + red;
+    // s_red, in float4 units from the start of shared memory
+    static constexpr size_t red_offset = (tile + cold + queue + acc) / sizeof(float4);
 };
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
@@ -159,48 +161,36 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
     kahan_add(sy, cy, s * dy);
 }
 
-// CL = true: the S ranks of a tile form a thread-block cluster, combine
-// through distributed shared memory and run the stage epilogue in the same
-// launch.  CL = false: plain blocks; each writes its partial sums to global
-// memory and stage_finish (below) completes the stage.
-template <int NW, int ILP, int TC, bool CL>
-__global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
-    pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+// The FP32C sweep of one i tile against rank `rank` of S of the j chunks:
+// i-side setup, filtered j loop with the compaction queue, and the combine
+// of the NW warps' Kahan sums into s_red[TILE] = (sx, sy, cx, cy).  Ends with
+// the block synchronised.  `P` may live in shared memory (batched kernel).
+// Particles are those of P.c (n = P.c.n); j at or beyond n read as padding,
+// so a cloud needs no padding of its own.
+template <int NW, int ILP, int TC>
+__device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConsts &E, int tile,
+                                            int rank, int S, unsigned char *smem_raw) {
     constexpr int NT = NW * 32;
     constexpr int TILE = 32 * ILP;  // particles per i tile
     static_assert(ILP <= 4, "queue counts are packed in one 32-bit word");
-    extern __shared__ __align__(128) unsigned char smem_raw[];
     float4 *s_x4 = reinterpret_cast<float4 *>(smem_raw);  // [TC] xh of 4 j
     float4 *s_y4 = s_x4 + TC;                              // [TC] yh
     float4 *s_b4 = s_y4 + TC;                              // [TC] xh^2 + yh^2
-    float4 *s_pb = s_b4 + TC;                              // [4*TC] (xl, yl, q, global j)
+    float4 *s_pb = s_b4 + TC;                              // [4*TC] (xl, yl, q, j)
     float4 *s_cold = s_pb + 4 * TC;                        // [ILP][32]
     int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * 32);           // [NW][ILP][32]
     float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);    // [NW][ILP][32]
     float4 *s_red = s_acc + NW * ILP * 32;                                 // [TILE]
 
-    const int S = CL ? (int)cg::this_cluster().num_blocks() : P.split;
-    const int rank = CL ? (int)cg::this_cluster().block_rank() : (int)(blockIdx.x % P.split);
-    const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
-    const int n = P.c.n, n_pad = P.c.n_pad;
+    const int n = P.c.n;
     const int st = (P.mode == kModeForceOnly) ? 1 : P.stage;
     const int b = (st - 1) & 1;
     const float4 *__restrict__ pa = P.c.pa[b];
     const float4 *__restrict__ pb = P.c.pb[b];
     int2 *my_queue = s_queue + warp * ILP * 32;
     float4 *my_acc = s_acc + warp * ILP * 32;
-
-    // This CTA finalises particles [rank*fchunk, (rank+1)*fchunk) of the tile,
-    // in whole warps: an FP64 warp instruction costs the same with 1 or 32
-    // active lanes, so the FP64 epilogue runs on as few warps as possible.
-    const int fchunk = max(32, (TILE + S - 1) / S);
-    int fin_e = -1;
-    if (tid < fchunk) {
-        const int e = rank * fchunk + tid;
-        if (e < TILE && tile * TILE + e < n) fin_e = e;
-    }
 
     // every warp owns the same TILE particles: lane l, slot k -> i = tile*TILE + k*32 + l.
     // i side duplicated into both halves of a packed pair: the packed FMAs
@@ -229,7 +219,7 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     // j chunks (4 consecutive j) are dealt round-robin: chunk c belongs to
     // rank c % S and, within this CTA, to warp (c / S) % NW.  Every warp thus
     // samples the whole cloud evenly, whatever the spatial order.
-    const int nch_all = n_pad >> 2;
+    const int nch_all = (n + 3) >> 2;
     const int my_nch = (nch_all - rank + S - 1) / S;  // chunks of this rank
     uint32_t qn = 0u;  // queue fill per slot, 8 bits per slot (warp-uniform)
 
@@ -274,12 +264,19 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
             float xs[4], ys[4], bs[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const float4 A = pa[jb + u];
-                const float4 B = pb[jb + u];
-                xs[u] = A.x;
-                ys[u] = A.y;
-                bs[u] = A.z;
-                s_pb[4 * e + u] = make_float4(B.x, B.y, A.w, __int_as_float(jb + u));
+                if (jb + u < n) {
+                    const float4 A = pa[jb + u];
+                    const float4 B = pb[jb + u];
+                    xs[u] = A.x;
+                    ys[u] = A.y;
+                    bs[u] = A.z;
+                    s_pb[4 * e + u] = make_float4(B.x, B.y, A.w, __int_as_float(jb + u));
+                } else {  // padding: never passes the filter
+                    xs[u] = kPadPosition;
+                    ys[u] = kPadPosition;
+                    bs[u] = INFINITY;
+                    s_pb[4 * e + u] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+                }
             }
             s_x4[e] = make_float4(xs[0], xs[1], xs[2], xs[3]);
             s_y4[e] = make_float4(ys[0], ys[1], ys[2], ys[3]);
@@ -329,8 +326,8 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     }
 
     // combine the NW warps in fixed order with a compensated FP32 sum (each
-    // warp's Kahan pair (s, c) stands for s - c); FP64 only once per particle
-    // below (FP64 runs at 1/64 of the FP32 rate here)
+    // warp's Kahan pair (s, c) stands for s - c); FP64 comes later, once per
+    // particle (FP64 runs at 1/64 of the FP32 rate here)
     __syncthreads();
     for (int e = tid; e < TILE; e += NT) {
         float sx = 0.0f, cx = 0.0f, sy = 0.0f, cy = 0.0f;
@@ -342,21 +339,49 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
             kahan_add(sy, cy, v.y);
             kahan_add(sy, cy, -v.w);
         }
-        if constexpr (CL) s_red[e] = make_float4(sx, sy, cx, cy);
-        else if (tile * TILE + e < n) P.partial[(size_t)rank * n_pad + tile * TILE + e] = make_float4(sx, sy, cx, cy);
+        s_red[e] = make_float4(sx, sy, cx, cy);
     }
-    if constexpr (CL) {
+    __syncthreads();
+}
+
+// CL = true: the S ranks of a tile form a thread-block cluster, combine
+// through distributed shared memory and run the stage epilogue in the same
+// launch.  CL = false: plain blocks; each writes its partial sums to global
+// memory and stage_finish (below) completes the stage.
+template <int NW, int ILP, int TC, bool CL>
+__global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
+    pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+    constexpr int TILE = 32 * ILP;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int S = CL ? (int)cg::this_cluster().num_blocks() : P.split;
+    const int rank = CL ? (int)cg::this_cluster().block_rank() : (int)(blockIdx.x % P.split);
+    const int tile = blockIdx.x / S;
+    const int tid = threadIdx.x;
+    const int n = P.c.n, n_pad = P.c.n_pad;
+    fp32c_sweep<NW, ILP, TC>(P, E, tile, rank, S, smem_raw);
+    float4 *s_red = reinterpret_cast<float4 *>(smem_raw) + Fp32cSmem<NW, ILP, TC>::red_offset;
+    if constexpr (!CL) {
+        for (int e = tid; e < TILE; e += NW * 32)
+            if (tile * TILE + e < n) P.partial[(size_t)rank * n_pad + tile * TILE + e] = s_red[e];
+    } else {
+        // finalise particles [rank*fchunk, (rank+1)*fchunk) of the tile in
+        // whole warps: an FP64 warp instruction costs the same with 1 or 32
+        // active lanes, so the FP64 epilogue runs on as few warps as possible
         cg::cluster_group cl = cg::this_cluster();
+        const int fchunk = max(32, (TILE + S - 1) / S);
         cl.sync();
-        if (fin_e >= 0) {
-            const int i = tile * TILE + fin_e;
-            double fx = 0.0, fy = 0.0;
-            for (int r = 0; r < S; r++) {
-                const float4 v = *cl.map_shared_rank(s_red + fin_e, r);
-                fx += (double)v.x - (double)v.z;
-                fy += (double)v.y - (double)v.w;
+        if (tid < fchunk) {
+            const int e = rank * fchunk + tid;
+            if (e < TILE && tile * TILE + e < n) {
+                const int i = tile * TILE + e;
+                double fx = 0.0, fy = 0.0;
+                for (int r = 0; r < S; r++) {
+                    const float4 v = *cl.map_shared_rank(s_red + e, r);
+                    fx += (double)v.x - (double)v.z;
+                    fy += (double)v.y - (double)v.w;
+                }
+                stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
             }
-            stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
         }
         stage_step_advance(P);
         cl.sync();

@@ -218,6 +218,29 @@ int dm_cloud_set_reorder_interval(dm_cloud *cloud, int steps);
 int dm_cloud_set_step_counter(dm_cloud *cloud, uint64_t step);
 int dm_cloud_get_step_counter(dm_cloud *cloud, uint64_t *step);
 
+/* ---- many clouds in one launch --------------------------------------- */
+
+/* A batch of independent clouds of uneven size, each with its own force
+ * parameters (params[c]).  Arrays are concatenated in cloud order (cloud 0's
+ * n[0] particles, then cloud 1's, ...).  Each RK4 stage of the whole batch is
+ * one persistent FP32C launch handing out (cloud, i-tile) work items, largest
+ * clouds first; kernel variants are autotuned at creation.  The reference
+ * runs one cloud per process; this has no reference counterpart beyond
+ * dm_cloud_* applied to each cloud. */
+int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x,
+                    const double *y, const double *vx, const double *vy,
+                    const double *q, const double *m,
+                    const dm_force_params *params, dm_batch **out);
+int dm_batch_destroy(dm_batch *batch);
+/* nsteps fixed-dt RK4 steps of every cloud (precision must be DM_FP32C). */
+int dm_batch_step(dm_batch *batch, int nsteps, double dt, int precision);
+/* All forces of every cloud at the current state (caller order). */
+int dm_batch_eval_forces(dm_batch *batch, int precision, double *fx, double *fy);
+int dm_batch_download(dm_batch *batch, double *x, double *y, double *vx, double *vy);
+/* The autotuned kernel variant, work-item count and persistent grid size. */
+int dm_batch_info(dm_batch *batch, char *variant, size_t len, int *nitems, int *grid);
+int dm_batch_set_step_counter(dm_batch *batch, uint64_t step);
+
 /* ---- allocation-free diagnostics ------------------------------------- */
 
 /* No counterpart in the reference.  dm_cloud_diagnostics' computation for
