@@ -98,6 +98,12 @@ SIGNATURES = {
     "dm_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "dm_batch_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "dm_adjoint_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ForceParams), ctypes.POINTER(ctypes.c_void_p)]),
+    "dm_adjoint_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dm_adjoint_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForceParams)]),
+    "dm_adjoint_forces": (ctypes.c_int, [ctypes.c_void_p] * 11),
+    "dm_adjoint_vjp": (ctypes.c_int, [ctypes.c_void_p] * 16),
     "dm_diagnostics_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.POINTER(ForceParams),

@@ -20,6 +20,7 @@
 #include "dm_pair.cuh"
 #include "dm_sort.cuh"
 #include "dm_batch.cuh"
+#include "dm_adjoint.cuh"
 
 using namespace dm;
 
@@ -1535,6 +1536,138 @@ int dm_batch_set_step_counter(dm_batch *B, uint64_t step) {
     dm_ctx *ctx = B->ctx;
     unsigned long long v[2] = {step, step};
     DM_CUDA(ctx, cudaMemcpy(B->d.step_ctr, v, sizeof(v), cudaMemcpyHostToDevice));
+    return DM_OK;
+}
+
+
+// ===========================================================================
+// Differentiable rollout support: FP64 forces and their VJP on device arrays
+// ===========================================================================
+}  // extern "C"
+
+struct dm_adjoint {
+    dm_ctx *ctx = nullptr;
+    int nclouds = 0, total = 0, nblocks = 0;
+    std::vector<AdjCloud> hdesc;
+    AdjCloud *ddesc = nullptr;
+    int *dcloud = nullptr, *dtile = nullptr;
+    double coulomb = 0.0;
+    ~dm_adjoint() {
+        if (ddesc) cudaFree(ddesc);
+        if (dcloud) cudaFree(dcloud);
+        if (dtile) cudaFree(dtile);
+    }
+};
+
+namespace {
+void adj_fill(dm_adjoint *A, const dm_force_params *params) {
+    for (int c = 0; c < A->nclouds; c++) {
+        AdjCloud &d = A->hdesc[c];
+        d.flags = params[c].flags;
+        d.kappa = params[c].shielding;
+        d.confine = params[c].confine;
+        d.confine_x = params[c].confine_x;
+        d.confine_y = params[c].confine_y;
+        d.gamma = params[c].gamma;
+        d.rc2 = (d.kappa > 0.0) ? (10.0 / d.kappa) * (10.0 / d.kappa) : 0.0;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int dm_adjoint_create(dm_ctx *ctx, int nclouds, const int *n, const dm_force_params *params,
+                      dm_adjoint **out) {
+    if (!ctx || !out || nclouds < 1 || !n || !params) return ctx ? ctx->fail(DM_ERR_ARG, "dm_adjoint_create: bad argument") : DM_ERR_ARG;
+    const long long known = kConfinement | kDrag | kShieldedCoulomb | kRectConfinement;
+    for (int c = 0; c < nclouds; c++) {
+        if (n[c] < 1) return ctx->fail(DM_ERR_ARG, "dm_adjoint_create: cloud %d is empty", c);
+        if (params[c].flags & ~known)
+            return ctx->fail(DM_ERR_UNSUPPORTED, "dm_adjoint_create: only confinement, drag and shielded "
+                                                 "Coulomb forces are differentiated");
+        if ((params[c].flags & kShieldedCoulomb) && !(params[c].shielding > 0.0))
+            return ctx->fail(DM_ERR_ARG, "dm_adjoint_create: shielding must be positive");
+    }
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    dm_adjoint *A = new dm_adjoint();
+    A->ctx = ctx;
+    A->nclouds = nclouds;
+    A->coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);
+    A->hdesc.resize(nclouds);
+    std::vector<int> bc, bt;
+    int off = 0;
+    for (int c = 0; c < nclouds; c++) {
+        A->hdesc[c].off = off;
+        A->hdesc[c].n = n[c];
+        for (int t = 0; t * kAdjThreads < n[c]; t++) {
+            bc.push_back(c);
+            bt.push_back(t);
+        }
+        off += n[c];
+    }
+    A->total = off;
+    A->nblocks = (int)bc.size();
+    adj_fill(A, params);
+    cudaError_t e = cudaMalloc((void **)&A->ddesc, nclouds * sizeof(AdjCloud));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A->dcloud, bc.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A->dtile, bt.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(A->ddesc, A->hdesc.data(), nclouds * sizeof(AdjCloud), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(A->dcloud, bc.data(), bc.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(A->dtile, bt.data(), bt.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete A;
+        return ctx->fail(DM_ERR_CUDA, "dm_adjoint_create: %s", cudaGetErrorString(e));
+    }
+    *out = A;
+    return DM_OK;
+}
+
+int dm_adjoint_destroy(dm_adjoint *A) {
+    if (!A) return DM_ERR_ARG;
+    cudaSetDevice(A->ctx->device);
+    cudaStreamSynchronize(A->ctx->stream);
+    delete A;
+    return DM_OK;
+}
+
+int dm_adjoint_set_params(dm_adjoint *A, const dm_force_params *params) {
+    if (!A || !params) return DM_ERR_ARG;
+    dm_ctx *ctx = A->ctx;
+    adj_fill(A, params);
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    DM_CUDA(ctx, cudaMemcpyAsync(A->ddesc, A->hdesc.data(), A->nclouds * sizeof(AdjCloud),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host copy may be reused at once
+    return DM_OK;
+}
+
+int dm_adjoint_forces(dm_adjoint *A, const double *x, const double *y, const double *vx,
+                      const double *vy, const double *q, const double *m, double *fx, double *fy,
+                      double *fpx, double *fpy) {
+    if (!A || !x || !y || !vx || !vy || !q || !m || !fx || !fy) return A ? A->ctx->fail(DM_ERR_ARG, "NULL pointer") : DM_ERR_ARG;
+    dm_ctx *ctx = A->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    adjoint_kernel<0><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(
+        A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, nullptr, nullptr, fx, fy, fpx, fpy, nullptr,
+        nullptr, nullptr, nullptr, A->coulomb);
+    DM_CUDA(ctx, cudaGetLastError());
+    ctx->launches++;
+    return DM_OK;
+}
+
+int dm_adjoint_vjp(dm_adjoint *A, const double *x, const double *y, const double *vx, const double *vy,
+                   const double *q, const double *m, const double *ax, const double *ay, double *gx,
+                   double *gy, double *gvx, double *gvy, double *gq, double *gkappa, double *gkc) {
+    if (!A || !x || !y || !vx || !vy || !q || !m || !ax || !ay || !gx || !gy || !gvx || !gvy || !gq ||
+        !gkappa || !gkc)
+        return A ? A->ctx->fail(DM_ERR_ARG, "NULL pointer") : DM_ERR_ARG;
+    dm_ctx *ctx = A->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    adjoint_kernel<1><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(
+        A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, gx, gy, gvx, gvy, gq, gkappa, gkc,
+        nullptr, A->coulomb);
+    DM_CUDA(ctx, cudaGetLastError());
+    ctx->launches++;
     return DM_OK;
 }
 

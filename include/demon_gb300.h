@@ -241,6 +241,33 @@ int dm_batch_download(dm_batch *batch, double *x, double *y, double *vx, double 
 int dm_batch_info(dm_batch *batch, char *variant, size_t len, int *nitems, int *grid);
 int dm_batch_set_step_counter(dm_batch *batch, uint64_t step);
 
+/* ---- differentiable rollout ------------------------------------------ */
+
+/* FP64 forces and their vector-Jacobian product for concatenated clouds on
+ * caller-owned DEVICE arrays (the rollout itself is driven from the host,
+ * e.g. by torch.autograd).  No reference counterpart: the reference has no
+ * derivatives.  Only Confinement, RectConfinement, Drag and ShieldedCoulomb
+ * are differentiated; the cutoff jump at kappa*r = 10 is not. */
+typedef struct dm_adjoint dm_adjoint;
+int dm_adjoint_create(dm_ctx *ctx, int nclouds, const int *n,
+                      const dm_force_params *params, dm_adjoint **out);
+int dm_adjoint_destroy(dm_adjoint *adj);
+/* New per-cloud parameters (kappa, confinement, drag) for later calls. */
+int dm_adjoint_set_params(dm_adjoint *adj, const dm_force_params *params);
+/* Total force (fx, fy) and, if fpx/fpy are non-NULL, the pair force alone. */
+int dm_adjoint_forces(dm_adjoint *adj, const double *x, const double *y,
+                      const double *vx, const double *vy, const double *q,
+                      const double *m, double *fx, double *fy, double *fpx,
+                      double *fpy);
+/* Given a = dL/dF per particle, writes dL/dp (gx, gy), dL/dv (gvx, gvy),
+ * dL/dq_i (gq) and per-particle contributions to dL/dkappa and dL/dk_c of
+ * the particle's cloud (gkappa, gkc; sum them over the cloud). */
+int dm_adjoint_vjp(dm_adjoint *adj, const double *x, const double *y,
+                   const double *vx, const double *vy, const double *q,
+                   const double *m, const double *ax, const double *ay,
+                   double *gx, double *gy, double *gvx, double *gvy, double *gq,
+                   double *gkappa, double *gkc);
+
 /* ---- allocation-free diagnostics ------------------------------------- */
 
 /* No counterpart in the reference.  dm_cloud_diagnostics' computation for

@@ -1,0 +1,177 @@
+"""Adjoint of the pair force and of the RK4 rollout (needs a GB300).
+
+* the VJP kernel against torch autograd through a dense FP64 torch
+  restatement of the same forces;
+* the rollout gradient (checkpointed recomputation) against central finite
+  differences (relative step 1e-6) and against the FP64 torch-autograd
+  gradient of the same rollout.
+Clouds are small enough that every pair stays inside the cutoff, so no pair
+crosses kappa*r = 10 (where the force jumps and differences are meaningless).
+"""
+import numpy as np
+import pytest
+
+from demon_simulation_code_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+C = 1.0 / (4.0 * np.pi * 8.8541878e-12)
+
+
+def clouds(ns, radius=6e-4, seed=0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for n in ns:
+        x, y = W.uniform_disk_minsep(rng, n, radius, 1e-4)
+        out.append((x, y, rng.normal(0, 1e-4, n), rng.normal(0, 1e-4, n)))
+    return out
+
+
+def torch_forces(x, y, vx, vy, q, m, kappa, kc, gamma, ns):
+    fxs, fys = [], []
+    off = 0
+    for c, n in enumerate(ns):
+        xs, ys, qs = x[off:off + n], y[off:off + n], q[off:off + n]
+        dx = xs[:, None] - xs[None, :]
+        dy = ys[:, None] - ys[None, :]
+        eye = torch.eye(n, dtype=torch.bool, device=x.device)
+        r = torch.sqrt(torch.where(eye, torch.ones_like(dx), dx * dx + dy * dy))
+        a = r * kappa[c]
+        mask = (a < 10.0) & ~eye
+        g = torch.where(mask, C * qs[:, None] * qs[None, :] * (1 + a) * torch.exp(-a) / r**3,
+                        torch.zeros_like(r))
+        fx = (g * dx).sum(1) + qs * kc[c] * xs - gamma * m[off:off + n] * vx[off:off + n]
+        fy = (g * dy).sum(1) + qs * kc[c] * ys - gamma * m[off:off + n] * vy[off:off + n]
+        fxs.append(fx)
+        fys.append(fy)
+        off += n
+    return torch.cat(fxs), torch.cat(fys)
+
+
+@pytest.fixture(scope="module")
+def setup(gpu_ctx):
+    from demon_simulation_code_gb300.adjoint import AdjointKernels
+
+    ns = [37, 64, 9]
+    data = clouds(ns)
+    cat = [torch.tensor(np.concatenate([d[k] for d in data]), dtype=torch.float64, device="cuda")
+           for k in range(4)]
+    total = sum(ns)
+    m = torch.full((total,), W.M_DUST, dtype=torch.float64, device="cuda")
+    kappa = torch.tensor([5e3, 6e3, 4.5e3], dtype=torch.float64, device="cuda")
+    kc = torch.tensor([1e4, 2e4, 5e3], dtype=torch.float64, device="cuda")
+    qc = torch.tensor([-1.6e-15, -1.2e-15, -2.0e-15], dtype=torch.float64, device="cuda")
+    K = AdjointKernels(gpu_ctx, ns, gamma=3.0)
+    return K, ns, cat, m, kappa, kc, qc
+
+
+def test_forces_match_dense_reference(setup):
+    K, ns, (x, y, vx, vy), m, kappa, kc, qc = setup
+    K.set_params(kappa.cpu().numpy(), kc.cpu().numpy())
+    q = qc[K.seg].contiguous()
+    fx, fy = K.forces(x, y, vx, vy, q, m)
+    rx, ry = torch_forces(x, y, vx, vy, q, m, kappa, kc, 3.0, ns)
+    err = torch.sqrt(((fx - rx) ** 2 + (fy - ry) ** 2).sum() / (rx**2 + ry**2).sum()).item()
+    assert err < 1e-12
+
+
+def test_vjp_matches_torch_autograd(setup):
+    K, ns, (x, y, vx, vy), m, kappa, kc, qc = setup
+    K.set_params(kappa.cpu().numpy(), kc.cpu().numpy())
+    g = torch.Generator(device="cuda").manual_seed(3)
+    ax = torch.randn(x.shape, dtype=torch.float64, device="cuda", generator=g)
+    ay = torch.randn(x.shape, dtype=torch.float64, device="cuda", generator=g)
+    q = qc[K.seg].contiguous()
+    gx, gy, gvx, gvy, gq, gk, gc = K.vjp(x, y, vx, vy, q, m, ax, ay)
+    leaves = [t.clone().requires_grad_(True) for t in (x, y, vx, vy, q)]
+    kap = kappa.clone().requires_grad_(True)
+    kcc = kc.clone().requires_grad_(True)
+    rx, ry = torch_forces(*leaves[:4], leaves[4], m, kap, kcc, 3.0, ns)
+    L = (ax * rx + ay * ry).sum()
+    L.backward()
+
+    def rel(a, b):
+        return (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
+
+    assert rel(gx, leaves[0].grad) < 1e-11
+    assert rel(gy, leaves[1].grad) < 1e-11
+    assert rel(gvx, leaves[2].grad) < 1e-12
+    assert rel(gvy, leaves[3].grad) < 1e-12
+    assert rel(gq, leaves[4].grad) < 1e-11
+    assert rel(K.per_cloud(gk), kap.grad) < 1e-11
+    assert rel(K.per_cloud(gc), kcc.grad) < 1e-12
+
+
+def _loss(K, x0, y0, vx0, vy0, kappa, qc, kc, m, xt, yt, steps, every):
+    from demon_simulation_code_gb300.adjoint import rollout
+
+    xT, yT, _, _ = rollout(K, x0, y0, vx0, vy0, kappa, qc, kc, m, 1e-5, steps, every)
+    return ((xT - xt) ** 2 + (yT - yt) ** 2).mean()
+
+
+def test_rollout_gradient_vs_finite_differences_and_torch(setup):
+    K, ns, (x, y, vx, vy), m, kappa, kc, qc = setup
+    steps, every = 23, 7  # a partial last segment
+    xt = x + 1e-5
+    yt = y - 2e-5
+    x0 = x.clone().requires_grad_(True)
+    kap = kappa.clone().requires_grad_(True)
+    qq = qc.clone().requires_grad_(True)
+    kcc = kc.clone().requires_grad_(True)
+    L = _loss(K, x0, y, vx, vy, kap, qq, kcc, m, xt, yt, steps, every)
+    L.backward()
+    grads = {"kappa": kap.grad, "q": qq.grad, "kc": kcc.grad}
+
+    def L_of(**over):
+        args = dict(kappa=kappa, q=qc, kc=kc, x0=x)
+        args.update(over)
+        with torch.no_grad():
+            return _loss(K, args["x0"], y, vx, vy, args["kappa"], args["q"], args["kc"], m, xt, yt,
+                         steps, every).item()
+
+    for name, base in (("kappa", kappa), ("q", qc), ("kc", kc)):
+        for c in range(len(ns)):
+            h = 1e-6 * abs(base[c].item())
+            up = base.clone()
+            dn = base.clone()
+            up[c] += h
+            dn[c] -= h
+            fd = (L_of(**{name: up}) - L_of(**{name: dn})) / (2 * h)
+            ad = grads[name][c].item()
+            assert abs(ad - fd) <= 1e-4 * max(abs(fd), 1e-300), (name, c, ad, fd)
+    for i in (0, 40, 105):
+        h = 1e-6 * 6e-4
+        up = x.clone()
+        dn = x.clone()
+        up[i] += h
+        dn[i] -= h
+        fd = (L_of(x0=up) - L_of(x0=dn)) / (2 * h)
+        assert abs(x0.grad[i].item() - fd) <= 1e-4 * abs(fd) + 1e-12 * abs(L.item()) / 6e-4, (i,)
+
+    # FP64 torch autograd through the same rollout (dense forces)
+    def f(s, q, kapv, kcv):
+        fx, fy = torch_forces(s[0], s[1], s[2], s[3], q, m, kapv, kcv, 3.0, ns)
+        return (s[2], s[3], fx / m, fy / m)
+
+    x0r = x.clone().requires_grad_(True)
+    kapr = kappa.clone().requires_grad_(True)
+    qr = qc.clone().requires_grad_(True)
+    kcr = kc.clone().requires_grad_(True)
+    qp = qr[K.seg]
+    s = (x0r, y, vx, vy)
+    dt = 1e-5
+    for _ in range(steps):
+        k1 = [dt * v for v in f(s, qp, kapr, kcr)]
+        s2 = [a + 0.5 * b for a, b in zip(s, k1)]
+        k2 = [dt * v for v in f(s2, qp, kapr, kcr)]
+        s3 = [a + 0.5 * b for a, b in zip(s, k2)]
+        k3 = [dt * v for v in f(s3, qp, kapr, kcr)]
+        s4 = [a + b for a, b in zip(s, k3)]
+        k4 = [dt * v for v in f(s4, qp, kapr, kcr)]
+        s = tuple(a + (p + ((u + v) * 2.0 + w)) / 6.0 for a, p, u, v, w in zip(s, k1, k2, k3, k4))
+    Lr = ((s[0] - xt) ** 2 + (s[1] - yt) ** 2).mean()
+    Lr.backward()
+    assert abs(Lr.item() - L.item()) <= 1e-12 * abs(L.item())
+    for a, b in ((kap.grad, kapr.grad), (qq.grad, qr.grad), (kcc.grad, kcr.grad), (x0.grad, x0r.grad)):
+        assert (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() < 1e-9
