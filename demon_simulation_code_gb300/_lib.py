@@ -56,6 +56,7 @@ SIGNATURES = {
     "dm_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "dm_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dm_ctx_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dm_ctx_reset_stream": (ctypes.c_int, [ctypes.c_void_p]),
     "dm_ctx_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "dm_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "dm_ctx_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

@@ -37,9 +37,16 @@ def _p(t: torch.Tensor) -> int:
 
 
 class AdjointKernels:
-    """dm_adjoint for a fixed list of cloud sizes (concatenated clouds)."""
+    """dm_adjoint for a fixed list of cloud sizes (concatenated clouds).
+
+    Owns a context whose work is queued on torch's current CUDA stream at
+    each call, so the kernels and the surrounding tensor arithmetic are
+    ordered on one stream."""
 
     def __init__(self, ctx, ns, flags=CONFINEMENT | DRAG | SHIELDED_COULOMB, gamma=3.0):
+        from .cloud import Context
+
+        ctx = Context(torch.cuda.current_device())
         self.ctx = ctx
         self.lib = ctx.lib
         self.ns = [int(v) for v in ns]
@@ -62,6 +69,7 @@ class AdjointKernels:
                                                 confine=float(kc[c]), gamma=self.gamma)
 
     def set_params(self, kappa, kc):
+        self._bind_stream()
         self._fill(np.asarray(kappa, dtype=np.float64), np.asarray(kc, dtype=np.float64))
         check(self.lib.dm_adjoint_set_params(self.h, self._params), self.ctx.h)
 
@@ -76,7 +84,11 @@ class AdjointKernels:
         except Exception:
             pass
 
+    def _bind_stream(self):
+        self.ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+
     def forces(self, x, y, vx, vy, q, m, pair=False):
+        self._bind_stream()
         fx = torch.empty_like(x)
         fy = torch.empty_like(x)
         fpx = torch.empty_like(x) if pair else None
@@ -86,6 +98,7 @@ class AdjointKernels:
         return (fx, fy, fpx, fpy) if pair else (fx, fy)
 
     def vjp(self, x, y, vx, vy, q, m, ax, ay):
+        self._bind_stream()
         out = [torch.empty_like(x) for _ in range(7)]
         check(self.lib.dm_adjoint_vjp(self.h, _p(x), _p(y), _p(vx), _p(vy), _p(q), _p(m), _p(ax), _p(ay),
                                       *(_p(o) for o in out)), self.ctx.h)

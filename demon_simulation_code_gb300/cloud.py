@@ -47,7 +47,11 @@ class Context:
             pass
 
     def set_stream(self, stream_handle: int | None):
+        """Queue all later work on this cudaStream_t handle (0 = the default stream)."""
         check(self.lib.dm_ctx_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)), self.h)
+
+    def reset_stream(self):
+        check(self.lib.dm_ctx_reset_stream(self.h), self.h)
 
     def synchronize(self):
         check(self.lib.dm_ctx_synchronize(self.h), self.h)

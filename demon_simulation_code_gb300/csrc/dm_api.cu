@@ -618,7 +618,13 @@ int dm_ctx_destroy(dm_ctx *ctx) {
 
 int dm_ctx_set_stream(dm_ctx *ctx, void *stream) {
     if (!ctx) return DM_ERR_ARG;
-    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    ctx->stream = (cudaStream_t)stream;  // NULL: the CUDA default (legacy) stream
+    return DM_OK;
+}
+
+int dm_ctx_reset_stream(dm_ctx *ctx) {
+    if (!ctx) return DM_ERR_ARG;
+    ctx->stream = ctx->own_stream;
     return DM_OK;
 }
 

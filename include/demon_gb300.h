@@ -94,8 +94,10 @@ int dm_ctx_create(int device, dm_ctx **out);
 int dm_ctx_destroy(dm_ctx *ctx);
 
 /* Use an existing cudaStream_t (passed as void*) for all later work; NULL
- * restores the context's own stream. */
+ * means the CUDA default (legacy) stream, as in the CUDA runtime. */
 int dm_ctx_set_stream(dm_ctx *ctx, void *cuda_stream);
+/* Back to the context's own stream. */
+int dm_ctx_reset_stream(dm_ctx *ctx);
 
 /* Blocks until all work queued on the context's stream has finished and
  * reports any asynchronous error (including device-side numeric flags). */
