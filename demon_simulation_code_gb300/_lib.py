@@ -103,8 +103,8 @@ SIGNATURES = {
                                          ctypes.POINTER(ForceParams), ctypes.POINTER(ctypes.c_void_p)]),
     "dm_adjoint_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dm_adjoint_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForceParams)]),
-    "dm_adjoint_forces": (ctypes.c_int, [ctypes.c_void_p] * 11),
-    "dm_adjoint_vjp": (ctypes.c_int, [ctypes.c_void_p] * 16),
+    "dm_adjoint_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 10),
+    "dm_adjoint_vjp": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 15),
     "dm_diagnostics_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.POINTER(ForceParams),

@@ -2,7 +2,7 @@
 ``torch.autograd.Function``.
 
 The O(N^2) work -- forces and their vector-Jacobian product -- runs in the
-FP64 CUDA kernels of libdemon_gb300.so (``dm_adjoint_forces`` /
+CUDA kernels of libdemon_gb300.so (FP64, or FP32 pair terms with Kahan sums) (``dm_adjoint_forces`` /
 ``dm_adjoint_vjp`` on the tensors' device memory); the O(N) RK4 stage
 bookkeeping is FP64 tensor arithmetic on the same stream.  The forward pass
 keeps the state every ``checkpoint_every`` steps; the backward pass
@@ -37,16 +37,20 @@ def _p(t: torch.Tensor) -> int:
 
 
 class AdjointKernels:
-    """dm_adjoint for a fixed list of cloud sizes (concatenated clouds).
+    """dm_adjoint for a fixed list of cloud sizes (concatenated clouds), in
+    "fp64" or "fp32c" pair arithmetic.
 
     Owns a context whose work is queued on torch's current CUDA stream at
     each call, so the kernels and the surrounding tensor arithmetic are
     ordered on one stream."""
 
-    def __init__(self, ctx, ns, flags=CONFINEMENT | DRAG | SHIELDED_COULOMB, gamma=3.0):
+    def __init__(self, ns, flags=CONFINEMENT | DRAG | SHIELDED_COULOMB, gamma=3.0, device=None,
+                 precision="fp64"):
         from .cloud import Context
 
-        ctx = Context(torch.cuda.current_device())
+        self.precision = {"fp64": 0, "fp32c": 1}[precision]
+
+        ctx = Context(torch.cuda.current_device() if device is None else int(device))
         self.ctx = ctx
         self.lib = ctx.lib
         self.ns = [int(v) for v in ns]
@@ -93,14 +97,15 @@ class AdjointKernels:
         fy = torch.empty_like(x)
         fpx = torch.empty_like(x) if pair else None
         fpy = torch.empty_like(x) if pair else None
-        check(self.lib.dm_adjoint_forces(self.h, _p(x), _p(y), _p(vx), _p(vy), _p(q), _p(m), _p(fx), _p(fy),
-                                         _p(fpx) if pair else None, _p(fpy) if pair else None), self.ctx.h)
+        check(self.lib.dm_adjoint_forces(self.h, self.precision, _p(x), _p(y), _p(vx), _p(vy), _p(q), _p(m),
+                                         _p(fx), _p(fy), _p(fpx) if pair else None,
+                                         _p(fpy) if pair else None), self.ctx.h)
         return (fx, fy, fpx, fpy) if pair else (fx, fy)
 
     def vjp(self, x, y, vx, vy, q, m, ax, ay):
         self._bind_stream()
         out = [torch.empty_like(x) for _ in range(7)]
-        check(self.lib.dm_adjoint_vjp(self.h, _p(x), _p(y), _p(vx), _p(vy), _p(q), _p(m), _p(ax), _p(ay),
+        check(self.lib.dm_adjoint_vjp(self.h, self.precision, _p(x), _p(y), _p(vx), _p(vy), _p(q), _p(m), _p(ax), _p(ay),
                                       *(_p(o) for o in out)), self.ctx.h)
         return out  # gx, gy, gvx, gvy, gq_i, gkappa_i, gkc_i
 

@@ -1,5 +1,5 @@
 // dm_adjoint.cuh -- forces and their vector-Jacobian product for the
-// differentiable rollout (FP64).
+// differentiable rollout, in FP64 or FP32-compensated pair arithmetic.
 //
 // Clouds are concatenated; cloud c owns particles [off_c, off_c + n_c) and
 // its own kappa, confinement and drag.  For particle k with force adjoint
@@ -21,7 +21,7 @@
 // discontinuous there and its jump is not differentiated (measure zero).
 #pragma once
 
-#include "dm_device.cuh"
+#include "dm_pair.cuh"
 
 namespace dm {
 
@@ -30,94 +30,211 @@ struct AdjCloud {
     long long flags;
     double kappa, confine, confine_x, confine_y, gamma;
     double rc2;
+    float rc2_lo, rc2_hi;  // FP32 certain-in / certain-out bounds on r^2
+    float kappa_f, kappa2_f;
 };
 
 constexpr int kAdjThreads = 128;
 constexpr int kAdjTile = 256;
 
 struct alignas(16) AdjJ {
-    double x, y, q, ax, ay, b;
+    double x, y, q, ax, ay;
 };
+
+// FP32 candidate test, conservative for the FP64 cutoff decision.  With
+// xf = fl32(x) (|xf - x| <= 2^-24 |x|) and dxf = fl32(xf_i - xf_j), the error of
+// dxf is at most 2^-24 (|x_i| + |x_j|) + 2^-24 |dxf| <= e = 2^-22 (A_i + A_t),
+// where A_i = max(|x_i|, |y_i|) and A_t bounds |x_j|, |y_j| over the j tile; the
+// error vector of (dxf, dyf) is shorter than 2e.  So every pair with true
+// r < r_c has fl32(dxf^2 + dyf^2) < (r_c + 2e)^2 (1 + 2^-20) -- the last factor
+// covers the three FP32 roundings of the square sum and of r_c itself.  The
+// exact decision is then the reference's FP64 test (ref_in_cutoff).
+__device__ __forceinline__ float adj_candidate_bound(double rc, float ai, float at) {
+    const float e = 2.384185791015625e-7f * (ai + at);  // 2^-22
+    const float r = __fadd_ru(__double2float_ru(rc), 2.0f * e);
+    return __fmul_ru(__fmul_ru(r, r), 1.0000009536743164f);  // 1 + 2^-20
+}
+
+// Pair sums of one particle: MODE 0 (sx, sy) = sum_j F_kj; MODE 1 the four
+// VJP sums (position x, position y, charge, kappa).
+struct AdjSums {
+    double v[4];
+};
+
+// FP64 pair loop over one shared-memory j tile.
+template <int MODE>
+__device__ __forceinline__ void adj_tile_fp64(const AdjCloud &d, const AdjJ *sj, const float2 *sf, int cnt,
+                                              int jbase, int li, double xi, double yi, double qi, double axi,
+                                              double ayi, float xfi, float yfi, float bound, double coulomb,
+                                              AdjSums &S) {
+    for (int e = 0; e < cnt; e++) {
+        const float2 f = sf[e];
+        const float dxf = xfi - f.x, dyf = yfi - f.y;
+        if (!(fmaf(dxf, dxf, dyf * dyf) < bound)) continue;
+        if (jbase + e == li) continue;
+        const AdjJ v = sj[e];
+        const double dx = __dsub_rn(xi, v.x), dy = __dsub_rn(yi, v.y);
+        double r, a;
+        if (!ref_in_cutoff(dx, dy, d.kappa, r, a)) continue;
+        const double ex = exp(-a);
+        const double g = coulomb * qi * v.q * (1.0 + a) * ex / (r * r * r);
+        if (MODE == 0) {
+            S.v[0] += g * dx;
+            S.v[1] += g * dy;
+        } else {
+            const double h = -g * (d.kappa * d.kappa / (1.0 + a) + 3.0 / (r * r));
+            const double bx = axi - v.ax, by = ayi - v.ay;
+            const double dd = dx * bx + dy * by;
+            S.v[0] += g * bx + h * dx * dd;                             // position adjoint
+            S.v[1] += g * by + h * dy * dd;
+            S.v[2] += g * dd;                                            // F_kj . (a_k - a_j)
+            S.v[3] += (-coulomb * qi * v.q * d.kappa * ex / r) * (axi * dx + ayi * dy);  // dg/dkappa
+        }
+    }
+}
+
+// FP32-compensated pair loop over one shared-memory j tile: positions as
+// float pairs (hi, lo) so the differences keep ~2^-24 relative accuracy,
+// pair terms in FP32, Kahan sums; pairs within 4e-6 of the cutoff in r^2 are
+// decided by the reference's FP64 test on the FP64 positions.
+template <int MODE>
+__device__ __forceinline__ void adj_tile_fp32c(const AdjCloud &d, const ExpConsts &E, const float4 *sp,
+                                               const float4 *sa, int cnt, int jbase, int li, float xh, float yh,
+                                               float xl, float yl, float qci, float axi, float ayi,
+                                               const double *__restrict__ x, const double *__restrict__ y,
+                                               double xi, double yi, float (&s)[4], float (&c)[4]) {
+    for (int e = 0; e < cnt; e++) {
+        const float4 P = sp[e];
+        const float dx = (xh - P.x) + (xl - P.z);
+        const float dy = (yh - P.y) + (yl - P.w);
+        const float r2 = fmaf(dx, dx, dy * dy);
+        if (!(r2 < d.rc2_hi)) continue;
+        if (jbase + e == li) continue;
+        if (!(r2 < d.rc2_lo)) {
+            const int j = d.off + jbase + e;
+            double r, a;
+            if (!ref_in_cutoff(__dsub_rn(xi, x[j]), __dsub_rn(yi, y[j]), d.kappa, r, a)) continue;
+        }
+        float w = rsqrtf(r2);  // 1/r, one Newton step
+        w = fmaf(0.5f * fmaf(-(r2 * w), w, 1.0f), w, w);
+        const float kr = d.kappa_f * (r2 * w);
+        const float ex = exp_neg(kr, E);
+        const float4 A = sa[e];  // (q_j, a_j.x, a_j.y, -)
+        const float qq = qci * A.x;
+        const float g = (qq * (1.0f + kr)) * ex * ((w * w) * w);
+        if (MODE == 0) {
+            kahan_add(s[0], c[0], g * dx);
+            kahan_add(s[1], c[1], g * dy);
+        } else {
+            const float h = -g * fmaf(d.kappa2_f, __frcp_rn(1.0f + kr), 3.0f * (w * w));
+            const float bx = axi - A.y, by = ayi - A.z;
+            const float hd = h * fmaf(dx, bx, dy * by);
+            kahan_add(s[0], c[0], fmaf(hd, dx, g * bx));
+            kahan_add(s[1], c[1], fmaf(hd, dy, g * by));
+            kahan_add(s[2], c[2], g * fmaf(dx, bx, dy * by));
+            kahan_add(s[3], c[3], (-(qq * d.kappa_f) * ex * w) * fmaf(axi, dx, ayi * dy));
+        }
+    }
+}
 
 // One thread per particle i, j of the same cloud staged through shared
 // memory.  MODE 0: forces (total F and pair-only Fp).  MODE 1: VJP.
-template <int MODE>
+// F32C selects the FP32-compensated pair arithmetic.
+template <int MODE, bool F32C>
 __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(
     const AdjCloud *__restrict__ desc, const int *__restrict__ cloud_of_block, const int *__restrict__ tile_of_block,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ vx,
     const double *__restrict__ vy, const double *__restrict__ q, const double *__restrict__ m,
     const double *__restrict__ ax, const double *__restrict__ ay,  // MODE 1: force adjoint
     double *__restrict__ o0, double *__restrict__ o1, double *__restrict__ o2, double *__restrict__ o3,
-    double *__restrict__ o4, double *__restrict__ o5, double *__restrict__ o6, double *__restrict__ o7,
-    double coulomb) {
-    __shared__ AdjJ sj[kAdjTile];
+    double *__restrict__ o4, double *__restrict__ o5, double *__restrict__ o6, double coulomb,
+    const ExpConsts E) {
+    // FP64: AdjJ[kAdjTile] + float2[kAdjTile]; FP32C: two float4[kAdjTile]
+    constexpr int kSmem = F32C ? 2 * 16 * kAdjTile : (int)(sizeof(AdjJ) + 8) * kAdjTile;
+    __shared__ __align__(16) unsigned char smem[kSmem];
+    __shared__ unsigned int s_amax;
     const AdjCloud d = desc[cloud_of_block[blockIdx.x]];
     const int li = tile_of_block[blockIdx.x] * kAdjThreads + threadIdx.x;  // index within the cloud
     const bool valid = li < d.n;
     const int i = d.off + (valid ? li : 0);
     const double xi = x[i], yi = y[i], qi = q[i];
     const double axi = (MODE == 1 && valid) ? ax[i] : 0.0, ayi = (MODE == 1 && valid) ? ay[i] : 0.0;
-    const double a2 = xi * xi + yi * yi;
-    const double rc = sqrt(d.rc2);
-    const double pr = sqrt(a2) + rc;
-    const double U = (d.rc2 - a2) + 5.684341886080802e-14 * pr * pr;
     const bool coul = (d.flags & kShieldedCoulomb) != 0;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0;
+    AdjSums S{};
+    // FP64 path state
+    const float xfi = (float)xi, yfi = (float)yi;
+    const float ai = fmaxf(fabsf(xfi), fabsf(yfi));
+    const double rc = sqrt(d.rc2);
+    // FP32C path state
+    const float xh = (float)xi, yh = (float)yi;
+    const float xl = (float)(xi - (double)xh), yl = (float)(yi - (double)yh);
+    const float qci = (float)(coulomb * qi);
+    const float axf = (float)axi, ayf = (float)ayi;
+    float fs[4] = {0.0f, 0.0f, 0.0f, 0.0f}, fc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int j0 = 0; j0 < d.n && coul; j0 += kAdjTile) {
         const int cnt = min(kAdjTile, d.n - j0);
         __syncthreads();
-        for (int e = threadIdx.x; e < cnt; e += kAdjThreads) {
-            const int j = d.off + j0 + e;
-            AdjJ v;
-            v.x = x[j];
-            v.y = y[j];
-            v.q = q[j];
-            v.ax = (MODE == 1) ? ax[j] : 0.0;
-            v.ay = (MODE == 1) ? ay[j] : 0.0;
-            v.b = v.x * v.x + v.y * v.y;
-            sj[e] = v;
-        }
-        __syncthreads();
-        if (!valid) continue;
-        for (int e = 0; e < cnt; e++) {
-            const AdjJ v = sj[e];
-            if (fma(-2.0 * xi, v.x, fma(-2.0 * yi, v.y, v.b)) >= U) continue;
-            if (j0 + e == li) continue;
-            const double dx = __dsub_rn(xi, v.x), dy = __dsub_rn(yi, v.y);
-            double r, a;
-            if (!ref_in_cutoff(dx, dy, d.kappa, r, a)) continue;
-            const double ex = exp(-a);
-            const double g = coulomb * qi * v.q * (1.0 + a) * ex / (r * r * r);
-            if (MODE == 0) {
-                s0 += g * dx;
-                s1 += g * dy;
-            } else {
-                const double h = -g * (d.kappa * d.kappa / (1.0 + a) + 3.0 / (r * r));
-                const double bx = axi - v.ax, by = ayi - v.ay;
-                const double dd = dx * bx + dy * by;
-                s0 += g * bx + h * dx * dd;         // position adjoint
-                s1 += g * by + h * dy * dd;
-                s2 += g * dd;                        // F_kj . (a_k - a_j)  (charge)
-                const double gk = -coulomb * qi * v.q * d.kappa * ex / r;  // dg/dkappa
-                s3 += gk * (axi * dx + ayi * dy);    // kappa
+        if (F32C) {
+            float4 *sp = reinterpret_cast<float4 *>(smem);
+            float4 *sa = sp + kAdjTile;
+            for (int e = threadIdx.x; e < cnt; e += kAdjThreads) {
+                const int j = d.off + j0 + e;
+                const double xj = x[j], yj = y[j];
+                const float hx = (float)xj, hy = (float)yj;
+                sp[e] = make_float4(hx, hy, (float)(xj - (double)hx), (float)(yj - (double)hy));
+                sa[e] = make_float4((float)q[j], MODE == 1 ? (float)ax[j] : 0.0f, MODE == 1 ? (float)ay[j] : 0.0f,
+                                    0.0f);
             }
+            __syncthreads();
+            if (valid)
+                adj_tile_fp32c<MODE>(d, E, sp, sa, cnt, j0, li, xh, yh, xl, yl, qci, axf, ayf, x, y, xi, yi, fs,
+                                     fc);
+        } else {
+            AdjJ *sj = reinterpret_cast<AdjJ *>(smem);
+            float2 *sf = reinterpret_cast<float2 *>(sj + kAdjTile);
+            if (threadIdx.x == 0) s_amax = 0u;
+            __syncthreads();
+            float am = 0.0f;
+            for (int e = threadIdx.x; e < cnt; e += kAdjThreads) {
+                const int j = d.off + j0 + e;
+                AdjJ v;
+                v.x = x[j];
+                v.y = y[j];
+                v.q = q[j];
+                v.ax = (MODE == 1) ? ax[j] : 0.0;
+                v.ay = (MODE == 1) ? ay[j] : 0.0;
+                sj[e] = v;
+                const float2 f = make_float2((float)v.x, (float)v.y);
+                sf[e] = f;
+                am = fmaxf(am, fmaxf(fabsf(f.x), fabsf(f.y)));  // NaN is dropped: its pairs fail the test
+            }
+            for (int o = 16; o > 0; o >>= 1) am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
+            if ((threadIdx.x & 31) == 0) atomicMax(&s_amax, __float_as_uint(am));  // non-negative: int order
+            __syncthreads();
+            if (valid)
+                adj_tile_fp64<MODE>(d, sj, sf, cnt, j0, li, xi, yi, qi, axi, ayi, xfi, yfi,
+                                    adj_candidate_bound(rc, ai, __uint_as_float(s_amax)), coulomb, S);
         }
     }
     if (!valid) return;
+    if (F32C) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) S.v[k] = (double)fs[k] - (double)fc[k];
+    }
     const double xv = vx[i], yv = vy[i], mi = m[i];
     if (MODE == 0) {
         double fx = 0.0, fy = 0.0;
         if (d.flags & kConfinement) { fx += qi * d.confine * xi; fy += qi * d.confine * yi; }
         if (d.flags & kDrag) { fx += -d.gamma * mi * xv; fy += -d.gamma * mi * yv; }
         if (d.flags & kRectConfinement) { fx += qi * d.confine_x * xi; fy += qi * d.confine_y * yi; }
-        fx += s0;
-        fy += s1;
+        fx += S.v[0];
+        fy += S.v[1];
         o0[i] = fx;   // total force
         o1[i] = fy;
-        if (o2) o2[i] = s0;  // pair force only
-        if (o3) o3[i] = s1;
+        if (o2) o2[i] = S.v[0];  // pair force only
+        if (o3) o3[i] = S.v[1];
     } else {
-        double gx = s0, gy = s1, gq = (qi != 0.0) ? s2 / qi : 0.0, gkc = 0.0;
+        double gx = S.v[0], gy = S.v[1], gq = (qi != 0.0) ? S.v[2] / qi : 0.0, gkc = 0.0;
         if (d.flags & kConfinement) {
             gx += qi * d.confine * axi;
             gy += qi * d.confine * ayi;
@@ -135,9 +252,8 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(
         o2[i] = gv * axi;    // dL/dv (through drag)
         o3[i] = gv * ayi;
         o4[i] = gq;          // dL/dq_i
-        o5[i] = s3;          // dL/dkappa contribution of particle i
+        o5[i] = S.v[3];      // dL/dkappa contribution of particle i
         o6[i] = gkc;         // dL/dk_c contribution of particle i
-        if (o7) o7[i] = 0.0;
     }
 }
 

@@ -1576,7 +1576,26 @@ void adj_fill(dm_adjoint *A, const dm_force_params *params) {
         d.confine_y = params[c].confine_y;
         d.gamma = params[c].gamma;
         d.rc2 = (d.kappa > 0.0) ? (10.0 / d.kappa) * (10.0 / d.kappa) : 0.0;
+        d.rc2_lo = (float)(d.rc2 * (1.0 - 4e-6));
+        d.rc2_hi = (float)(d.rc2 * (1.0 + 4e-6));
+        d.kappa_f = (float)d.kappa;
+        d.kappa2_f = (float)(d.kappa * d.kappa);
     }
+}
+
+template <int MODE>
+void adj_launch(dm_adjoint *A, int precision, const double *x, const double *y, const double *vx,
+                const double *vy, const double *q, const double *m, const double *ax, const double *ay,
+                double *o0, double *o1, double *o2, double *o3, double *o4, double *o5, double *o6) {
+    cudaStream_t st = A->ctx->stream;
+    if (precision == DM_FP32C)
+        adjoint_kernel<MODE, true><<<A->nblocks, kAdjThreads, 0, st>>>(
+            A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, o0, o1, o2, o3, o4, o5, o6, A->coulomb,
+            exp_consts());
+    else
+        adjoint_kernel<MODE, false><<<A->nblocks, kAdjThreads, 0, st>>>(
+            A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, o0, o1, o2, o3, o4, o5, o6, A->coulomb,
+            exp_consts());
 }
 }  // namespace
 
@@ -1647,31 +1666,32 @@ int dm_adjoint_set_params(dm_adjoint *A, const dm_force_params *params) {
     return DM_OK;
 }
 
-int dm_adjoint_forces(dm_adjoint *A, const double *x, const double *y, const double *vx,
+int dm_adjoint_forces(dm_adjoint *A, int precision, const double *x, const double *y, const double *vx,
                       const double *vy, const double *q, const double *m, double *fx, double *fy,
                       double *fpx, double *fpy) {
     if (!A || !x || !y || !vx || !vy || !q || !m || !fx || !fy) return A ? A->ctx->fail(DM_ERR_ARG, "NULL pointer") : DM_ERR_ARG;
     dm_ctx *ctx = A->ctx;
+    if (precision != DM_FP64 && precision != DM_FP32C)
+        return ctx->fail(DM_ERR_ARG, "dm_adjoint_forces: unknown precision %d", precision);
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
-    adjoint_kernel<0><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(
-        A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, nullptr, nullptr, fx, fy, fpx, fpy, nullptr,
-        nullptr, nullptr, nullptr, A->coulomb);
+    adj_launch<0>(A, precision, x, y, vx, vy, q, m, nullptr, nullptr, fx, fy, fpx, fpy, nullptr, nullptr,
+                  nullptr);
     DM_CUDA(ctx, cudaGetLastError());
     ctx->launches++;
     return DM_OK;
 }
 
-int dm_adjoint_vjp(dm_adjoint *A, const double *x, const double *y, const double *vx, const double *vy,
-                   const double *q, const double *m, const double *ax, const double *ay, double *gx,
-                   double *gy, double *gvx, double *gvy, double *gq, double *gkappa, double *gkc) {
+int dm_adjoint_vjp(dm_adjoint *A, int precision, const double *x, const double *y, const double *vx,
+                   const double *vy, const double *q, const double *m, const double *ax, const double *ay,
+                   double *gx, double *gy, double *gvx, double *gvy, double *gq, double *gkappa, double *gkc) {
     if (!A || !x || !y || !vx || !vy || !q || !m || !ax || !ay || !gx || !gy || !gvx || !gvy || !gq ||
         !gkappa || !gkc)
         return A ? A->ctx->fail(DM_ERR_ARG, "NULL pointer") : DM_ERR_ARG;
     dm_ctx *ctx = A->ctx;
+    if (precision != DM_FP64 && precision != DM_FP32C)
+        return ctx->fail(DM_ERR_ARG, "dm_adjoint_vjp: unknown precision %d", precision);
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
-    adjoint_kernel<1><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(
-        A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, gx, gy, gvx, gvy, gq, gkappa, gkc,
-        nullptr, A->coulomb);
+    adj_launch<1>(A, precision, x, y, vx, vy, q, m, ax, ay, gx, gy, gvx, gvy, gq, gkappa, gkc);
     DM_CUDA(ctx, cudaGetLastError());
     ctx->launches++;
     return DM_OK;

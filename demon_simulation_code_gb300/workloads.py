@@ -195,5 +195,31 @@ def adjoint64(seed: int = 4, nclouds: int = 64, n: int = 2048) -> Workload:
                     extra={"perturb": 0.2, "checkpoint_every": 20})
 
 
+def adjoint64_smooth(seed: int = 4, nclouds: int = 64, n: int = 2048) -> Workload:
+    """adjoint64's shape (64 x 2048 in a 9e-3 m disk, 200 steps of 1e-4 s,
+    checkpoints every 20, +/-20% start) with a loss that is smooth in every
+    parameter, for gradient checks against finite differences: minimum pair
+    separation 1.2e-4 m, kappa = 400 so that the cutoff radius 10/kappa
+    (>= 20.8 mm over the +/-20% range) exceeds the cloud's diameter and no pair
+    crosses kappa*r = 10 during the rollout, k_c = 4e4.
+
+    adjoint64 itself is chaotic: k_c = 1e8 pulls the random disk through its
+    centre every 0.66 ms, where close pairs are kicked by millimetres per
+    step.  And wherever pairs cross the cutoff, the reference's force jumps
+    there, so a central difference picks up jump terms that no derivative
+    has."""
+    rng = np.random.default_rng(seed)
+    clouds = []
+    for _ in range(nclouds):
+        x, y = uniform_disk_minsep(rng, n, 9e-3, 1.2e-4)
+        clouds.append(Cloud(x=x, y=y, vx=rng.normal(0, 1e-4, n), vy=rng.normal(0, 1e-4, n),
+                            q=np.full(n, Q_DUST), m=np.full(n, M_DUST), shielding=400.0, confine=4e4,
+                            gamma=3.0))
+    return Workload("adjoint64_smooth", clouds, 1e-4, 200,
+                    f"{nclouds} clouds N={n} disk R=9e-3, min separation 1.2e-4, "
+                    "true (kappa,q,k_c)=(400,-1.6e-15,4e4)",
+                    extra={"perturb": 0.2, "checkpoint_every": 20})
+
+
 WORKLOADS = {"disk512": disk512, "disk16k": disk16k, "square256k": square256k,
-             "batch256": batch256, "adjoint64": adjoint64}
+             "batch256": batch256, "adjoint64": adjoint64, "adjoint64_smooth": adjoint64_smooth}

@@ -256,19 +256,22 @@ int dm_adjoint_create(dm_ctx *ctx, int nclouds, const int *n,
 int dm_adjoint_destroy(dm_adjoint *adj);
 /* New per-cloud parameters (kappa, confinement, drag) for later calls. */
 int dm_adjoint_set_params(dm_adjoint *adj, const dm_force_params *params);
-/* Total force (fx, fy) and, if fpx/fpy are non-NULL, the pair force alone. */
-int dm_adjoint_forces(dm_adjoint *adj, const double *x, const double *y,
-                      const double *vx, const double *vy, const double *q,
-                      const double *m, double *fx, double *fy, double *fpx,
-                      double *fpy);
+/* Total force (fx, fy) and, if fpx/fpy are non-NULL, the pair force alone.
+ * precision: DM_FP64, or DM_FP32C (FP32 pair terms, Kahan sums, FP64 per
+ * particle; ~1e-6 relative).  All pointers are device arrays of the
+ * concatenated clouds. */
+int dm_adjoint_forces(dm_adjoint *adj, int precision, const double *x,
+                      const double *y, const double *vx, const double *vy,
+                      const double *q, const double *m, double *fx, double *fy,
+                      double *fpx, double *fpy);
 /* Given a = dL/dF per particle, writes dL/dp (gx, gy), dL/dv (gvx, gvy),
  * dL/dq_i (gq) and per-particle contributions to dL/dkappa and dL/dk_c of
  * the particle's cloud (gkappa, gkc; sum them over the cloud). */
-int dm_adjoint_vjp(dm_adjoint *adj, const double *x, const double *y,
-                   const double *vx, const double *vy, const double *q,
-                   const double *m, const double *ax, const double *ay,
-                   double *gx, double *gy, double *gvx, double *gvy, double *gq,
-                   double *gkappa, double *gkc);
+int dm_adjoint_vjp(dm_adjoint *adj, int precision, const double *x,
+                   const double *y, const double *vx, const double *vy,
+                   const double *q, const double *m, const double *ax,
+                   const double *ay, double *gx, double *gy, double *gvx,
+                   double *gvy, double *gq, double *gkappa, double *gkc);
 
 /* ---- allocation-free diagnostics ------------------------------------- */
 

@@ -62,22 +62,37 @@ def setup(gpu_ctx):
     kappa = torch.tensor([5e3, 6e3, 4.5e3], dtype=torch.float64, device="cuda")
     kc = torch.tensor([1e4, 2e4, 5e3], dtype=torch.float64, device="cuda")
     qc = torch.tensor([-1.6e-15, -1.2e-15, -2.0e-15], dtype=torch.float64, device="cuda")
-    K = AdjointKernels(gpu_ctx, ns, gamma=3.0)
-    return K, ns, cat, m, kappa, kc, qc
+    K = AdjointKernels(ns, gamma=3.0)
+    K32 = AdjointKernels(ns, gamma=3.0, precision="fp32c")
+    return K, ns, cat, m, kappa, kc, qc, K32
 
 
-def test_forces_match_dense_reference(setup):
-    K, ns, (x, y, vx, vy), m, kappa, kc, qc = setup
+# relative-error bounds: FP64, and FP32 pair terms with Kahan sums
+TOL = {"fp64": {"f": 1e-12, "pos": 1e-11, "vel": 1e-12, "q": 1e-11, "kappa": 1e-11, "kc": 1e-12},
+       "fp32c": {"f": 1e-6, "pos": 1e-5, "vel": 1e-12, "q": 1e-5, "kappa": 1e-5, "kc": 1e-12}}
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_forces_match_dense_reference(setup, prec):
+    K64, ns, (x, y, vx, vy), m, kappa, kc, qc, K32 = setup
+    K = K64 if prec == "fp64" else K32
     K.set_params(kappa.cpu().numpy(), kc.cpu().numpy())
     q = qc[K.seg].contiguous()
-    fx, fy = K.forces(x, y, vx, vy, q, m)
+    fx, fy, px, py = K.forces(x, y, vx, vy, q, m, pair=True)
     rx, ry = torch_forces(x, y, vx, vy, q, m, kappa, kc, 3.0, ns)
     err = torch.sqrt(((fx - rx) ** 2 + (fy - ry) ** 2).sum() / (rx**2 + ry**2).sum()).item()
-    assert err < 1e-12
+    assert err < TOL[prec]["f"]
+    zero = torch.zeros_like(kc)
+    rpx, rpy = torch_forces(x, y, torch.zeros_like(vx), torch.zeros_like(vy), q, m, kappa, zero, 0.0, ns)
+    err = torch.sqrt(((px - rpx) ** 2 + (py - rpy) ** 2).sum() / (rpx**2 + rpy**2).sum()).item()
+    assert err < TOL[prec]["f"]
 
 
-def test_vjp_matches_torch_autograd(setup):
-    K, ns, (x, y, vx, vy), m, kappa, kc, qc = setup
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_vjp_matches_torch_autograd(setup, prec):
+    K64, ns, (x, y, vx, vy), m, kappa, kc, qc, K32 = setup
+    K = K64 if prec == "fp64" else K32
+    tol = TOL[prec]
     K.set_params(kappa.cpu().numpy(), kc.cpu().numpy())
     g = torch.Generator(device="cuda").manual_seed(3)
     ax = torch.randn(x.shape, dtype=torch.float64, device="cuda", generator=g)
@@ -94,13 +109,13 @@ def test_vjp_matches_torch_autograd(setup):
     def rel(a, b):
         return (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
 
-    assert rel(gx, leaves[0].grad) < 1e-11
-    assert rel(gy, leaves[1].grad) < 1e-11
-    assert rel(gvx, leaves[2].grad) < 1e-12
-    assert rel(gvy, leaves[3].grad) < 1e-12
-    assert rel(gq, leaves[4].grad) < 1e-11
-    assert rel(K.per_cloud(gk), kap.grad) < 1e-11
-    assert rel(K.per_cloud(gc), kcc.grad) < 1e-12
+    assert rel(gx, leaves[0].grad) < tol["pos"]
+    assert rel(gy, leaves[1].grad) < tol["pos"]
+    assert rel(gvx, leaves[2].grad) < tol["vel"]
+    assert rel(gvy, leaves[3].grad) < tol["vel"]
+    assert rel(gq, leaves[4].grad) < tol["q"]
+    assert rel(K.per_cloud(gk), kap.grad) < tol["kappa"]
+    assert rel(K.per_cloud(gc), kcc.grad) < tol["kc"]
 
 
 def _loss(K, x0, y0, vx0, vy0, kappa, qc, kc, m, xt, yt, steps, every):
@@ -111,7 +126,7 @@ def _loss(K, x0, y0, vx0, vy0, kappa, qc, kc, m, xt, yt, steps, every):
 
 
 def test_rollout_gradient_vs_finite_differences_and_torch(setup):
-    K, ns, (x, y, vx, vy), m, kappa, kc, qc = setup
+    K, ns, (x, y, vx, vy), m, kappa, kc, qc, _ = setup
     steps, every = 23, 7  # a partial last segment
     xt = x + 1e-5
     yt = y - 2e-5
@@ -175,3 +190,30 @@ def test_rollout_gradient_vs_finite_differences_and_torch(setup):
     assert abs(Lr.item() - L.item()) <= 1e-12 * abs(L.item())
     for a, b in ((kap.grad, kapr.grad), (qq.grad, qr.grad), (kcc.grad, kcr.grad), (x0.grad, x0r.grad)):
         assert (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() < 1e-9
+
+
+def test_adjoint64_smooth_gradients_vs_finite_differences_and_fp64():
+    """The 64 x 2048-particle, 200-step workload's shape on its first four
+    clouds (clouds are independent, so each cloud's gradient is the same in
+    the 64-cloud problem): FP32C and FP64 adjoint gradients of the loss with
+    respect to kappa, q, k_c and initial positions against central finite
+    differences (relative step 1e-6, FP64 rollouts) to 1e-4, and FP32C
+    against the FP64 adjoint gradient."""
+    from demon_simulation_code_gb300.fit import TrajectoryFit
+
+    w = W.adjoint64_smooth()
+    sub = W.Workload(w.name, w.clouds[:4], w.dt, w.steps, extra=w.extra)
+    f64 = TrajectoryFit(sub, precision="fp64")
+    f32 = TrajectoryFit(sub, precision="fp32c")
+    L64, g64 = f64.loss_and_grad()
+    L32, g32 = f32.loss_and_grad()
+    assert abs(L32.item() / L64.item() - 1) < 1e-6
+    for name in ("kappa", "q", "kc"):
+        fd = f64.finite_difference(name)
+        assert ((g64[name] - fd).abs() / fd.abs()).max().item() < 1e-6, name
+        assert ((g32[name] - fd).abs() / fd.abs()).max().item() < 1e-4, name
+        assert ((g32[name] - g64[name]).abs() / g64[name].abs()).max().item() < 1e-5, name
+    fd, idx = f64.finite_difference("x0", particles=[3, 510, 1029, 2047])
+    assert ((g64["x0"][idx] - fd).abs() / fd.abs()).max().item() < 1e-4
+    assert ((g32["x0"][idx] - fd).abs() / fd.abs()).max().item() < 1e-4
+    assert ((g32["x0"] - g64["x0"]).norm() / g64["x0"].norm()).item() < 1e-3
