@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--batch-steps", type=int, default=32)
+    ap.add_argument("--adjoint-grads", type=int, default=2,
+                    help="timed loss+gradient evaluations of the 64-cloud trajectory fit (0 = skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", default=None, help="pin a kernel variant (skips the autotuner)")
     ap.add_argument("--split", type=int, default=0, help="j split for --kernel (0 = cost model)")
@@ -356,6 +358,37 @@ def run_gb300(args, world, rank, local):
                  "graph_captured": args.batch_steps >= 16}
         bt.close()
 
+    # differentiable rollout: 64 clouds x 2048, 200 RK4 steps forward, checkpointed
+    # adjoint backward (FP32C pair arithmetic; FP64 targets built untimed)
+    adjoint = None
+    if args.adjoint_grads > 0:
+        from demon_simulation_code_gb300.fit import TrajectoryFit
+
+        wa = W.adjoint64_smooth()
+        fit = TrajectoryFit(wa, precision="fp32c")
+        fit.loss_and_grad()  # warm-up
+        torch.cuda.synchronize()
+        l0 = fit.K.ctx.launch_count()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record(stream)
+        for _ in range(args.adjoint_grads):
+            L, _ = fit.loss_and_grad()
+        b.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        el = a.elapsed_time(b) / 1e3
+        sweeps = (fit.K.ctx.launch_count() - l0) / args.adjoint_grads  # force + VJP launches per gradient
+        adjoint = {"workload": wa.name, "clouds": len(fit.ns), "n": fit.ns[0], "steps": fit.steps,
+                   "checkpoint_every": fit.every, "precision": "fp32c",
+                   "seconds_per_gradient": el / args.adjoint_grads,
+                   "wall_seconds_per_gradient": wall / args.adjoint_grads,
+                   "pair_sweeps_per_gradient": sweeps,
+                   "value": sweeps * fit.pairs_per_eval * args.adjoint_grads / el, "unit": UNIT,
+                   "loss": float(L.item()), "gradients": "kappa, q, k_c per cloud; initial positions"}
+        del fit
+
     cpu = None
     if rank == 0 and not args.no_cpu and args.cpu_steps > 0:
         threads = cpu_threads()
@@ -389,6 +422,7 @@ def run_gb300(args, world, rank, local):
                          "peak_source": "in-run FP32 FMA probe (dm_probe_peak); "
                                         "MEASURED_PEAKS.json has no FP32 figure"},
             "batch": batch,
+            "adjoint": adjoint,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

@@ -88,6 +88,9 @@ class Oracle:
         lib.or_forces.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp,
                                   ctypes.POINTER(Params), ctypes.c_uint64, ctypes.c_int,
                                   _dp, _dp, ctypes.c_int]
+        lib.or_forces_rows.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp,
+                                       ctypes.POINTER(Params), ctypes.c_uint64, ctypes.c_int,
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp, _dp, ctypes.c_int]
         lib.or_rk4_fixed.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp,
                                      ctypes.POINTER(Params), ctypes.c_double, ctypes.c_int,
                                      ctypes.c_uint64, ctypes.c_int]
@@ -127,6 +130,16 @@ class Oracle:
         fy = np.zeros(n)
         self.lib.or_forces(n, _ptr(x), _ptr(y), _ptr(vx), _ptr(vy), _ptr(q), _ptr(m),
                            ctypes.byref(params), step, stage, _ptr(fx), _ptr(fy), nthreads)
+        return fx, fy
+
+    def forces_rows(self, x, y, vx, vy, q, m, params, rows, step=0, stage=1, nthreads=1):
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        fx = np.zeros(len(rows))
+        fy = np.zeros(len(rows))
+        self.lib.or_forces_rows(len(x), _ptr(x), _ptr(y), _ptr(vx), _ptr(vy), _ptr(q), _ptr(m),
+                                ctypes.byref(params), step, stage, len(rows),
+                                rows.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(fx), _ptr(fy),
+                                nthreads)
         return fx, fy
 
     def rk4_fixed(self, x, y, vx, vy, q, m, params, dt, nsteps, step0=0, nthreads=1):

@@ -298,6 +298,57 @@ void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
  * All forces of one RK stage.
  * ------------------------------------------------------------------------- */
 
+void or_forces_rows(int n, const double *xs, const double *ys,
+                    const double *vxs, const double *vys, const double *q,
+                    const double *m, const or_params *p, uint64_t step,
+                    int stage, int nrows, const int *rows, double *fx,
+                    double *fy, int nthreads) {
+    const double C = or_coulomb();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int k = 0; k < nrows; k++) {
+        const int i = rows[k];
+        double sx = 0.0, sy = 0.0;
+        if (p->flags & OR_CONFINEMENT_FORCE) {
+            const double c = q[i] * p->confine;
+            sx += c * xs[i];
+            sy += c * ys[i];
+        }
+        if (p->flags & OR_DRAG_FORCE) {
+            const double d = m[i] * -p->gamma;
+            sx += d * vxs[i];
+            sy += d * vys[i];
+        }
+        if (p->flags & OR_RECT_CONFINEMENT_FORCE) {
+            sx += (q[i] * p->confine_x) * xs[i];
+            sy += (q[i] * p->confine_y) * ys[i];
+        }
+        if (p->flags & OR_SHIELDED_COULOMB_FORCE) {
+            double px = 0.0, py = 0.0;
+            for (int j = 0; j < n; j++) {
+                if (j == i) continue;
+                double ax, ay;
+                /* the (i, i+1) pair of an even-aligned 2-block takes the
+                 * intra-block form, every other pair the block form; a pair's
+                 * value is the same from either side (qq and r are symmetric) */
+                const int hit = ((j ^ 1) == i && (i | 1) < n)
+                    ? pair_intra(xs[i] - xs[j], ys[i] - ys[j], q[i] * q[j], p->shielding, C, &ax, &ay)
+                    : pair_block(xs[i] - xs[j], ys[i] - ys[j], q[i] * q[j], p->shielding, C, &ax, &ay);
+                if (hit) { px += ax; py += ay; }
+            }
+            sx += px;
+            sy += py;
+        }
+        if (p->flags & OR_THERMAL_FORCE) {
+            double tx, ty;
+            or_thermal_one(p, (uint32_t)i, step, stage, &tx, &ty);
+            sx += tx;
+            sy += ty;
+        }
+        fx[k] = sx;
+        fy[k] = sy;
+    }
+}
+
 void or_forces(int n, const double *xs, const double *ys, const double *vxs,
                const double *vys, const double *q, const double *m,
                const or_params *p, uint64_t step, int stage, double *fx,

@@ -86,6 +86,18 @@ void or_forces(int n, const double *xs, const double *ys,
                const double *q, const double *m, const or_params *p,
                uint64_t step, int stage, double *fx, double *fy, int nthreads);
 
+/* The same total force for selected particles only (fx[k], fy[k] for
+ * particle rows[k]), each row's pair sum in index order j = 0..n-1 with the
+ * reference's pair formulas (ShieldedCoulombForce.cpp:138-159 for the
+ * particle's 2-block partner, :172-237 otherwise).  Pair values are those of
+ * or_forces; only the summation order differs.  For spot checks at sizes
+ * where the full O(N^2) pass is too slow on the CPU. */
+void or_forces_rows(int n, const double *xs, const double *ys,
+                    const double *vxs, const double *vys, const double *q,
+                    const double *m, const or_params *p, uint64_t step,
+                    int stage, int nrows, const int *rows, double *fx,
+                    double *fy, int nthreads);
+
 /* Runge_Kutta4::moveParticles (Runge_Kutta4.cpp:23-137) with CacheOperator
  * (CacheOperator.cpp:18-73) and a FIXED dt (line 25's modifyTimeStep left out),
  * for an explicit step count.  x, y, vx, vy are updated in place.  step0 is

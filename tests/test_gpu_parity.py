@@ -323,3 +323,64 @@ def test_autotuner_reports_a_variant(gpu_ctx):
     assert name.startswith("fp32c<") and split >= 1
     name64, split64 = c.autotune("fp64")
     assert name64.startswith("fp64<") and split64 >= 1
+
+
+@pytest.fixture(scope="module")
+def square256k_forces(gpu_ctx):
+    """FP64 and FP32C shielded-Coulomb forces of the N=262144 cloud (0.1 m
+    square, charges normal(-1.6e-15, 5%), kappa = 5e4), in caller order.  The
+    pair force alone: the 1e8 V/m^2 walls are ~1e4 times stronger and would
+    hide it in a total-force comparison."""
+    c0 = W.square256k().clouds[0]
+    out = {}
+    for prec in ("fp64", "fp32c"):
+        c = coulomb_cloud(gpu_ctx, c0.x, c0.y, c0.q, c0.shielding)
+        out[prec] = c.eval_forces(prec)
+        c.close()
+    return c0, out
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_square256k_rows_vs_oracle(square256k_forces, oracle_lib, prec):
+    """Full size: 1024 seeded rows against the oracle's row-wise restatement
+    (same pair values as the reference; only the summation order differs)."""
+    c0, out = square256k_forces
+    rows = np.sort(np.random.default_rng(11).choice(c0.n, 1024, replace=False))
+    p = oracle.make_params(flags=W.SHIELDED_COULOMB, shielding=c0.shielding)
+    rx, ry = oracle_lib.forces_rows(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m, p, rows, nthreads=os.cpu_count())
+    fx, fy = out[prec]
+    err = e_F(fx[rows], fy[rows], rx, ry)
+    print(f"square256k {prec} e_F(1024 rows) = {err:.3e}")
+    assert err <= TOL[prec]
+
+
+def test_square256k_fp32c_vs_fp64_all_rows(square256k_forces):
+    """Full size, every row: the FP32C forces against the FP64 kernel's."""
+    _, out = square256k_forces
+    (fx, fy), (rx, ry) = out["fp32c"], out["fp64"]
+    err = e_F(fx, fy, rx, ry)
+    print(f"square256k fp32c vs fp64 e_F = {err:.3e}")
+    assert err <= TOL["fp32c"]
+
+
+def test_square256k_step_fp32c_tracks_fp64(gpu_ctx):
+    """Two RK4 steps of dt = 5e-5 s at full size: FP32C displacements and
+    velocities within 1e-5 of the FP64 ones (relative to their largest
+    value).  The uniform random square holds pairs ~1e-7 m apart that are
+    kicked by decimetres in a step, so errors are relative to the motion,
+    not to the box."""
+    c0 = W.square256k().clouds[0]
+    res = {}
+    for prec in ("fp64", "fp32c"):
+        c = DeviceCloud.from_cloud(gpu_ctx, c0)
+        c.step(2, 5e-5, prec)
+        res[prec] = c.download()
+        c.close()
+    (x, y, vx, vy), (x64, y64, vx64, vy64) = res["fp32c"], res["fp64"]
+    assert np.all(np.isfinite(x)) and np.all(np.isfinite(vx))
+    disp = max(np.abs(x64 - c0.x).max(), np.abs(y64 - c0.y).max())
+    err = max(np.abs(x - x64).max(), np.abs(y - y64).max())
+    print(f"square256k 2 steps: max displacement {disp:.3e} m, fp32c-fp64 {err:.3e} m")
+    assert err <= 1e-5 * disp
+    vmax = max(np.abs(vx64).max(), np.abs(vy64).max())
+    assert max(np.abs(vx - vx64).max(), np.abs(vy - vy64).max()) <= 1e-5 * vmax
