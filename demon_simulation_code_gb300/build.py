@@ -64,5 +64,48 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+HOST = os.path.join(PKG, "host")
+HOST_LIB = os.path.join(PKG, "libdemon_gb300_host.so")
+DRIVER = os.path.join(PKG, "demon_gb300")
+HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
+              "-Wno-ignored-qualifiers",  # the reference's signatures return const values
+              "-I" + os.path.join(ROOT, "include"), "-I" + HOST]
+
+
+def cxx() -> str:
+    return os.environ.get("CXX") or "g++"
+
+
+def build_host(force: bool = False, verbose: bool = False) -> tuple[str, str]:
+    """The C++ host classes (libdemon_gb300_host.so, linked to the CUDA
+    library) and the demon_gb300 driver program."""
+    lib = build(force=force, verbose=verbose)
+    srcs = sorted(os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".cpp") and f != "driver.cpp")
+    deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
+    deps += [os.path.join(ROOT, "include", "demon_gb300.h"), lib]
+    link = ["-L" + PKG, "-ldemon_gb300", "-Wl,-rpath,$ORIGIN"]
+    if force or _stale(HOST_LIB, deps):
+        tmp = HOST_LIB + ".tmp"
+        cmd = [cxx(), *HOST_FLAGS, "-shared", "-o", tmp, *srcs, *link]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError("host build failed: %s\n%s" % (" ".join(cmd), r.stdout.decode(errors="replace")))
+        os.replace(tmp, HOST_LIB)
+    drv = os.path.join(HOST, "driver.cpp")
+    if force or _stale(DRIVER, deps + [drv, HOST_LIB]):
+        tmp = DRIVER + ".tmp"
+        cmd = [cxx(), *HOST_FLAGS, "-o", tmp, drv, "-L" + PKG, "-ldemon_gb300_host", *link]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed: %s\n%s" % (" ".join(cmd), r.stdout.decode(errors="replace")))
+        os.replace(tmp, DRIVER)
+    return HOST_LIB, DRIVER
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
+    print(build_host(force="--force" in sys.argv, verbose=True))

@@ -87,6 +87,7 @@ struct dm_cloud {
     double *d_dt = nullptr;
     unsigned int *d_min = nullptr;
     float *d_dmin = nullptr;
+    int eval_thermal_stage = 1;  // substep of the thermal kicks in force-only evaluations
     int split[2] = {0, 0};  // cluster size per precision (0 = not chosen yet)
     int tuned_variant[2] = {-1, -1};  // per precision: index into kVariants
     float4 *partial = nullptr;         // [partial_cap][n_pad] non-cluster partial sums
@@ -158,6 +159,7 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     P.f = c->f;
     P.stage = stage;
     P.mode = mode;
+    P.therm_stage = (mode == kModeForceOnly) ? c->eval_thermal_stage : stage;
     P.dt = dt;
     P.dt_dev = dt_dev;
     P.coulomb = c->coulomb;
@@ -908,6 +910,15 @@ int dm_cloud_eval_forces(dm_cloud *c, int precision, double *fx, double *fy) {
     return DM_OK;
 }
 
+int dm_cloud_eval_forces_stage(dm_cloud *c, int precision, int stage, double *fx, double *fy) {
+    if (!c) return DM_ERR_ARG;
+    if (stage < 1 || stage > 4) return c->ctx->fail(DM_ERR_ARG, "dm_cloud_eval_forces_stage: stage must be 1..4");
+    c->eval_thermal_stage = stage;
+    const int rc = dm_cloud_eval_forces(c, precision, fx, fy);
+    c->eval_thermal_stage = 1;
+    return rc;
+}
+
 int dm_cloud_step(dm_cloud *c, int nsteps, double dt, int precision, double *t_inout) {
     if (!c) return DM_ERR_ARG;
     dm_ctx *ctx = c->ctx;
@@ -1184,6 +1195,7 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt) {
     P.c = B->d;
     P.stage = stage;
     P.mode = mode;
+    P.therm_stage = (mode == kModeForceOnly) ? 1 : stage;
     P.dt = dt;
     P.coulomb = B->d.coulomb;
     P.fx_out = B->d_fx;

@@ -62,6 +62,7 @@ struct StageParams {
     ForceParams f;
     int stage;            // 1..4
     int mode;             // StageMode
+    int therm_stage;      // substep index of the thermal kicks (force-only: any of 1..4)
     double dt;            // fixed dt (used when dt_dev == nullptr)
     const double *dt_dev; // adaptive dt computed on the device
     double coulomb;       // 1/(4 pi eps0)
@@ -248,8 +249,7 @@ __device__ __forceinline__ bool ref_in_cutoff(double dx, double dy, double kappa
 __device__ __forceinline__ double2 stage_thermal(const StageParams &P, int i) {
     double tx = 0.0, ty = 0.0;
     if (P.f.flags & kThermal) {
-        const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
-        thermal_kick(P.f, (uint32_t)P.c.orig[i], stage_step_index(P), s, tx, ty);
+        thermal_kick(P.f, (uint32_t)P.c.orig[i], stage_step_index(P), P.therm_stage, tx, ty);
     }
     return make_double2(tx, ty);
 }

@@ -6,8 +6,8 @@
  * a set of C++ virtual classes.  Each entry point below replaces one piece of
  * that class API; the comment on each names the reference interface it
  * stands in for (file:line).  The C++ classes in
- * demon_simulation_code_gb300/csrc/host/ re-expose the reference's class
- * names on top of these calls.
+ * demon_simulation_code_gb300/host/ re-expose the reference's class names
+ * on top of these calls.
  *
  * Conventions
  *  - Every call returns an int status: 0 (DM_OK) on success, a DM_ERR_* code
@@ -161,9 +161,15 @@ int dm_cloud_set_forces(dm_cloud *cloud, const dm_force_params *params);
 
 /* One force evaluation of every enabled force at the current state, i.e.
  * the sum of Force::force1 over the ForceArray (Runge_Kutta2.cpp:90-93,
- * Force.h:28-49) written to host fx, fy (not accumulated).  `thermal_step`
- * is the RNG step index used for ThermalForce. */
+ * Force.h:28-49) written to host fx, fy (not accumulated).  ThermalForce's
+ * kicks are those of substep 1 of the step counter's step. */
 int dm_cloud_eval_forces(dm_cloud *cloud, int precision, double *fx, double *fy);
+/* The same at the current state taken as the inputs of RK substep `stage`
+ * (1..4): the thermal kicks are substep `stage`'s.  Stands in for
+ * Force::force1..4 (Force.h:28-49) when the caller supplies the substep
+ * positions and velocities (dm_cloud_upload). */
+int dm_cloud_eval_forces_stage(dm_cloud *cloud, int precision, int stage,
+                               double *fx, double *fy);
 
 /* Same, writing to device arrays of n doubles. */
 int dm_cloud_eval_forces_device(dm_cloud *cloud, int precision, double *d_fx,
