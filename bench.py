@@ -340,22 +340,37 @@ def run_gb300(args, world, rank, local):
     if args.batch_steps > 0:
         from demon_simulation_code_gb300 import DeviceBatch
 
+        from demon_simulation_code_gb300.shard import assign_clouds, imbalance
+
         wb = W.batch256()
-        bt = DeviceBatch(ctx, wb.clouds)
+        # N > 1: whole clouds per rank, balanced by sum N^2 (no exchange)
+        parts = assign_clouds([c.n for c in wb.clouds], world)
+        bt = DeviceBatch(ctx, [wb.clouds[c] for c in parts[rank]])
         bt.step(4, wb.dt)
         torch.cuda.synchronize()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
         a.record(stream)
         bt.step(args.batch_steps, wb.dt)
         b.record(stream)
         torch.cuda.synchronize()
         el = a.elapsed_time(b) / 1e3
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([el], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
         name, nitems, grid = bt.info()
         batch = {"workload": wb.name, "value": 4.0 * wb.pairs_per_eval * args.batch_steps / el,
                  "unit": UNIT, "steps": args.batch_steps, "ms_per_step": el / args.batch_steps * 1e3,
                  "variant": name, "work_items": nitems, "persistent_grid": grid,
-                 "graph_captured": args.batch_steps >= 16}
+                 "graph_captured": args.batch_steps >= 16,
+                 "sharding": {"ranks": world, "clouds_per_rank": [len(p) for p in parts],
+                              "imbalance": imbalance([c.n for c in wb.clouds], parts),
+                              "scaling": "strong"}}
         bt.close()
 
     # differentiable rollout: 64 clouds x 2048, 200 RK4 steps forward, checkpointed

@@ -1,0 +1,66 @@
+"""Many clouds over several GPUs: one process per GPU, whole clouds per rank.
+
+Clouds never interact, so the batched and trajectory-fit workloads shard
+with no data-path exchange: each rank steps (or differentiates) its own
+clouds and only small per-cloud results meet at the end.  Work per cloud is
+~N^2 pair interactions, so clouds are dealt by longest-processing-time:
+largest N^2 first, each to the rank with the least work so far (ties to the
+lower rank) -- deterministic, so every rank computes the same assignment
+without talking.
+
+A single cloud does not shard here (this path runs one GPU per cloud:
+replicas).  The reference has no multi-process mode.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def assign_clouds(ns, world: int) -> list[list[int]]:
+    """Cloud indices per rank (each list ascending), balanced by sum N_c^2."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    load = [0] * world
+    out = [[] for _ in range(world)]
+    order = sorted(range(len(ns)), key=lambda c: (-int(ns[c]) ** 2, c))
+    for c in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(c)
+        load[r] += int(ns[c]) ** 2
+    return [sorted(v) for v in out]
+
+
+def imbalance(ns, parts) -> float:
+    """max rank work / mean rank work (1.0 = perfect)."""
+    w = [sum(int(ns[c]) ** 2 for c in p) for p in parts]
+    return max(w) / (sum(w) / len(w)) if sum(w) else 1.0
+
+
+def gather_per_cloud(values, ids, nclouds: int, group=None):
+    """Per-cloud values computed on each rank (values[k] for cloud ids[k],
+    a float64 array of shape [len(ids), ...]) -> the full [nclouds, ...]
+    array on every rank (all_gather of a zero-padded buffer + sum; each
+    cloud belongs to exactly one rank)."""
+    import torch
+    import torch.distributed as dist
+
+    values = np.asarray(values, dtype=np.float64)
+    full = np.zeros((nclouds,) + values.shape[1:], dtype=np.float64)
+    full[np.asarray(ids, dtype=np.int64)] = values
+    t = torch.from_numpy(full)
+    if dist.get_backend(group) == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return t.cpu().numpy()
+
+
+def sum_scalar(value: float, group=None) -> float:
+    """Sum of one float over the ranks (e.g. the trajectory-fit loss)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    if dist.get_backend(group) == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return float(t.item())

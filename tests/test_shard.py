@@ -1,0 +1,82 @@
+"""Cloud sharding over ranks (CPU, gloo, world size 2): the assignment is
+balanced and deterministic, and per-cloud results computed on each rank's
+shard -- here the oracle's FP64 diagnostics of every cloud -- gather to
+exactly the single-process result."""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from demon_simulation_code_gb300 import workloads as W
+from demon_simulation_code_gb300.shard import assign_clouds, imbalance
+
+torch = pytest.importorskip("torch")
+
+
+def test_assignment_covers_every_cloud_once_and_balances():
+    ns = W.batch256().clouds
+    ns = [c.n for c in ns]
+    for world in (1, 2, 3, 4, 8):
+        parts = assign_clouds(ns, world)
+        flat = sorted(c for p in parts for c in p)
+        assert flat == list(range(len(ns)))
+        assert imbalance(ns, parts) < 1.01
+        assert parts == assign_clouds(ns, world)  # deterministic
+
+
+def test_assignment_edge_cases():
+    assert assign_clouds([], 2) == [[], []]
+    assert assign_clouds([5], 3) == [[0], [], []]
+    assert assign_clouds([10, 10, 1], 2) == [[0, 2], [1]]
+    with pytest.raises(ValueError):
+        assign_clouds([1], 0)
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank, world, port, out_dir):
+    import torch.distributed as dist
+
+    import oracle
+    from demon_simulation_code_gb300.shard import gather_per_cloud, sum_scalar
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        clouds = W.batch256(nclouds=12, nmin=16, nmax=128).clouds
+        ids = assign_clouds([c.n for c in clouds], world)[rank]
+        o = oracle.Oracle()
+        vals = []
+        for c in ids:
+            cl = clouds[c]
+            d = o.diagnostics(cl.x, cl.y, cl.vx, cl.vy, cl.q, cl.m, oracle.make_params(**cl.params()))
+            vals.append(d)
+        full = gather_per_cloud(np.array(vals).reshape(len(ids), 5), ids, len(clouds))
+        total = sum_scalar(float(sum(v[1] for v in vals)))
+        np.save(os.path.join(out_dir, f"r{rank}.npy"), np.concatenate([full.ravel(), [total]]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gloo_two_ranks_gather_per_cloud_results(tmp_path):
+    import torch.multiprocessing as mp
+
+    import oracle
+
+    mp.spawn(_worker, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
+    r0, r1 = np.load(tmp_path / "r0.npy"), np.load(tmp_path / "r1.npy")
+    assert np.array_equal(r0, r1)
+    clouds = W.batch256(nclouds=12, nmin=16, nmax=128).clouds
+    o = oracle.Oracle()
+    ref = np.array([o.diagnostics(c.x, c.y, c.vx, c.vy, c.q, c.m, oracle.make_params(**c.params()))
+                    for c in clouds])
+    assert np.array_equal(r0[:-1].reshape(12, 5), ref)
+    assert abs(r0[-1] - ref[:, 1].sum()) <= 1e-12 * abs(ref[:, 1].sum())
