@@ -54,6 +54,19 @@ __device__ __forceinline__ float exp_neg(float a, const ExpConsts &E) {
     return p * scale;
 }
 
+// e^{-a} for a >= 0 on the SFU: t = a*log2(e) is rounded to FP32 (absolute
+// error up to ~1e-6 at a = 10, i.e. a relative error of the result of
+// ~6e-7); the rounding residue t_lo (exact to ~2^-48) is put back to first
+// order, 2^{-(t + t_lo)} = 2^{-t} (1 - t_lo ln 2).  Relative error: that of
+// the hardware ex2.approx (a few ulp) plus ~(t_lo ln 2)^2 / 2 < 1e-12.
+__device__ __forceinline__ float exp_neg_sfu(float a, const ExpConsts &E) {
+    const float t = a * E.l2e_hi;
+    const float t_lo = fmaf(a, E.l2e_lo, fmaf(a, E.l2e_hi, -t));
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(-t));
+    return e * fmaf(-t_lo, 0.693147182f, 1.0f);
+}
+
 // Kahan (compensated) accumulation: true sum ~= s - c.
 __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
     const float y = v - c;
@@ -131,10 +144,12 @@ struct PairCtx {
     int ii;
 };
 
+// The pair force on i from j (added into px, py; nothing for j == i or a
+// pair outside the cutoff).
 __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpConsts &E, int b,
                                              float xh_i, float yh_i, const PairCtx &ic,
-                                             const float4 &A, const float4 &Bj, int jg, float &sx,
-                                             float &sy, float &cx, float &cy) {
+                                             const float4 &A, const float4 &Bj, int jg, float &px,
+                                             float &py) {
     if (jg == ic.ii) return;
     const float dx = (xh_i - A.x) + (ic.xl - Bj.x);
     const float dy = (yh_i - A.y) + (ic.yl - Bj.y);
@@ -154,11 +169,11 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
     y = fmaf(0.5f * ee, y, y);
     const float r = r2 * y;
     const float kr = P.kappa_f * r;
-    const float ex = exp_neg(kr, E);
+    const float ex = exp_neg_sfu(kr, E);
     // C q_i q_j (1 + kr) e^{-kr} / r^3
     const float s = ((ic.qc * A.w) * (1.0f + kr)) * ex * ((y * y) * y);
-    kahan_add(sx, cx, s * dx);
-    kahan_add(sy, cy, s * dy);
+    px = fmaf(s, dx, px);
+    py = fmaf(s, dy, py);
 }
 
 // The FP32C sweep of one i tile against rank `rank` of S of the j chunks:
@@ -239,15 +254,23 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
             ic.ii = __float_as_int(c4.w);
             const float xh = -0.5f * mx2[K].x, yh = -0.5f * my2[K].x;
             float4 acc = my_acc[K * 32 + lane];
+            // up to 4 pair terms are summed plainly, each group then added to
+            // the compensated sums (the group's rounding is that of one pair term)
             do {
-                const int e = __ffs(mask) - 1;
-                mask &= mask - 1u;
-                const int jj = my_queue[K * 32 + e].x;  // index into the tile's j
-                const float4 Bj = s_pb[jj];
-                const float xj = reinterpret_cast<const float *>(s_x4)[jj];
-                const float yj = reinterpret_cast<const float *>(s_y4)[jj];
-                precise_pair(P, E, b, xh, yh, ic, make_float4(xj, yj, 0.0f, Bj.z), Bj,
-                             __float_as_int(Bj.w), acc.x, acc.y, acc.z, acc.w);
+                float px = 0.0f, py = 0.0f;
+#pragma unroll 1
+                for (int g = 0; g < 4 && mask; g++) {
+                    const int e = __ffs(mask) - 1;
+                    mask &= mask - 1u;
+                    const int jj = my_queue[K * 32 + e].x;  // index into the tile's j
+                    const float4 Bj = s_pb[jj];
+                    const float xj = reinterpret_cast<const float *>(s_x4)[jj];
+                    const float yj = reinterpret_cast<const float *>(s_y4)[jj];
+                    precise_pair(P, E, b, xh, yh, ic, make_float4(xj, yj, 0.0f, Bj.z), Bj,
+                                 __float_as_int(Bj.w), px, py);
+                }
+                kahan_add(acc.x, acc.z, px);
+                kahan_add(acc.y, acc.w, py);
             } while (mask);
             my_acc[K * 32 + lane] = acc;
         }
