@@ -30,9 +30,6 @@ namespace {
 
 std::string g_create_error;
 
-// FP32C default shape: 8 warps sharing one 128-particle i tile (4 per
-// lane), j tiles of 256 4-j chunks; the autotuner may pick another variant.
-constexpr int kNW32 = 8, kILP32 = 4, kTC32 = 256;
 // FP64: 2 j-groups x 128 i-lanes, 2 particles per lane, 512-particle j tiles
 constexpr int kNI64 = 128, kG64 = 2, kILP64 = 2, kJT64 = 512;
 constexpr int kGraphSteps = 16;
@@ -332,6 +329,7 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
 }
 
 int tune_precision(dm_cloud *c, int precision);
+int reorder(dm_cloud *c);
 
 // One launch of the fused pair + stage kernel(s) with the cloud's tuned
 // variant and split.
@@ -391,6 +389,10 @@ int tune_precision(dm_cloud *c, int precision) {
         DM_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
         if (cs != cudaStreamCaptureStatusNone)
             return ctx->fail(DM_ERR_STATE, "autotuning needs an uncaptured stream (run one step first)");
+        if (c->order_dirty) {  // tune on the particle order the steps will see
+            int rc = reorder(c);
+            if (rc) return rc;
+        }
         cudaEvent_t a, b;
         DM_CUDA(ctx, cudaEventCreate(&a));
         DM_CUDA(ctx, cudaEventCreate(&b));
@@ -1286,6 +1288,10 @@ int batch_tune(dm_batch *B) {
     }
     int best = 0;
     if (ctx->autotune) {
+        if (B->order_dirty) {  // tune on the particle order the steps will see
+            rc = batch_reorder(B);
+            if (rc) return rc;
+        }
         cudaEvent_t a, b;
         DM_CUDA(ctx, cudaEventCreate(&a));
         DM_CUDA(ctx, cudaEventCreate(&b));
@@ -1295,17 +1301,19 @@ int batch_tune(dm_batch *B) {
             DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
             rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);  // warm-up
             if (rc) return rc;
-            DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
-            DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
-            rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);
-            if (rc) return rc;
-            DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
-            DM_CUDA(ctx, cudaEventSynchronize(b));
-            float ms = 0.0f;
-            DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = v;
+            for (int r = 0; r < 3; r++) {  // best of three
+                DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
+                DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
+                rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);
+                if (rc) return rc;
+                DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
+                DM_CUDA(ctx, cudaEventSynchronize(b));
+                float ms = 0.0f;
+                DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = v;
+                }
             }
         }
         cudaEventDestroy(a);

@@ -239,8 +239,9 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
     uint32_t qn = 0u;  // queue fill per slot, 8 bits per slot (warp-uniform)
 
     // Run the precise path on the queued entries of slot K, then empty it.
-    auto flush = [&](auto kc) {
-        constexpr int K = decltype(kc)::value;
+    // K is a runtime value (the slot's i position comes in xh, yh), so the
+    // precise path exists once in the kernel's code.
+    auto flush = [&](int K, float xh, float yh) {
         __syncwarp();
         const int fill = (int)((qn >> (8 * K)) & 0xFFu);
         const int2 ent = (lane < fill) ? my_queue[K * 32 + lane] : make_int2(0, 0);
@@ -252,7 +253,6 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
             ic.yl = c4.y;
             ic.qc = c4.z;
             ic.ii = __float_as_int(c4.w);
-            const float xh = -0.5f * mx2[K].x, yh = -0.5f * my2[K].x;
             float4 acc = my_acc[K * 32 + lane];
             // up to 4 pair terms are summed plainly, each group then added to
             // the compensated sums (the group's rounding is that of one pair term)
@@ -276,6 +276,23 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         }
         __syncwarp();
         qn &= ~(0xFFu << (8 * K));
+    };
+
+    // Flushes every slot holding at least `lim` entries (runtime loop: one
+    // copy of the flush in the code).
+    auto flush_slots = [&](int lim) {
+#pragma unroll 1
+        for (int k = 0; k < ILP; k++) {
+            if ((int)((qn >> (8 * k)) & 0xFFu) >= lim) {
+                float xh = -0.5f * mx2[0].x, yh = -0.5f * my2[0].x;
+#pragma unroll
+                for (int t = 1; t < ILP; t++) {
+                    xh = (k == t) ? -0.5f * mx2[t].x : xh;
+                    yh = (k == t) ? -0.5f * my2[t].x : yh;
+                }
+                flush(k, xh, yh);
+            }
+        }
     };
 
     __syncthreads();  // s_cold complete
@@ -336,16 +353,18 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
                             const int fill = (int)((qn >> (8 * k)) & 0xFFu);
                             if (lane == 0) my_queue[k * 32 + fill] = make_int2(4 * c + u, (int)bal);
                             qn += 1u << (8 * k);
-                            if (fill == 31) flush(kc);
                         }
                     });
                 }
+                // a chunk adds at most 4 entries to a slot: keep each slot at
+                // <= 28 so the next chunk fits its 32.  The fills are 8-bit
+                // fields of qn (<= 32 each); adding 99 to every field sets its
+                // top bit exactly when the fill is >= 29.
+                if ((qn + 0x63636363u) & 0x80808080u) flush_slots(29);
             }
         }
         // queued entries index into this tile: drain before it is overwritten
-        static_for<ILP>([&](auto kc) {
-            if ((qn >> (8 * decltype(kc)::value)) & 0xFFu) flush(kc);
-        });
+        flush_slots(1);
     }
 
     // combine the NW warps in fixed order with a compensated FP32 sum (each

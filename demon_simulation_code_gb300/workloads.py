@@ -155,6 +155,16 @@ def disk16k(seed: int = 1, thermal: bool = True) -> Workload:
                     f"thermal {'Gaussian sigma=1e-14 N' if thermal else 'off'}, dt=1e-4")
 
 
+def disk16k_dense(seed: int = 1) -> Workload:
+    """disk16k's particles in a 7e-4 m disk: ~35% of all pairs inside the
+    cutoff, the density disk16k reaches when it collapses under its
+    confinement (for profiling the precise path; the state explodes within a
+    few steps)."""
+    c = disk_cloud(16384, 7e-4, seed, heat=1e-14, thermal_seed=1)
+    return Workload("disk16k_dense", [c], 1e-4, 10,
+                    "N=16384 disk R=7e-4 m (35% of pairs within kappa*r < 10), kappa=2e4, k_c=1e8")
+
+
 def square256k(seed: int = 2, n: int = 262144) -> Workload:
     rng = np.random.default_rng(seed)
     x = (rng.random(n) - 0.5) * 0.1
@@ -221,5 +231,5 @@ def adjoint64_smooth(seed: int = 4, nclouds: int = 64, n: int = 2048) -> Workloa
                     extra={"perturb": 0.2, "checkpoint_every": 20})
 
 
-WORKLOADS = {"disk512": disk512, "disk16k": disk16k, "square256k": square256k,
+WORKLOADS = {"disk512": disk512, "disk16k": disk16k, "disk16k_dense": disk16k_dense, "square256k": square256k,
              "batch256": batch256, "adjoint64": adjoint64, "adjoint64_smooth": adjoint64_smooth}

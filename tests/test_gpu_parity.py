@@ -290,16 +290,22 @@ def test_reorder_interval_does_not_change_fp64_results_beyond_rounding(gpu_ctx):
             assert rel(a, b) < 1e-13
 
 
+# kernel families by precision: FP32C has the shared-memory (fp32c) and the
+# streamed (fp32s) sweeps
+FAMILIES = {"fp64": ("fp64<",), "fp32c": ("fp32c<", "fp32s<")}
+
+
 def _variants(prec):
     from demon_simulation_code_gb300 import _lib
 
-    return [v for v in _lib.kernel_variants() if v.startswith(prec + "<")]
+    return [v for v in _lib.kernel_variants() if v.startswith(FAMILIES[prec])]
 
 
+@pytest.mark.parametrize("n", [65, 3000])
 @pytest.mark.parametrize("prec", ["fp64", "fp32c"])
-def test_every_kernel_variant_and_split_is_correct(gpu_ctx, oracle_lib, prec):
+def test_every_kernel_variant_and_split_is_correct(gpu_ctx, oracle_lib, prec, n):
     """The autotuner may pick any variant/split: every one must pass parity."""
-    c0 = W.disk_cloud(3000, 2.5e-3, 21)
+    c0 = W.disk_cloud(n, 2.5e-3 * np.sqrt(n / 3000), 21)
     rx, ry = oracle_lib.forces(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m,
                                oracle.make_params(**c0.params()))
     names = _variants(prec)
