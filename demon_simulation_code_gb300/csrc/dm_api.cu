@@ -85,6 +85,7 @@ struct dm_cloud {
     unsigned int *d_min = nullptr;
     float *d_dmin = nullptr;
     int eval_thermal_stage = 1;  // substep of the thermal kicks in force-only evaluations
+    int fo_buf = 0;              // stage buffer force-only launches read (the autotuner's dense copy: 1)
     int split[2] = {0, 0};  // cluster size per precision (0 = not chosen yet)
     int tuned_variant[2] = {-1, -1};  // per precision: index into kVariants
     float4 *partial = nullptr;         // [partial_cap][n_pad] non-cluster partial sums
@@ -157,6 +158,7 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     P.stage = stage;
     P.mode = mode;
     P.therm_stage = (mode == kModeForceOnly) ? c->eval_thermal_stage : stage;
+    P.fo_buf = (mode == kModeForceOnly) ? c->fo_buf : 0;
     P.dt = dt;
     P.dt_dev = dt_dev;
     P.coulomb = c->coulomb;
@@ -393,11 +395,36 @@ int tune_precision(dm_cloud *c, int precision) {
             int rc = reorder(c);
             if (rc) return rc;
         }
+        // Time every candidate on two states: the cloud as it is (buffer 0)
+        // and, unless it is dense already, a copy squeezed about its centre
+        // so that ~30% of the pairs are inside the cutoff (buffer 1).  A
+        // trajectory passes through both kinds (a confined cloud collapses
+        // and re-expands), and the best shape differs between them.
+        const bool big = (double)c->n * c->n > 4e9;  // ~64k particles: keep tuning short
+        int nstates = 1;
+        if (!big && c->d.rc2 > 0.0 && std::isfinite(c->d.rc2)) {
+            unsigned long long hb[4];
+            DM_CUDA(ctx, cudaMemcpyAsync(hb, c->sort.bbox, sizeof hb, cudaMemcpyDeviceToHost, ctx->stream));
+            DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            double v[4];
+            for (int k = 0; k < 4; k++) {
+                const unsigned long long o = hb[k];
+                const unsigned long long bits = (o & 0x8000000000000000ull) ? (o & 0x7fffffffffffffffull) : ~o;
+                std::memcpy(&v[k], &bits, sizeof bits);
+            }
+            const double half = 0.5 * std::max(v[2] - v[0], v[3] - v[1]);
+            const double lam = 1.8 * std::sqrt(c->d.rc2) / half;
+            if (std::isfinite(half) && half > 0.0 && lam < 0.9) {
+                tune_compress<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->d, 0.5 * (v[0] + v[2]),
+                                                                            0.5 * (v[1] + v[3]), lam);
+                DM_CUDA(ctx, cudaGetLastError());
+                nstates = 2;
+            }
+        }
         cudaEvent_t a, b;
         DM_CUDA(ctx, cudaEventCreate(&a));
         DM_CUDA(ctx, cudaEventCreate(&b));
         float best_ms = 1e30f;
-        const bool big = (double)c->n * c->n > 4e9;  // ~64k particles: keep tuning short
         for (int vi = 0; vi < kNumVariants; vi++) {
             const Variant &k = kVariants[vi];
             if (k.precision != precision) continue;
@@ -425,18 +452,21 @@ int tune_precision(dm_cloud *c, int precision) {
                     int rc = ensure_partial(c, S);
                     if (rc) return rc;
                 }
-                int rc = launch_variant(c, vi, S, 1, kModeForceOnly, 0.0, nullptr);  // warm-up
-                if (rc) return rc;
                 const int reps = big ? 1 : 3;
-                DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
-                for (int r = 0; r < reps; r++) {
-                    rc = launch_variant(c, vi, S, 1, kModeForceOnly, 0.0, nullptr);
-                    if (rc) return rc;
-                }
-                DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
-                DM_CUDA(ctx, cudaEventSynchronize(b));
                 float ms = 0.0f;
-                DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+                for (int st = 0; st < nstates; st++) {
+                    c->fo_buf = st;
+                    int rc = launch_variant(c, vi, S, 1, kModeForceOnly, 0.0, nullptr);  // warm-up
+                    if (!rc) rc = cudaEventRecord(a, ctx->stream) == cudaSuccess ? DM_OK : DM_ERR_CUDA;
+                    for (int r = 0; r < reps && !rc; r++) rc = launch_variant(c, vi, S, 1, kModeForceOnly, 0.0, nullptr);
+                    if (!rc) rc = cudaEventRecord(b, ctx->stream) == cudaSuccess ? DM_OK : DM_ERR_CUDA;
+                    if (!rc) rc = cudaEventSynchronize(b) == cudaSuccess ? DM_OK : DM_ERR_CUDA;
+                    c->fo_buf = 0;
+                    if (rc) return rc == DM_ERR_CUDA ? ctx->fail(rc, "autotuner timing failed") : rc;
+                    float one = 0.0f;
+                    DM_CUDA(ctx, cudaEventElapsedTime(&one, a, b));
+                    ms += one;
+                }
                 ms /= reps;
                 if (ms < best_ms) {
                     best_ms = ms;
@@ -1190,7 +1220,7 @@ struct dm_batch {
 
 namespace {
 
-int batch_launch_stage(dm_batch *B, int stage, int mode, double dt) {
+int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf = 0) {
     dm_ctx *ctx = B->ctx;
     const BatchVariant &k = kBatchVariants[B->variant];
     StageParams P{};
@@ -1198,6 +1228,7 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt) {
     P.stage = stage;
     P.mode = mode;
     P.therm_stage = (mode == kModeForceOnly) ? 1 : stage;
+    P.fo_buf = (mode == kModeForceOnly) ? fo_buf : 0;
     P.dt = dt;
     P.coulomb = B->d.coulomb;
     P.fx_out = B->d_fx;
@@ -1292,28 +1323,38 @@ int batch_tune(dm_batch *B) {
             rc = batch_reorder(B);
             if (rc) return rc;
         }
+        // two states, as for one cloud: the batch as it is (buffer 0) and
+        // every cloud squeezed to ~30% in-cutoff pairs (buffer 1)
+        batch_tune_compress<<<(B->total + 255) / 256, 256, 0, ctx->stream>>>(B->d, B->ddesc, B->dseg, B->dbbox);
+        DM_CUDA(ctx, cudaGetLastError());
         cudaEvent_t a, b;
         DM_CUDA(ctx, cudaEventCreate(&a));
         DM_CUDA(ctx, cudaEventCreate(&b));
         float best_ms = 1e30f;
         for (int v = 0; v < kNumBatchVariants; v++) {
             B->variant = v;
-            DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
-            rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);  // warm-up
-            if (rc) return rc;
-            for (int r = 0; r < 3; r++) {  // best of three
+            float total = 0.0f;
+            for (int st = 0; st < 2; st++) {
                 DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
-                DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
-                rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0);
+                rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0, st);  // warm-up
                 if (rc) return rc;
-                DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
-                DM_CUDA(ctx, cudaEventSynchronize(b));
-                float ms = 0.0f;
-                DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best = v;
+                float one = 1e30f;
+                for (int r = 0; r < 3; r++) {  // best of three
+                    DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, sizeof(unsigned int), ctx->stream));
+                    DM_CUDA(ctx, cudaEventRecord(a, ctx->stream));
+                    rc = batch_launch_stage(B, 1, kModeForceOnly, 0.0, st);
+                    if (rc) return rc;
+                    DM_CUDA(ctx, cudaEventRecord(b, ctx->stream));
+                    DM_CUDA(ctx, cudaEventSynchronize(b));
+                    float ms = 0.0f;
+                    DM_CUDA(ctx, cudaEventElapsedTime(&ms, a, b));
+                    one = std::min(one, ms);
                 }
+                total += one;
+            }
+            if (total < best_ms) {
+                best_ms = total;
+                best = v;
             }
         }
         cudaEventDestroy(a);

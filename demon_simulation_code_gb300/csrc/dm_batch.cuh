@@ -127,6 +127,27 @@ static __global__ void batch_keys(const double *__restrict__ x, const double *__
     vals[i] = i;
 }
 
+// For the batch autotuner: every cloud squeezed about its own box centre
+// so that ~30% of its pairs are inside its cutoff (clouds already that dense
+// are copied as they are), written as stage buffer 1 (nothing live there
+// between steps).
+static __global__ void batch_tune_compress(CloudDev c, const BatchCloud *__restrict__ desc,
+                                           const int *__restrict__ seg, const unsigned long long *bbox) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const int sg = seg[i];
+    const unsigned long long *bb = bbox + 4 * sg;
+    const double x0 = from_ordered_bits(bb[0]), y0 = from_ordered_bits(bb[1]);
+    const double x1 = from_ordered_bits(bb[2]), y1 = from_ordered_bits(bb[3]);
+    const double half = 0.5 * fmax(x1 - x0, y1 - y0);
+    double lam = 1.8 * sqrt(desc[sg].rc2) / half;
+    if (!(isfinite(lam) && lam > 0.0 && lam < 1.0)) lam = 1.0;
+    const double cx = 0.5 * (x0 + x1), cy = 0.5 * (y0 + y1);
+    CloudDev v = c;
+    v.rc2 = desc[sg].rc2;
+    write_stage_position(v, 1, i, cx + lam * (c.x[i] - cx), cy + lam * (c.y[i] - cy));
+}
+
 // Stage buffer 0 from the base positions, with each particle's own cloud's
 // filter bound.
 static __global__ void batch_init_positions(CloudDev c, const BatchCloud *__restrict__ desc,

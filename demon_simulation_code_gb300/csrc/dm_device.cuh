@@ -63,6 +63,7 @@ struct StageParams {
     int stage;            // 1..4
     int mode;             // StageMode
     int therm_stage;      // substep index of the thermal kicks (force-only: any of 1..4)
+    int fo_buf;           // force-only launches: stage position buffer to read (0 = the state)
     double dt;            // fixed dt (used when dt_dev == nullptr)
     const double *dt_dev; // adaptive dt computed on the device
     double coulomb;       // 1/(4 pi eps0)
@@ -258,7 +259,7 @@ __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, doub
                                                double fpy, double2 therm) {
     const CloudDev &c = P.c;
     const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
-    const int b = (s - 1) & 1;
+    const int b = (P.mode == kModeForceOnly) ? P.fo_buf : (s - 1) & 1;
     const double xs = c.px[b][i], ys = c.py[b][i];
     const double vxs = (s == 1) ? c.vx[i] : c.vxc[i];
     const double vys = (s == 1) ? c.vy[i] : c.vyc[i];

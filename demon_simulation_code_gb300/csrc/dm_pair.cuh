@@ -200,8 +200,7 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     const int n = P.c.n;
-    const int st = (P.mode == kModeForceOnly) ? 1 : P.stage;
-    const int b = (st - 1) & 1;
+    const int b = (P.mode == kModeForceOnly) ? P.fo_buf : (P.stage - 1) & 1;
     const float4 *__restrict__ pa = P.c.pa[b];
     const float4 *__restrict__ pb = P.c.pb[b];
     int2 *my_queue = s_queue + warp * ILP * 32;
@@ -478,8 +477,7 @@ __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp64(const StageParams P
     const int tid = threadIdx.x;
     const int t = tid % NI, g = tid / NI;
     const int n = P.c.n, n_pad = P.c.n_pad;
-    const int st = (P.mode == kModeForceOnly) ? 1 : P.stage;
-    const int b = (st - 1) & 1;
+    const int b = (P.mode == kModeForceOnly) ? P.fo_buf : (P.stage - 1) & 1;
     const double *__restrict__ px = P.c.px[b];
     const double *__restrict__ py = P.c.py[b];
     const double *__restrict__ qa = P.c.q;
