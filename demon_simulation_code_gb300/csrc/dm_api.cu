@@ -1246,13 +1246,8 @@ int batch_reorder(dm_batch *B) {
     const int n = B->total;
     const int grid = (n + 255) / 256;
     SortScratch &z = B->sort;
-    const size_t half = 2 * sizeof(unsigned long long);
-    for (int c = 0; c < B->nclouds; c++) {  // one memset pair would do; keep it simple and capturable
-        (void)c;
-    }
     // min entries to all-ones, max entries to zero: bbox layout [cloud][4]
     DM_CUDA(ctx, cudaMemsetAsync(B->dbbox, 0xFF, 4 * sizeof(unsigned long long) * B->nclouds, s));
-    (void)half;
     batch_init_bbox_max<<<(B->nclouds + 127) / 128, 128, 0, s>>>(B->dbbox, B->nclouds);
     batch_bbox<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbbox);
     batch_keys<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbbox, B->mbits, z.keys[0], z.vals[0]);

@@ -11,7 +11,7 @@
 // pair pattern, all of which are defined on the caller's order).
 //
 // Sort: 24-bit Morton keys (12 bits per axis over the cloud's bounding box)
-// and a deterministic, stable LSD radix sort with 4-bit digits (per-block
+// and a deterministic, stable LSD radix sort with 8-bit digits (per-block
 // digit histograms, one scan, stable scatter ranked with __match_any_sync).
 // No atomics decide any order; the result depends only on the positions.
 #pragma once
@@ -23,7 +23,7 @@ namespace dm {
 constexpr int kSortThreads = 256;
 constexpr int kSortPerBlock = 4 * kSortThreads;  // keys per block
 constexpr int kSortBits = 24;
-constexpr int kSortDigitBits = 4;
+constexpr int kSortDigitBits = 8;  // 24-bit keys: 3 passes
 constexpr int kSortBuckets = 1 << kSortDigitBits;
 
 struct SortScratch {
