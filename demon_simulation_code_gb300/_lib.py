@@ -78,6 +78,7 @@ SIGNATURES = {
     "dm_cloud_set_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForceParams)]),
     "dm_cloud_eval_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
     "dm_cloud_eval_forces_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]),
+    "dm_cloud_evaluated_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_ulonglong)]),
     "dm_cloud_eval_forces_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                    ctypes.c_void_p]),
     "dm_cloud_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]),

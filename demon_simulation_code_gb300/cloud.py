@@ -182,6 +182,12 @@ class DeviceCloud:
     def set_reorder_interval(self, steps: int):
         self._chk(self.lib.dm_cloud_set_reorder_interval(self.h, int(steps)))
 
+    def evaluated_pairs(self) -> int:
+        """Ordered pairs the culling kernels swept so far (cumulative)."""
+        v = ctypes.c_ulonglong()
+        self._chk(self.lib.dm_cloud_evaluated_pairs(self.h, ctypes.byref(v)))
+        return int(v.value)
+
     def set_step_counter(self, step: int):
         self._chk(self.lib.dm_cloud_set_step_counter(self.h, int(step)))
 

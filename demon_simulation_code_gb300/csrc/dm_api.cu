@@ -181,6 +181,7 @@ struct Variant {
     const char *name;
     int precision;
     bool cluster;  // reduce through a thread-block cluster (else global partials + stage_finish)
+    bool cull;     // skip j groups whose box is beyond the cutoff from the tile's (group_bounds first)
     int nt;        // threads per CTA
     int tile;      // particles per i tile
     size_t smem;
@@ -188,9 +189,9 @@ struct Variant {
     cudaError_t (*launch)(const cudaLaunchConfig_t *, const StageParams &);
 };
 
-template <int NW, int ILP, int TC, bool CL>
+template <int NW, int ILP, int TC, bool CL, bool CULL>
 cudaError_t launch_fp32c(const cudaLaunchConfig_t *cfg, const StageParams &P) {
-    return cudaLaunchKernelEx(cfg, pair_stage_fp32c<NW, ILP, TC, CL>, P, exp_consts());
+    return cudaLaunchKernelEx(cfg, pair_stage_fp32c<NW, ILP, TC, CL, CULL>, P, exp_consts());
 }
 template <int NI, int G, int ILP, int JT>
 cudaError_t launch_fp64(const cudaLaunchConfig_t *cfg, const StageParams &P) {
@@ -198,9 +199,13 @@ cudaError_t launch_fp64(const cudaLaunchConfig_t *cfg, const StageParams &P) {
 }
 
 #define DM_FP32C_VARIANT(NW, ILP, TC, CL)                                                        \
-    {"fp32c<" #NW "," #ILP "," #TC "," #CL ">", DM_FP32C, CL, NW * 32, 32 * ILP,                  \
-     Fp32cSmem<NW, ILP, TC>::bytes, (const void *)pair_stage_fp32c<NW, ILP, TC, CL>,              \
-     launch_fp32c<NW, ILP, TC, CL>}
+    {"fp32c<" #NW "," #ILP "," #TC "," #CL ">", DM_FP32C, CL, false, NW * 32, 32 * ILP,           \
+     Fp32cSmem<NW, ILP, TC>::bytes, (const void *)pair_stage_fp32c<NW, ILP, TC, CL, false>,       \
+     launch_fp32c<NW, ILP, TC, CL, false>}
+#define DM_FP32C_CULL_VARIANT(NW, ILP, TC, CL)                                                   \
+    {"fp32c<" #NW "," #ILP "," #TC "," #CL ",cull>", DM_FP32C, CL, true, NW * 32, 32 * ILP,      \
+     Fp32cSmem<NW, ILP, TC>::bytes, (const void *)pair_stage_fp32c<NW, ILP, TC, CL, true>,        \
+     launch_fp32c<NW, ILP, TC, CL, true>}
 
 const Variant kVariants[] = {
     DM_FP32C_VARIANT(8, 4, 256, true),
@@ -209,7 +214,12 @@ const Variant kVariants[] = {
     DM_FP32C_VARIANT(4, 4, 256, false),
     DM_FP32C_VARIANT(16, 4, 256, false),
     DM_FP32C_VARIANT(8, 2, 256, false),
-    {"fp64<128,2,2,512>", DM_FP64, true, kNI64 * kG64, kNI64 * kILP64,
+    DM_FP32C_CULL_VARIANT(8, 4, 256, false),
+    DM_FP32C_CULL_VARIANT(4, 4, 256, false),
+    DM_FP32C_CULL_VARIANT(8, 2, 256, false),
+    DM_FP32C_CULL_VARIANT(4, 2, 128, false),
+    DM_FP32C_CULL_VARIANT(8, 4, 256, true),
+    {"fp64<128,2,2,512>", DM_FP64, true, false, kNI64 * kG64, kNI64 * kILP64,
      Fp64Smem<kNI64, kG64, kILP64>::bytes(kJT64),
      (const void *)pair_stage_fp64<kNI64, kG64, kILP64, kJT64>, launch_fp64<kNI64, kG64, kILP64, kJT64>},
 };
@@ -320,6 +330,12 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
     const int ntiles = (c->n + k.tile - 1) / k.tile;
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = make_cfg(ctx, k, ntiles, S, attr);
+    if (k.cull) {  // boxes of the buffer this stage reads
+        const int br = (mode == kModeForceOnly) ? c->fo_buf : (stage - 1) & 1;
+        group_bounds<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d, br);
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches++;
+    }
     DM_CUDA(ctx, k.launch(&cfg, P));
     ctx->launches++;
     if (!k.cluster) {
@@ -760,7 +776,8 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     const size_t ni = align256((size_t)c->n_pad * sizeof(int));
     c->sort_blocks = (n + kSortPerBlock - 1) / kSortPerBlock;
     const size_t nh = align256((size_t)kSortBuckets * c->sort_blocks * sizeof(uint32_t));
-    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ni * 6 + nh + 1024 + 256;
+    const size_t ngb = align256((size_t)(c->n_pad / 32) * sizeof(float4));
+    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ngb * 2 + ni * 6 + nh + 1024 + 512;
     cudaError_t e = cudaMalloc(&c->block, total);
     if (e != cudaSuccess) {
         delete c;
@@ -780,6 +797,8 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->d_fx = takeD();
     c->d_fy = takeD();
     for (int b = 0; b < 2; b++) { c->d.pa[b] = takeF4(); c->d.pb[b] = takeF4(); }
+    for (int b = 0; b < 2; b++) { c->d.gbox[b] = (float4 *)p; p += ngb; }
+    c->d.eval_pairs = (unsigned long long *)p; p += 256;
     c->d.step_ctr = (unsigned long long *)p; p += 256;
     c->d.err = (int *)p; p += 256;
     c->d_dt = (double *)p; p += 256;
@@ -921,6 +940,10 @@ int dm_cloud_eval_forces_device(dm_cloud *c, int precision, double *d_fx, double
     if (precision != DM_FP64 && precision != DM_FP32C)
         return ctx->fail(DM_ERR_ARG, "bad precision %d", precision);
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (c->order_dirty) {  // spatial order first (internal only: outputs are in the caller's order)
+        const int rc = reorder(c);
+        if (rc) return rc;
+    }
     int rc = launch_stage(c, precision, 1, kModeForceOnly, 0.0, nullptr);
     if (rc) return rc;
     const size_t bytes = (size_t)c->n * sizeof(double);
@@ -938,6 +961,16 @@ int dm_cloud_eval_forces(dm_cloud *c, int precision, double *fx, double *fy) {
     const size_t bytes = (size_t)c->n * sizeof(double);
     DM_CUDA(ctx, cudaMemcpyAsync(fx, c->d_fx, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     DM_CUDA(ctx, cudaMemcpyAsync(fy, c->d_fy, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DM_OK;
+}
+
+int dm_cloud_evaluated_pairs(dm_cloud *c, unsigned long long *pairs) {
+    if (!c || !pairs) return c ? c->ctx->fail(DM_ERR_ARG, "dm_cloud_evaluated_pairs: NULL") : DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    DM_CUDA(ctx, cudaMemcpyAsync(pairs, c->d.eval_pairs, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
     DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DM_OK;
 }

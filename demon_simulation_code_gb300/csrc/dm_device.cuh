@@ -47,6 +47,8 @@ struct CloudDev {
     double *a23[4];
     double *px[2], *py[2];
     float4 *pa[2], *pb[2];
+    float4 *gbox[2];               // [n_pad/32] FP32 box (x0, y0, x1, y1) of each 32-particle group
+    unsigned long long *eval_pairs;  // ordered pairs the culling kernels swept (cumulative)
     unsigned long long *step_ctr;  // [2], see stage_step_index()
     int *err;                      // device error flags
     double rc2;                    // (10/kappa)^2 of the current force parameters

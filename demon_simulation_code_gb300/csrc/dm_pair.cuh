@@ -107,10 +107,26 @@ struct Fp32cSmem {
     static constexpr size_t queue = (size_t)NW * ILP * 32 * sizeof(int2);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
-    static constexpr size_t bytes = tile + cold + queue + acc + red;
+    static constexpr size_t glist = (size_t)NW * 32 * sizeof(int) + NW * sizeof(int);  // culling
+    static constexpr size_t bytes = tile + cold + queue + acc + red + glist;
     // s_red, in float4 units from the start of shared memory
     static constexpr size_t red_offset = (tile + cold + queue + acc) / sizeof(float4);
 };
+
+// Conservative FP32 test: can any point of box a come within the cutoff of
+// any point of box b?  Boxes are (x0, y0, x1, y1) of FP32 hi parts; the true
+// positions lie within an ulp of them and the box arithmetic rounds, so the
+// gaps are shrunk by 2^-20 of the largest coordinate before comparing with
+// r_c^2 (already rounded up, rc2_hi).
+__device__ __forceinline__ bool boxes_near(const float4 &a, const float4 &b, float rc2_hi) {
+    const float gx = fmaxf(a.x - b.z, b.x - a.z);
+    const float gy = fmaxf(a.y - b.w, b.y - a.w);
+    const float big = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.z)), fmaxf(fabsf(b.x), fabsf(b.z))),
+                            fmaxf(fmaxf(fabsf(a.y), fabsf(a.w)), fmaxf(fabsf(b.y), fabsf(b.w))));
+    const float m = 9.5367431640625e-7f * big;  // 2^-20
+    const float dx = fmaxf(0.0f, gx - m), dy = fmaxf(0.0f, gy - m);
+    return !(fmaf(dx, dx, dy * dy) >= rc2_hi);  // NaN: near (never drops a pair)
+}
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
 // column r (bit c = bit r of row c) on exit.
@@ -182,7 +198,7 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
 // the block synchronised.  `P` may live in shared memory (batched kernel).
 // Particles are those of P.c (n = P.c.n); j at or beyond n read as padding,
 // so a cloud needs no padding of its own.
-template <int NW, int ILP, int TC>
+template <int NW, int ILP, int TC, bool CULL = false>
 __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConsts &E, int tile,
                                             int rank, int S, unsigned char *smem_raw) {
     constexpr int NT = NW * 32;
@@ -196,6 +212,8 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
     int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * 32);           // [NW][ILP][32]
     float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);    // [NW][ILP][32]
     float4 *s_red = s_acc + NW * ILP * 32;                                 // [TILE]
+    int *s_glist = reinterpret_cast<int *>(s_red + TILE);                  // [NT] surviving groups
+    int *s_wcount = s_glist + NT;                                          // [NW]
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
@@ -230,11 +248,6 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         my_acc[k * 32 + lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 
-    // j chunks (4 consecutive j) are dealt round-robin: chunk c belongs to
-    // rank c % S and, within this CTA, to warp (c / S) % NW.  Every warp thus
-    // samples the whole cloud evenly, whatever the spatial order.
-    const int nch_all = (n + 3) >> 2;
-    const int my_nch = (nch_all - rank + S - 1) / S;  // chunks of this rank
     uint32_t qn = 0u;  // queue fill per slot, 8 bits per slot (warp-uniform)
 
     // Run the precise path on the queued entries of slot K, then empty it.
@@ -294,12 +307,15 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         }
     };
 
-    __syncthreads();  // s_cold complete
-    for (int q0 = 0; q0 < my_nch; q0 += TC) {
-        const int tcn = min(TC, my_nch - q0);
+    // Sweeps the `count` chunks (4 consecutive j) of this CTA's list through
+    // shared-memory tiles; chunk_of(q) is the cloud chunk index of entry q.
+    // Within a tile, chunk c goes to warp c % NW.
+    auto sweep = [&](int count, auto chunk_of) {
+    for (int q0 = 0; q0 < count; q0 += TC) {
+        const int tcn = min(TC, count - q0);
         __syncthreads();
         for (int e = tid; e < tcn; e += NT) {
-            const int jb = 4 * ((q0 + e) * S + rank);  // first j of the chunk
+            const int jb = 4 * chunk_of(q0 + e);  // first j of the chunk
             float xs[4], ys[4], bs[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
@@ -365,6 +381,50 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         // queued entries index into this tile: drain before it is overwritten
         flush_slots(1);
     }
+    };
+
+    __syncthreads();  // s_cold complete
+    if constexpr (!CULL) {
+        // chunks dealt round-robin: chunk c belongs to rank c % S, so every
+        // rank (and every warp) samples the whole cloud evenly
+        const int nch_all = (n + 3) >> 2;
+        const int my_nch = (nch_all - rank + S - 1) / S;  // chunks of this rank
+        sweep(my_nch, [&](int q) { return q * S + rank; });
+    } else {
+        // 32-particle groups dealt round-robin to ranks; a group whose box is
+        // beyond the cutoff from the tile's box is skipped whole (it holds no
+        // pair the reference counts).  The survivors keep their order.
+        const float4 *__restrict__ gb = P.c.gbox[b];
+        float4 tb = gb[tile * ILP];
+#pragma unroll
+        for (int k = 1; k < ILP; k++) {
+            const float4 v = gb[tile * ILP + k];
+            tb = make_float4(fminf(tb.x, v.x), fminf(tb.y, v.y), fmaxf(tb.z, v.z), fmaxf(tb.w, v.w));
+        }
+        const int ngroups = (n + 31) >> 5;
+        const int my_ng = (ngroups - rank + S - 1) / S;
+        unsigned long long swept = 0ull;
+        for (int t0 = 0; t0 < my_ng; t0 += NT) {
+            const int t = t0 + tid;
+            const int g = t * S + rank;
+            const bool keep = (t < my_ng) && boxes_near(tb, gb[g], P.rc2_hi);
+            const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) s_wcount[warp] = __popc(bal);
+            __syncthreads();
+            int off = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                const int cw = s_wcount[w];
+                off += (w < warp) ? cw : 0;
+                total += cw;
+            }
+            if (keep) s_glist[off + __popc(bal & ((1u << lane) - 1u))] = g;
+            sweep(8 * total, [&](int q) { return 8 * s_glist[q >> 3] + (q & 7); });
+            swept += (unsigned long long)total;
+            __syncthreads();  // s_glist, s_wcount reused by the next batch
+        }
+        if (tid == 0 && swept) atomicAdd(P.c.eval_pairs, swept * 32ull * (unsigned long long)TILE);
+    }
 
     // combine the NW warps in fixed order with a compensated FP32 sum (each
     // warp's Kahan pair (s, c) stands for s - c); FP64 comes later, once per
@@ -389,7 +449,7 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
 // through distributed shared memory and run the stage epilogue in the same
 // launch.  CL = false: plain blocks; each writes its partial sums to global
 // memory and stage_finish (below) completes the stage.
-template <int NW, int ILP, int TC, bool CL>
+template <int NW, int ILP, int TC, bool CL, bool CULL = false>
 __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     pair_stage_fp32c(const StageParams P, const ExpConsts E) {
     constexpr int TILE = 32 * ILP;
@@ -399,7 +459,7 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
     const int n = P.c.n, n_pad = P.c.n_pad;
-    fp32c_sweep<NW, ILP, TC>(P, E, tile, rank, S, smem_raw);
+    fp32c_sweep<NW, ILP, TC, CULL>(P, E, tile, rank, S, smem_raw);
     float4 *s_red = reinterpret_cast<float4 *>(smem_raw) + Fp32cSmem<NW, ILP, TC>::red_offset;
     if constexpr (!CL) {
         for (int e = tid; e < TILE; e += NW * 32)

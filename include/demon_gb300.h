@@ -222,6 +222,13 @@ int dm_cloud_set_kernel(dm_cloud *cloud, const char *variant, int split);
  * power of two <= 16).  No reference counterpart. */
 int dm_cloud_set_reorder_interval(dm_cloud *cloud, int steps);
 
+/* Ordered pairs the culling kernel variants actually swept so far (32-
+ * particle j groups within reach of an i tile's box, times the tile), the
+ * rest having been skipped by the box test; 0 while no culling variant has
+ * run.  Work counter for reports: the pair-interaction metric counts all
+ * N(N-1) ordered pairs per force evaluation either way.  No reference
+ * counterpart (the reference tests every pair). */
+int dm_cloud_evaluated_pairs(dm_cloud *cloud, unsigned long long *pairs);
 /* RNG step counter used by ThermalForce (advanced by one per RK4 step). */
 int dm_cloud_set_step_counter(dm_cloud *cloud, uint64_t step);
 int dm_cloud_get_step_counter(dm_cloud *cloud, uint64_t *step);

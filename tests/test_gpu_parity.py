@@ -390,3 +390,35 @@ def test_square256k_step_fp32c_tracks_fp64(gpu_ctx):
     assert err <= 1e-5 * disp
     vmax = max(np.abs(vx64).max(), np.abs(vy64).max())
     assert max(np.abs(vx - vx64).max(), np.abs(vy - vy64).max()) <= 1e-5 * vmax
+
+
+@pytest.mark.parametrize("name", ["fp32c<8,4,256,false,cull>", "fp32c<8,4,256,true,cull>"])
+def test_culled_variants_keep_every_pair_and_skip_far_groups(gpu_ctx, oracle_lib, name):
+    """Box culling skips whole 32-particle j groups out of reach of an i
+    tile; every pair inside the cutoff must still be counted (forces match
+    the oracle) while most of a sparse cloud's pairs are never swept."""
+    c0 = W.disk16k(thermal=False).clouds[0]
+    c = coulomb_cloud(gpu_ctx, c0.x, c0.y, c0.q, 2e4)
+    c.set_kernel(name, 0)
+    e0 = c.evaluated_pairs()
+    fx, fy = c.eval_forces("fp32c")
+    swept = c.evaluated_pairs() - e0
+    rx, ry = oracle_lib.shielded_coulomb(c0.x, c0.y, c0.q, 2e4, nthreads=8)
+    err = e_F(fx, fy, rx, ry)
+    print(f"{name}: e_F = {err:.3e}, swept {swept / c0.n**2:.4f} of all pairs")
+    assert err <= TOL["fp32c"]
+    assert 0 < swept < 0.1 * c0.n * c0.n
+
+
+def test_culled_square256k_vs_fp64_all_rows(gpu_ctx, square256k_forces):
+    c0, out = square256k_forces
+    c = coulomb_cloud(gpu_ctx, c0.x, c0.y, c0.q, c0.shielding)
+    c.set_kernel("fp32c<8,4,256,false,cull>", 0)
+    fx, fy = c.eval_forces("fp32c")
+    swept = c.evaluated_pairs()
+    c.close()
+    rx, ry = out["fp64"]
+    err = e_F(fx, fy, rx, ry)
+    print(f"square256k culled: e_F vs fp64 = {err:.3e}, swept {swept / c0.n**2:.2e} of all pairs")
+    assert err <= TOL["fp32c"]
+    assert swept < 0.01 * c0.n * c0.n
