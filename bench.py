@@ -271,9 +271,12 @@ def run_gb300(args, world, rank, local):
     barrier()
     torch.cuda.synchronize()
     l0 = ctx.launch_count()
+    ev0 = cloud.evaluated_pairs()
     with ClockSampler(local) as clk:
         elapsed = timed_steps(args.precision, args.steps)
     launches_timed = ctx.launch_count() - l0
+    # ordered pairs the culling kernel swept (0: no culling variant ran, every pair was swept)
+    swept = cloud.evaluated_pairs() - ev0
     pair_ms, launches, pairs_prof = ctx.profile_read()
     main_step_ms = list(step_ms)
     ctx.profile(False)
@@ -333,6 +336,7 @@ def run_gb300(args, world, rank, local):
     avg_launch_s = pair_ms / 1e3 / max(launches, 1)
     achieved = FLOPS_PER_PAIR * n * (n - 1) / avg_launch_s / 1e12
     kname = "pair_stage_fp32c" if args.precision == "fp32c" else "pair_stage_fp64"
+    swept_frac = swept / (pairs_step * args.steps) if swept > 0 else 1.0
     traffic = traffic_from_profiles(kname, w.name)
 
     # batched workload (256 clouds of uneven N, one persistent launch per stage)
@@ -434,6 +438,11 @@ def run_gb300(args, world, rank, local):
                          "traffic": traffic,
                          "flops_per_pair": FLOPS_PER_PAIR,
                          "avg_launch_us": avg_launch_s * 1e6,
+                         # box culling skips pair groups out of reach: the work the
+                         # kernel actually swept, and the pipe fraction on that work
+                         "swept_pair_fraction": swept_frac,
+                         "achieved_on_swept": achieved * swept_frac,
+                         "frac_on_swept": achieved * swept_frac / peak,
                          "peak_source": "in-run FP32 FMA probe (dm_probe_peak); "
                                         "MEASURED_PEAKS.json has no FP32 figure"},
             "batch": batch,
