@@ -356,11 +356,13 @@ def run_gb300(args, world, rank, local):
         b = torch.cuda.Event(enable_timing=True)
         barrier()
         torch.cuda.synchronize()
+        ev0 = bt.evaluated_pairs()
         a.record(stream)
         bt.step(args.batch_steps, wb.dt)
         b.record(stream)
         torch.cuda.synchronize()
         el = a.elapsed_time(b) / 1e3
+        bswept = bt.evaluated_pairs() - ev0
         if world > 1:
             import torch.distributed as dist
 
@@ -372,6 +374,9 @@ def run_gb300(args, world, rank, local):
                  "unit": UNIT, "steps": args.batch_steps, "ms_per_step": el / args.batch_steps * 1e3,
                  "variant": name, "work_items": nitems, "persistent_grid": grid,
                  "graph_captured": args.batch_steps >= 16,
+                 "swept_pair_fraction": (bswept / (4.0 * sum(wb.clouds[c].n * (wb.clouds[c].n - 1)
+                                                              for c in parts[rank]) * args.batch_steps)
+                                         if bswept > 0 else 1.0),
                  "sharding": {"ranks": world, "clouds_per_rank": [len(p) for p in parts],
                               "imbalance": imbalance([c.n for c in wb.clouds], parts),
                               "scaling": "strong"}}

@@ -79,6 +79,9 @@ SIGNATURES = {
     "dm_cloud_eval_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
     "dm_cloud_eval_forces_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "dm_cloud_evaluated_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "dm_batch_evaluated_pairs": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "dm_batch_variants": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "dm_batch_set_kernel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "dm_cloud_eval_forces_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                    ctypes.c_void_p]),
     "dm_cloud_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp]),
@@ -139,6 +142,12 @@ def last_error(ctx) -> str:
 def check(rc: int, ctx=None) -> None:
     if rc != DM_OK:
         raise DemonError(rc, last_error(ctx))
+
+
+def batch_variants() -> list[str]:
+    buf = ctypes.create_string_buffer(4096)
+    check(load().dm_batch_variants(buf, len(buf)))
+    return buf.value.decode().split(";")
 
 
 def kernel_variants() -> list[str]:

@@ -243,6 +243,16 @@ class DeviceBatch:
         """Splits a concatenated array into per-cloud arrays."""
         return np.split(arr, np.cumsum(self.ns)[:-1])
 
+    def set_kernel(self, variant: str):
+        """Pins a batch kernel variant (names: _lib.batch_variants())."""
+        check(self.lib.dm_batch_set_kernel(self.h, variant.encode()), self.ctx.h)
+
+    def evaluated_pairs(self) -> int:
+        """Ordered pairs the culling kernels swept so far (cumulative)."""
+        v = ctypes.c_ulonglong()
+        check(self.lib.dm_batch_evaluated_pairs(self.h, ctypes.byref(v)), self.ctx.h)
+        return int(v.value)
+
     def info(self):
         buf = ctypes.create_string_buffer(128)
         ni = ctypes.c_int()

@@ -1186,6 +1186,7 @@ namespace {
 
 struct BatchVariant {
     const char *name;
+    bool cull;
     int nt, tile;
     size_t smem;
     const void *fn;
@@ -1193,22 +1194,26 @@ struct BatchVariant {
                           const int2 *, int, unsigned int *);
 };
 
-template <int NW, int ILP, int TC>
+template <int NW, int ILP, int TC, bool CULL>
 cudaError_t launch_batch(dim3 g, dim3 b, size_t smem, cudaStream_t s, const StageParams &P,
                          const BatchCloud *desc, const int2 *items, int nitems, unsigned int *ctr) {
-    batch_stage_fp32c<NW, ILP, TC><<<g, b, smem, s>>>(P, desc, items, nitems, ctr, exp_consts());
+    batch_stage_fp32c<NW, ILP, TC, CULL><<<g, b, smem, s>>>(P, desc, items, nitems, ctr, exp_consts());
     return cudaGetLastError();
 }
 
-#define DM_BATCH_VARIANT(NW, ILP, TC)                                                            \
-    {"batch_fp32c<" #NW "," #ILP "," #TC ">", NW * 32, 32 * ILP, Fp32cSmem<NW, ILP, TC>::bytes,  \
-     (const void *)batch_stage_fp32c<NW, ILP, TC>, launch_batch<NW, ILP, TC>}
+#define DM_BATCH_VARIANT(NW, ILP, TC, CULL, SUFFIX)                                                \
+    {"batch_fp32c<" #NW "," #ILP "," #TC SUFFIX ">", CULL, NW * 32, 32 * ILP,                      \
+     Fp32cSmem<NW, ILP, TC>::bytes, (const void *)batch_stage_fp32c<NW, ILP, TC, CULL>,            \
+     launch_batch<NW, ILP, TC, CULL>}
 
 const BatchVariant kBatchVariants[] = {
-    DM_BATCH_VARIANT(8, 4, 256),
-    DM_BATCH_VARIANT(4, 4, 256),
-    DM_BATCH_VARIANT(8, 2, 256),
-    DM_BATCH_VARIANT(4, 2, 128),
+    DM_BATCH_VARIANT(8, 4, 256, false, ""),
+    DM_BATCH_VARIANT(4, 4, 256, false, ""),
+    DM_BATCH_VARIANT(8, 2, 256, false, ""),
+    DM_BATCH_VARIANT(4, 2, 128, false, ""),
+    DM_BATCH_VARIANT(8, 4, 256, true, ",cull"),
+    DM_BATCH_VARIANT(4, 2, 128, true, ",cull"),
+    DM_BATCH_VARIANT(8, 2, 256, true, ",cull"),
 };
 constexpr int kNumBatchVariants = (int)(sizeof(kBatchVariants) / sizeof(kBatchVariants[0]));
 
@@ -1232,6 +1237,8 @@ struct dm_batch {
     int sort_blocks = 0;
     int mbits = 24;
     double *d_fx = nullptr, *d_fy = nullptr;
+    int ngroups = 0;            // 32-particle groups over all clouds
+    int *dgseg = nullptr;       // [ngroups] cloud of each group
     int variant = -1;
     int reorder_interval = 4;
     bool order_dirty = true;
@@ -1267,6 +1274,13 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf =
     P.fx_out = B->d_fx;
     P.fy_out = B->d_fy;
     const int slot = (mode == kModeForceOnly) ? 0 : stage - 1;
+    if (k.cull) {  // group boxes of the buffer this stage reads
+        const int br = (mode == kModeForceOnly) ? fo_buf : (stage - 1) & 1;
+        batch_group_bounds<<<(B->ngroups * 32 + 255) / 256, 256, 0, ctx->stream>>>(B->d, B->ddesc, B->dgseg,
+                                                                                    B->ngroups, br);
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches++;
+    }
     DM_CUDA(ctx, k.launch(dim3(B->grid[B->variant]), dim3(k.nt), k.smem, ctx->stream, P, B->ddesc,
                           B->ditems[B->variant], B->nitems[B->variant], B->dcounter + slot));
     ctx->launches++;
@@ -1469,13 +1483,15 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     B->dcounter = (unsigned int *)p; p += 256;
     // host descriptors
     B->hdesc.resize(nclouds);
-    std::vector<int> seg((size_t)B->total), orig((size_t)B->total);
+    std::vector<int> seg((size_t)B->total), orig((size_t)B->total), gseg;
     int off = 0;
     for (int c = 0; c < nclouds; c++) {
         BatchCloud &bc = B->hdesc[c];
         bc.off = off;
         bc.n = n[c];
-        bc.pad_ = 0;
+        bc.goff = B->ngroups;
+        for (int g = 0; g < (n[c] + 31) / 32; g++) gseg.push_back(c);
+        B->ngroups += (n[c] + 31) / 32;
         std::memcpy(&bc.f, &params[c], sizeof(ForceParams));
         const double kappa = params[c].shielding;
         bc.rc2 = (kappa > 0.0) ? (10.0 / kappa) * (10.0 / kappa) : 0.0;
@@ -1489,8 +1505,20 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
         off += n[c];
     }
     cudaStream_t s = ctx->stream;
+    // group boxes (culling kernels), the group -> cloud map, the swept-pair counter
+    for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+        e = cudaMalloc((void **)&d.gbox[b], (size_t)B->ngroups * sizeof(float4));
+        if (e == cudaSuccess) B->extra.push_back(d.gbox[b]);
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void **)&B->dgseg, gseg.size() * sizeof(int));
+    if (e == cudaSuccess) B->extra.push_back(B->dgseg);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d.eval_pairs, sizeof(unsigned long long));
+    if (e == cudaSuccess) B->extra.push_back(d.eval_pairs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.eval_pairs, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(B->dgseg, gseg.data(), gseg.size() * sizeof(int), cudaMemcpyHostToDevice, s);
     const size_t bt = (size_t)B->total * sizeof(double);
-    e = cudaMemsetAsync(B->block, 0, bytes_total, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B->block, 0, bytes_total, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d.x, x, bt, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d.y, y, bt, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d.vx, vx, bt, cudaMemcpyHostToDevice, s);
@@ -1615,6 +1643,38 @@ int dm_batch_download(dm_batch *B, double *x, double *y, double *vx, double *vy)
         cudaMemset(B->d.err, 0, sizeof(int));
         return ctx->fail(DM_ERR_NUMERIC, "non-finite particle position in the batch");
     }
+    return DM_OK;
+}
+
+int dm_batch_variants(char *buf, size_t len) {
+    if (!buf || len == 0) return DM_ERR_ARG;
+    std::string out;
+    for (int v = 0; v < kNumBatchVariants; v++) {
+        if (v) out += ";";
+        out += kBatchVariants[v].name;
+    }
+    snprintf(buf, len, "%s", out.c_str());
+    return out.size() < len ? DM_OK : DM_ERR_ARG;
+}
+
+int dm_batch_set_kernel(dm_batch *B, const char *variant) {
+    if (!B || !variant) return B ? B->ctx->fail(DM_ERR_ARG, "dm_batch_set_kernel: NULL") : DM_ERR_ARG;
+    for (int v = 0; v < kNumBatchVariants; v++)
+        if (std::strcmp(kBatchVariants[v].name, variant) == 0) {
+            B->variant = v;
+            B->drop_graphs();
+            return DM_OK;
+        }
+    return B->ctx->fail(DM_ERR_ARG, "dm_batch_set_kernel: unknown variant '%s'", variant);
+}
+
+int dm_batch_evaluated_pairs(dm_batch *B, unsigned long long *pairs) {
+    if (!B || !pairs) return B ? B->ctx->fail(DM_ERR_ARG, "dm_batch_evaluated_pairs: NULL") : DM_ERR_ARG;
+    dm_ctx *ctx = B->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    DM_CUDA(ctx, cudaMemcpyAsync(pairs, B->d.eval_pairs, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return DM_OK;
 }
 

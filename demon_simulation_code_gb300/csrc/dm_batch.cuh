@@ -20,7 +20,7 @@ namespace dm {
 struct BatchCloud {
     int off;        // first particle in the concatenated arrays
     int n;
-    int pad_;
+    int goff;       // first of the cloud's 32-particle groups in the batch's group boxes
     ForceParams f;
     double rc2;
     float rc2_lo, rc2_hi, kappa_f;
@@ -34,7 +34,10 @@ __device__ __forceinline__ void batch_view(StageParams &V, const StageParams &P0
     c.x += o; c.y += o; c.vx += o; c.vy += o; c.q += o; c.m += o;
     c.vxc += o; c.vyc += o;
     for (int k = 0; k < 4; k++) { c.a1[k] += o; c.a23[k] += o; }
-    for (int b = 0; b < 2; b++) { c.px[b] += o; c.py[b] += o; c.pa[b] += o; c.pb[b] += o; }
+    for (int b = 0; b < 2; b++) {
+        c.px[b] += o; c.py[b] += o; c.pa[b] += o; c.pb[b] += o;
+        c.gbox[b] += d.goff;  // group boxes numbered within the cloud
+    }
     c.orig += o;  // values stay global caller indices (thermal counter, outputs)
     c.n = d.n;
     c.n_pad = d.n;
@@ -46,7 +49,7 @@ __device__ __forceinline__ void batch_view(StageParams &V, const StageParams &P0
     V.kappa_f = d.kappa_f;
 }
 
-template <int NW, int ILP, int TC>
+template <int NW, int ILP, int TC, bool CULL = false>
 __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     batch_stage_fp32c(const StageParams P0, const BatchCloud *__restrict__ desc,
                       const int2 *__restrict__ items, int nitems, unsigned int *counter,
@@ -66,7 +69,7 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
         if (tid == 0) batch_view(sV, P0, desc[w.x]);
         __syncthreads();
         const int tile = w.y;
-        fp32c_sweep<NW, ILP, TC>(sV, E, tile, 0, 1, smem_raw);
+        fp32c_sweep<NW, ILP, TC, CULL>(sV, E, tile, 0, 1, smem_raw);
         if (tid < TILE) {
             const int i = tile * TILE + tid;
             if (i < sV.c.n) {
@@ -78,6 +81,31 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
         __syncthreads();  // before the next item reuses shared memory
     }
     stage_step_advance(P0);
+}
+
+// Box of every cloud's 32-particle groups in stage buffer b (one warp per
+// group; gseg[w] is group w's cloud; a cloud's last group may be partial).
+static __global__ void batch_group_bounds(CloudDev c, const BatchCloud *__restrict__ desc,
+                                          const int *__restrict__ gseg, int ngroups, int b) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= ngroups) return;  // whole warp
+    const BatchCloud d = desc[gseg[w]];
+    const int li = 32 * (w - d.goff) + lane;
+    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+    if (li < d.n) {
+        const float4 A = c.pa[b][d.off + li];
+        x0 = x1 = A.x;
+        y0 = y1 = A.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if (lane == 0) c.gbox[b][w] = make_float4(x0, y0, x1, y1);
 }
 
 // --- per-cloud Morton order ------------------------------------------------

@@ -395,13 +395,15 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         // beyond the cutoff from the tile's box is skipped whole (it holds no
         // pair the reference counts).  The survivors keep their order.
         const float4 *__restrict__ gb = P.c.gbox[b];
+        const int ngroups = (n + 31) >> 5;
         float4 tb = gb[tile * ILP];
 #pragma unroll
         for (int k = 1; k < ILP; k++) {
-            const float4 v = gb[tile * ILP + k];
-            tb = make_float4(fminf(tb.x, v.x), fminf(tb.y, v.y), fmaxf(tb.z, v.z), fmaxf(tb.w, v.w));
+            if (tile * ILP + k < ngroups) {  // a cloud's last tile may hold fewer groups
+                const float4 v = gb[tile * ILP + k];
+                tb = make_float4(fminf(tb.x, v.x), fminf(tb.y, v.y), fmaxf(tb.z, v.z), fmaxf(tb.w, v.w));
+            }
         }
-        const int ngroups = (n + 31) >> 5;
         const int my_ng = (ngroups - rank + S - 1) / S;
         unsigned long long swept = 0ull;
         for (int t0 = 0; t0 < my_ng; t0 += NT) {

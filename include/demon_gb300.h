@@ -252,6 +252,13 @@ int dm_batch_step(dm_batch *batch, int nsteps, double dt, int precision);
 /* All forces of every cloud at the current state (caller order). */
 int dm_batch_eval_forces(dm_batch *batch, int precision, double *fx, double *fy);
 int dm_batch_download(dm_batch *batch, double *x, double *y, double *vx, double *vy);
+/* Names of the compiled batch kernel variants, ';'-separated, and pinning
+ * one (instead of the autotuner's choice). */
+int dm_batch_variants(char *buf, size_t len);
+int dm_batch_set_kernel(dm_batch *batch, const char *variant);
+/* Ordered pairs the batch's culling kernel variants swept so far (see
+ * dm_cloud_evaluated_pairs). */
+int dm_batch_evaluated_pairs(dm_batch *batch, unsigned long long *pairs);
 /* The autotuned kernel variant, work-item count and persistent grid size. */
 int dm_batch_info(dm_batch *batch, char *variant, size_t len, int *nitems, int *grid);
 int dm_batch_set_step_counter(dm_batch *batch, uint64_t step);

@@ -28,6 +28,30 @@ def test_batch_forces_vs_oracle_per_cloud(gpu_ctx, oracle_lib):
             assert e_F(gx, gy, rx, ry) <= 1e-6, c.n
 
 
+def test_every_batch_variant_matches_the_oracle(gpu_ctx, oracle_lib):
+    """Each batch variant (culling ones included) on clouds that are sparse
+    enough for the box test to skip groups."""
+    from demon_simulation_code_gb300 import _lib
+
+    clouds = W.batch256(seed=7, nclouds=10, nmin=30, nmax=3000).clouds
+    refs = [oracle_lib.forces(c.x, c.y, c.vx, c.vy, c.q, c.m, oracle.make_params(**c.params())) for c in clouds]
+    total = sum(c.n * c.n for c in clouds)
+    for name in _lib.batch_variants():
+        b = DeviceBatch(gpu_ctx, clouds)  # a fresh state per variant (the check steps it)
+        b.set_kernel(name)
+        e0 = b.evaluated_pairs()
+        fx, fy = b.eval_forces("fp32c")
+        swept = b.evaluated_pairs() - e0
+        for c, gx, gy, (rx, ry) in zip(clouds, b.split(fx), b.split(fy), refs):
+            assert e_F(gx, gy, rx, ry) <= 1e-6, (name, c.n)
+        if name.endswith(",cull>"):
+            print(name, "swept", swept / total)
+            assert 0 < swept < total
+        b.step(2, 1e-4)
+        assert np.all(np.isfinite(b.download()[0]))
+        b.close()
+
+
 def test_batch_steps_match_single_cloud_steps(gpu_ctx):
     """Each cloud of a batch integrates like the same cloud stepped alone."""
     # well-conditioned clouds (minimum separation), uneven sizes and kappa
