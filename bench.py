@@ -337,7 +337,7 @@ def run_gb300(args, world, rank, local):
     achieved = FLOPS_PER_PAIR * n * (n - 1) / avg_launch_s / 1e12
     kname = "pair_stage_fp32c" if args.precision == "fp32c" else "pair_stage_fp64"
     swept_frac = swept / (pairs_step * args.steps) if swept > 0 else 1.0
-    traffic = traffic_from_profiles(kname, w.name)
+    traffic = traffic_from_profiles(kname + ("_cull" if "cull" in tuned[0] else ""), w.name)
 
     # batched workload (256 clouds of uneven N, one persistent launch per stage)
     batch = None

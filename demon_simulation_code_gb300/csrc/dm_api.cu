@@ -86,6 +86,7 @@ struct dm_cloud {
     float *d_dmin = nullptr;
     int eval_thermal_stage = 1;  // substep of the thermal kicks in force-only evaluations
     int fo_buf = 0;              // stage buffer force-only launches read (the autotuner's dense copy: 1)
+    bool boxes_valid[2] = {false, false};  // group boxes (culling) match stage buffer b
     int split[2] = {0, 0};  // cluster size per precision (0 = not chosen yet)
     int tuned_variant[2] = {-1, -1};  // per precision: index into kVariants
     float4 *partial = nullptr;         // [partial_cap][n_pad] non-cluster partial sums
@@ -330,19 +331,23 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
     const int ntiles = (c->n + k.tile - 1) / k.tile;
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = make_cfg(ctx, k, ntiles, S, attr);
-    if (k.cull) {  // boxes of the buffer this stage reads
-        const int br = (mode == kModeForceOnly) ? c->fo_buf : (stage - 1) & 1;
+    const int br = (mode == kModeForceOnly) ? c->fo_buf : (stage - 1) & 1;  // buffer read
+    if (k.cull && !c->boxes_valid[br]) {  // boxes of the buffer this stage reads
         group_bounds<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d, br);
         DM_CUDA(ctx, cudaGetLastError());
         ctx->launches++;
+        c->boxes_valid[br] = true;
     }
     DM_CUDA(ctx, k.launch(&cfg, P));
     ctx->launches++;
     if (!k.cluster) {
-        stage_finish<<<(c->n + 127) / 128, 128, 0, ctx->stream>>>(P);
+        // stage_finish also writes the group boxes of the buffer the stage writes
+        P.box_out = (mode != kModeForceOnly) ? 1 : 0;
+        stage_finish<<<(c->n + 63) / 64, 64, 0, ctx->stream>>>(P);
         DM_CUDA(ctx, cudaGetLastError());
         ctx->launches++;
     }
+    if (mode != kModeForceOnly) c->boxes_valid[stage & 1] = !k.cluster;
     return DM_OK;
 }
 
@@ -431,6 +436,7 @@ int tune_precision(dm_cloud *c, int precision) {
             const double half = 0.5 * std::max(v[2] - v[0], v[3] - v[1]);
             const double lam = 1.8 * std::sqrt(c->d.rc2) / half;
             if (std::isfinite(half) && half > 0.0 && lam < 0.9) {
+                c->boxes_valid[1] = false;
                 tune_compress<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->d, 0.5 * (v[0] + v[2]),
                                                                             0.5 * (v[1] + v[3]), lam);
                 DM_CUDA(ctx, cudaGetLastError());
@@ -536,6 +542,7 @@ int reorder(dm_cloud *c) {
     permute_gather<<<grid, 256, 0, s>>>(c->d, z.vals[cur], z);
     permute_commit<<<grid, 256, 0, s>>>(c->d, z);
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
+    c->boxes_valid[0] = c->boxes_valid[1] = false;
     DM_CUDA(ctx, cudaGetLastError());
     ctx->launches += 5 + 3 * (kSortBits / kSortDigitBits);
     c->order_dirty = false;
@@ -825,6 +832,7 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     if (e == cudaSuccess) {
         set_identity<<<(n + 255) / 256, 256, 0, s>>>(c->d.orig, n);
         init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
+        c->boxes_valid[0] = c->boxes_valid[1] = false;
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -872,6 +880,7 @@ int dm_cloud_upload(dm_cloud *c, const double *x, const double *y, const double 
     if (rc) return rc;
     set_identity<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->d.orig, c->n);
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
+    c->boxes_valid[0] = c->boxes_valid[1] = false;
     DM_CUDA(ctx, cudaGetLastError());
     ctx->launches += 3;
     c->order_dirty = true;
@@ -909,6 +918,7 @@ int dm_cloud_set_charge_mass(dm_cloud *c, const double *q, const double *m) {
         c->d.orig, c->n, q ? st[4] : nullptr, m ? st[5] : nullptr, c->d.q, c->d.m);
     // the float charge copy lives in the stage buffers: refresh buffer 0
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
+    c->boxes_valid[0] = c->boxes_valid[1] = false;
     DM_CUDA(ctx, cudaGetLastError());
     return DM_OK;
 }
@@ -930,6 +940,7 @@ int dm_cloud_set_forces(dm_cloud *c, const dm_force_params *p) {
     // the stage buffers carry a per-particle filter bound that depends on kappa
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
+    c->boxes_valid[0] = c->boxes_valid[1] = false;
     DM_CUDA(ctx, cudaGetLastError());
     return DM_OK;
 }

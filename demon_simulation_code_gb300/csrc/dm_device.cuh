@@ -78,6 +78,7 @@ struct StageParams {
     // writes its partial sums to partial[r*n_pad + i]; stage_finish sums them
     int split;
     float4 *partial;
+    int box_out;  // stage_finish: also write the group boxes of the buffer the epilogue writes
 };
 
 // ---------------------------------------------------------------------------

@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
 // Completes a stage after a non-cluster pair launch: per particle, the
 // split partial sums in rank order (FP64), then the stage epilogue.  One
 // particle per thread: the FP64 work runs in full warps on every SM.
-static __global__ void __launch_bounds__(128) stage_finish(const StageParams P) {
+static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P.c.n) {
         double fx = 0.0, fy = 0.0;
@@ -517,6 +517,23 @@ static __global__ void __launch_bounds__(128) stage_finish(const StageParams P) 
             fy += (double)v.y - (double)v.w;
         }
         stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
+    }
+    if (P.box_out) {  // a warp is one 32-particle group: its box in the buffer just written
+        const int bw = P.stage & 1;
+        float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+        if (i < P.c.n) {
+            const float4 A = P.c.pa[bw][i];
+            x0 = x1 = A.x;
+            y0 = y1 = A.y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+            y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+            x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+            y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        }
+        if ((threadIdx.x & 31) == 0 && i < P.c.n_pad) P.c.gbox[bw][i >> 5] = make_float4(x0, y0, x1, y1);
     }
     stage_step_advance(P);
 }
