@@ -107,7 +107,8 @@ struct Fp32cSmem {
     static constexpr size_t queue = (size_t)NW * ILP * 32 * sizeof(int2);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
-    static constexpr size_t glist = (size_t)NW * 32 * sizeof(int) + NW * sizeof(int);  // culling
+    // culling: near and inside group lists (NT each) and their per-warp counts
+    static constexpr size_t glist = 2 * ((size_t)NW * 32 * sizeof(int) + NW * sizeof(int));
     static constexpr size_t bytes = tile + cold + queue + acc + red + glist;
     // s_red, in float4 units from the start of shared memory
     static constexpr size_t red_offset = (tile + cold + queue + acc) / sizeof(float4);
@@ -126,6 +127,21 @@ __device__ __forceinline__ bool boxes_near(const float4 &a, const float4 &b, flo
     const float m = 9.5367431640625e-7f * big;  // 2^-20
     const float dx = fmaxf(0.0f, gx - m), dy = fmaxf(0.0f, gy - m);
     return !(fmaf(dx, dx, dy * dy) >= rc2_hi);  // NaN: near (never drops a pair)
+}
+
+// Conservative FP32 test: is every point of box a within the cutoff of every
+// point of box b?  The farthest separations are widened by 2^-20 of the
+// largest coordinate and the squared distance must stay below 0.999 r_c^2,
+// so for every pair of the two groups the reference's FP64 test
+// kappa*sqrt(dx*dx + dy*dy) < 10 holds (NaN: false).
+__device__ __forceinline__ bool boxes_inside(const float4 &a, const float4 &b, float rc2_lo) {
+    const float gx = fmaxf(a.z - b.x, b.z - a.x);
+    const float gy = fmaxf(a.w - b.y, b.w - a.y);
+    const float big = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.z)), fmaxf(fabsf(b.x), fabsf(b.z))),
+                            fmaxf(fmaxf(fabsf(a.y), fabsf(a.w)), fmaxf(fabsf(b.y), fabsf(b.w))));
+    const float m = 9.5367431640625e-7f * big;  // 2^-20
+    const float dx = gx + m, dy = gy + m;
+    return fmaf(dx, dx, dy * dy) < 0.999f * rc2_lo;
 }
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
@@ -188,6 +204,27 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
     const float ex = exp_neg_sfu(kr, E);
     // C q_i q_j (1 + kr) e^{-kr} / r^3
     const float s = ((ic.qc * A.w) * (1.0f + kr)) * ex * ((y * y) * y);
+    px = fmaf(s, dx, px);
+    py = fmaf(s, dy, py);
+}
+
+// The pair force on i from j for a pair known to be inside the cutoff (a
+// j group entirely within reach of the i tile): the precise arithmetic with
+// no cutoff test; the pair j == i (its own tile) gives zero by selection.
+__device__ __forceinline__ void inside_pair(const StageParams &P, const ExpConsts &E, float xh_i, float yh_i,
+                                            const PairCtx &ic, float xj, float yj, const float4 &Bj, float &px,
+                                            float &py) {
+    const float dx = (xh_i - xj) + (ic.xl - Bj.x);
+    const float dy = (yh_i - yj) + (ic.yl - Bj.y);
+    const bool self = __float_as_int(Bj.w) == ic.ii;
+    const float r2 = self ? 1.0f : fmaf(dx, dx, dy * dy);
+    float y = rsqrtf(r2);
+    const float h = r2 * y;
+    const float ee = fmaf(-h, y, 1.0f);
+    y = fmaf(0.5f * ee, y, y);
+    const float kr = P.kappa_f * (r2 * y);
+    const float ex = exp_neg_sfu(kr, E);
+    const float s = self ? 0.0f : ((ic.qc * Bj.z) * (1.0f + kr)) * ex * ((y * y) * y);
     px = fmaf(s, dx, px);
     py = fmaf(s, dy, py);
 }
@@ -310,7 +347,8 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
     // Sweeps the `count` chunks (4 consecutive j) of this CTA's list through
     // shared-memory tiles; chunk_of(q) is the cloud chunk index of entry q.
     // Within a tile, chunk c goes to warp c % NW.
-    auto sweep = [&](int count, auto chunk_of) {
+    auto sweep = [&](int count, auto chunk_of, auto dense_tag) {
+    constexpr bool DENSE = decltype(dense_tag)::value;
     for (int q0 = 0; q0 < count; q0 += TC) {
         const int tcn = min(TC, count - q0);
         __syncthreads();
@@ -338,6 +376,32 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
             s_b4[e] = make_float4(bs[0], bs[1], bs[2], bs[3]);
         }
         __syncthreads();
+        if constexpr (DENSE) {
+            // every pair of these groups is inside the cutoff: no filter, no
+            // queue; each lane evaluates its own i against the chunk's 4 j
+            for (int c = warp; c < tcn; c += NW) {
+                const float4 X = s_x4[c], Y = s_y4[c];
+                const float xs[4] = {X.x, X.y, X.z, X.w};
+                const float ys[4] = {Y.x, Y.y, Y.z, Y.w};
+                static_for<ILP>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
+                    const float4 c4 = s_cold[k * 32 + lane];
+                    PairCtx ic;
+                    ic.xl = c4.x;
+                    ic.yl = c4.y;
+                    ic.qc = c4.z;
+                    ic.ii = __float_as_int(c4.w);
+                    const float xh = -0.5f * mx2[k].x, yh = -0.5f * my2[k].x;
+                    float px = 0.0f, py = 0.0f;
+#pragma unroll 1
+                    for (int u = 0; u < 4; u++) inside_pair(P, E, xh, yh, ic, xs[u], ys[u], s_pb[4 * c + u], px, py);
+                    float4 acc = my_acc[k * 32 + lane];
+                    kahan_add(acc.x, acc.z, px);
+                    kahan_add(acc.y, acc.w, py);
+                    my_acc[k * 32 + lane] = acc;
+                });
+            }
+        } else {
         for (int c = warp; c < tcn; c += NW) {
             const float4 X = s_x4[c], Y = s_y4[c], Bq = s_b4[c];
             const float2 X01 = make_float2(X.x, X.y), X23 = make_float2(X.z, X.w);
@@ -380,6 +444,7 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         }
         // queued entries index into this tile: drain before it is overwritten
         flush_slots(1);
+        }
     }
     };
 
@@ -389,7 +454,7 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         // rank (and every warp) samples the whole cloud evenly
         const int nch_all = (n + 3) >> 2;
         const int my_nch = (nch_all - rank + S - 1) / S;  // chunks of this rank
-        sweep(my_nch, [&](int q) { return q * S + rank; });
+        sweep(my_nch, [&](int q) { return q * S + rank; }, std::false_type{});
     } else {
         // 32-particle groups dealt round-robin to ranks; a group whose box is
         // beyond the cutoff from the tile's box is skipped whole (it holds no
@@ -406,24 +471,40 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         }
         const int my_ng = (ngroups - rank + S - 1) / S;
         unsigned long long swept = 0ull;
+        int *s_glist2 = s_wcount + NW;  // [NT] groups entirely inside the cutoff
+        int *s_wcount2 = s_glist2 + NT;  // [NW]
         for (int t0 = 0; t0 < my_ng; t0 += NT) {
             const int t = t0 + tid;
             const int g = t * S + rank;
-            const bool keep = (t < my_ng) && boxes_near(tb, gb[g], P.rc2_hi);
-            const uint32_t bal = __ballot_sync(0xffffffffu, keep);
-            if (lane == 0) s_wcount[warp] = __popc(bal);
+            bool near = false, inside = false;
+            if (t < my_ng) {
+                const float4 gbox = gb[g];
+                near = boxes_near(tb, gbox, P.rc2_hi);
+                inside = near && boxes_inside(tb, gbox, P.rc2_lo);
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, near && !inside);
+            const uint32_t bal2 = __ballot_sync(0xffffffffu, inside);
+            if (lane == 0) {
+                s_wcount[warp] = __popc(bal);
+                s_wcount2[warp] = __popc(bal2);
+            }
             __syncthreads();
-            int off = 0, total = 0;
+            int off = 0, total = 0, off2 = 0, total2 = 0;
 #pragma unroll
             for (int w = 0; w < NW; w++) {
-                const int cw = s_wcount[w];
+                const int cw = s_wcount[w], cw2 = s_wcount2[w];
                 off += (w < warp) ? cw : 0;
+                off2 += (w < warp) ? cw2 : 0;
                 total += cw;
+                total2 += cw2;
             }
-            if (keep) s_glist[off + __popc(bal & ((1u << lane) - 1u))] = g;
-            sweep(8 * total, [&](int q) { return 8 * s_glist[q >> 3] + (q & 7); });
-            swept += (unsigned long long)total;
-            __syncthreads();  // s_glist, s_wcount reused by the next batch
+            const uint32_t below = (1u << lane) - 1u;
+            if (near && !inside) s_glist[off + __popc(bal & below)] = g;
+            if (inside) s_glist2[off2 + __popc(bal2 & below)] = g;
+            sweep(8 * total, [&](int q) { return 8 * s_glist[q >> 3] + (q & 7); }, std::false_type{});
+            sweep(8 * total2, [&](int q) { return 8 * s_glist2[q >> 3] + (q & 7); }, std::true_type{});
+            swept += (unsigned long long)(total + total2);
+            __syncthreads();  // the lists and counts are reused by the next batch
         }
         if (tid == 0 && swept) atomicAdd(P.c.eval_pairs, swept * 32ull * (unsigned long long)TILE);
     }
