@@ -41,13 +41,48 @@ class ForceParams(ctypes.Structure):
         ("thermal_mode", ctypes.c_int),
         ("reserved", ctypes.c_int),
         ("seed", ctypes.c_uint64),
+        ("void_decay", ctypes.c_double),
+        ("drive_const", ctypes.c_double),
+        ("drive_amplitude", ctypes.c_double),
+        ("drive_shift", ctypes.c_double),
+        ("magnetic", ctypes.c_double),
+        ("rot_rmin", ctypes.c_double),
+        ("rot_rmax", ctypes.c_double),
+        ("rot_const", ctypes.c_double),
+        ("heat_in", ctypes.c_double),
+        ("heat_out", ctypes.c_double),
+        ("heat_radius", ctypes.c_double),
+        ("drag_scale", ctypes.c_double),
+        ("drag_offset", ctypes.c_double),
+        ("heat_scale", ctypes.c_double),
+        ("heat_offset", ctypes.c_double),
+        ("electric", ctypes.c_double),
+        ("electric_radius", ctypes.c_double),
+        ("gravity", ctypes.c_double),
+        ("vert_electric", ctypes.c_double),
+        ("vert_decay", ctypes.c_double),
     ]
 
 
+# dm_force_params fields after seed, in order
+EXTRA_FIELDS = [
+    "void_decay", "drive_const", "drive_amplitude", "drive_shift", "magnetic",
+    "rot_rmin", "rot_rmax", "rot_const", "heat_in", "heat_out", "heat_radius",
+    "drag_scale", "drag_offset", "heat_scale", "heat_offset", "electric",
+    "electric_radius", "gravity", "vert_electric", "vert_decay",
+]
+
+
 def force_params(flags, shielding=2e4, confine=0.0, confine_x=0.0, confine_y=0.0, gamma=0.0,
-                 heat=0.0, thermal_mode=1, seed=0) -> ForceParams:
-    return ForceParams(int(flags), shielding, confine, confine_x, confine_y, gamma, heat,
-                       int(thermal_mode), 0, int(seed))
+                 heat=0.0, thermal_mode=1, seed=0, **extra) -> ForceParams:
+    """extra: the other forces' fields of dm_force_params by name (0 if not given)."""
+    p = ForceParams(int(flags), shielding, confine, confine_x, confine_y, gamma, heat, int(thermal_mode), 0,
+                    int(seed))
+    for k, v in extra.items():
+        if k not in EXTRA_FIELDS:
+            raise TypeError(f"unknown force parameter {k!r}")
+        setattr(p, k, float(v))
+    return p
 
 
 # (name, restype, argtypes) of every exported symbol
@@ -94,6 +129,8 @@ SIGNATURES = {
     "dm_cloud_set_reorder_interval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dm_cloud_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dm_cloud_get_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "dm_cloud_set_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "dm_cloud_get_time": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "dm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp, _dp,
                                        _dp, _dp, _dp, _dp, ctypes.POINTER(ForceParams),
                                        ctypes.POINTER(ctypes.c_void_p)]),
@@ -104,6 +141,8 @@ SIGNATURES = {
     "dm_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "dm_batch_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "dm_batch_set_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "dm_batch_get_time": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "dm_adjoint_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                          ctypes.POINTER(ForceParams), ctypes.POINTER(ctypes.c_void_p)]),
     "dm_adjoint_destroy": (ctypes.c_int, [ctypes.c_void_p]),

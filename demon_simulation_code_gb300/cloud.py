@@ -144,7 +144,13 @@ class DeviceCloud:
         return fx, fy
 
     def step(self, nsteps: int, dt: float, precision="fp32c", t: float | None = None):
-        tt = ctypes.c_double(t or 0.0)
+        """nsteps fixed-dt RK4 steps.  With t, the force time starts at t and
+        the time after the steps is returned; without, the steps continue
+        from the cloud's force time and None is returned."""
+        if t is None:
+            self._chk(self.lib.dm_cloud_step(self.h, int(nsteps), float(dt), _prec(precision), None))
+            return None
+        tt = ctypes.c_double(t)
         self._chk(self.lib.dm_cloud_step(self.h, int(nsteps), float(dt), _prec(precision),
                                          ctypes.byref(tt)))
         return tt.value
@@ -194,6 +200,15 @@ class DeviceCloud:
     def get_step_counter(self) -> int:
         v = ctypes.c_uint64()
         self._chk(self.lib.dm_cloud_get_step_counter(self.h, ctypes.byref(v)))
+        return v.value
+
+    def set_time(self, t: float):
+        """Force time of the next step (Integrator::currentTime)."""
+        self._chk(self.lib.dm_cloud_set_time(self.h, float(t)))
+
+    def get_time(self) -> float:
+        v = ctypes.c_double()
+        self._chk(self.lib.dm_cloud_get_time(self.h, ctypes.byref(v)))
         return v.value
 
 
@@ -262,3 +277,11 @@ class DeviceBatch:
 
     def set_step_counter(self, step: int):
         check(self.lib.dm_batch_set_step_counter(self.h, int(step)), self.ctx.h)
+
+    def set_time(self, t: float):
+        check(self.lib.dm_batch_set_time(self.h, float(t)), self.ctx.h)
+
+    def get_time(self) -> float:
+        v = ctypes.c_double()
+        check(self.lib.dm_batch_get_time(self.h, ctypes.byref(v)), self.ctx.h)
+        return v.value

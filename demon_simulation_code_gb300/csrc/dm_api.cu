@@ -807,6 +807,7 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     for (int b = 0; b < 2; b++) { c->d.gbox[b] = (float4 *)p; p += ngb; }
     c->d.eval_pairs = (unsigned long long *)p; p += 256;
     c->d.step_ctr = (unsigned long long *)p; p += 256;
+    c->d.time = (double *)(c->d.step_ctr + 4);  // same 256-byte slot, bytes 32-47
     c->d.err = (int *)p; p += 256;
     c->d_dt = (double *)p; p += 256;
     c->d_min = (unsigned int *)p; c->d_dmin = (float *)(p + 64); p += 256;
@@ -926,10 +927,9 @@ int dm_cloud_set_charge_mass(dm_cloud *c, const double *q, const double *m) {
 int dm_cloud_set_forces(dm_cloud *c, const dm_force_params *p) {
     if (!c || !p) return DM_ERR_ARG;
     dm_ctx *ctx = c->ctx;
-    const long long known = kConfinement | kDrag | kShieldedCoulomb | kThermal | kRectConfinement;
-    if (p->flags & ~known)
-        return ctx->fail(DM_ERR_UNSUPPORTED, "dm_cloud_set_forces: unsupported force flags 0x%llx",
-                         (unsigned long long)(p->flags & ~known));
+    if (p->flags & ~kAllForces)
+        return ctx->fail(DM_ERR_UNSUPPORTED, "dm_cloud_set_forces: unknown force flags 0x%llx",
+                         (unsigned long long)(p->flags & ~kAllForces));
     if ((p->flags & kShieldedCoulomb) && !(p->shielding > 0.0 && std::isfinite(p->shielding)))
         return ctx->fail(DM_ERR_ARG, "dm_cloud_set_forces: shielding must be positive and finite");
     if (p->thermal_mode != 0 && p->thermal_mode != 1)
@@ -1002,6 +1002,10 @@ int dm_cloud_step(dm_cloud *c, int nsteps, double dt, int precision, double *t_i
     if (precision != DM_FP64 && precision != DM_FP32C)
         return ctx->fail(DM_ERR_ARG, "bad precision %d", precision);
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (t_inout) {  // the force time of the first step is the caller's time
+        set_time_slots<<<1, 1, 0, ctx->stream>>>(c->d.time, *t_inout);
+        DM_CUDA(ctx, cudaGetLastError());
+    }
     int rc = run_steps(c, nsteps, dt, precision);
     if (rc) return rc;
     if (t_inout)
@@ -1041,6 +1045,10 @@ int dm_cloud_move_particles(dm_cloud *c, double end_time, double dt, int precisi
     if (!(dt > 0.0)) return ctx->fail(DM_ERR_ARG, "dt must be positive");
     double t = *t_inout;
     int count = 0;
+    // the force time of the first step is the caller's time
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    set_time_slots<<<1, 1, 0, ctx->stream>>>(c->d.time, t);
+    DM_CUDA(ctx, cudaGetLastError());
     if (!adaptive) {
         // same accumulation as `while (currentTime < endTime) currentTime += dt`
         while (t < end_time) {
@@ -1173,6 +1181,26 @@ int dm_cloud_set_step_counter(dm_cloud *c, uint64_t step) {
     unsigned long long v[2] = {step, step};
     DM_CUDA(ctx, cudaMemcpyAsync(c->d.step_ctr, v, sizeof(v), cudaMemcpyHostToDevice, ctx->stream));
     DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return DM_OK;
+}
+
+int dm_cloud_set_time(dm_cloud *c, double t) {
+    if (!c) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    set_time_slots<<<1, 1, 0, ctx->stream>>>(c->d.time, t);
+    DM_CUDA(ctx, cudaGetLastError());
+    return DM_OK;
+}
+
+int dm_cloud_get_time(dm_cloud *c, double *t) {
+    if (!c || !t) return DM_ERR_ARG;
+    dm_ctx *ctx = c->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    double v = 0.0;
+    DM_CUDA(ctx, cudaMemcpyAsync(&v, c->d.time, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *t = v;
     return DM_OK;
 }
 
@@ -1431,8 +1459,10 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     long long total = 0;
     for (int c = 0; c < nclouds; c++) {
         if (n[c] < 1) return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d has n = %d", c, n[c]);
-        const long long kn = params[c].flags & ~(kConfinement | kDrag | kShieldedCoulomb | kThermal | kRectConfinement);
-        if (kn) return ctx->fail(DM_ERR_UNSUPPORTED, "dm_batch_create: unsupported force flags in cloud %d", c);
+        if (params[c].flags & ~kAllForces)
+            return ctx->fail(DM_ERR_UNSUPPORTED, "dm_batch_create: unknown force flags in cloud %d", c);
+        if (params[c].thermal_mode != 0 && params[c].thermal_mode != 1)
+            return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d thermal_mode must be 0 or 1", c);
         if ((params[c].flags & kShieldedCoulomb) && !(params[c].shielding > 0.0))
             return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d shielding must be positive", c);
         total += n[c];
@@ -1490,6 +1520,7 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     B->ddesc = (BatchCloud *)p; p += ndesc;
     B->dbbox = (unsigned long long *)p; p += nbb;
     d.step_ctr = (unsigned long long *)p; p += 256;
+    d.time = (double *)(d.step_ctr + 4);  // same 256-byte slot, bytes 32-47
     d.err = (int *)p; p += 256;
     B->dcounter = (unsigned int *)p; p += 256;
     // host descriptors
@@ -1694,6 +1725,26 @@ int dm_batch_info(dm_batch *B, char *variant, size_t len, int *nitems, int *grid
     if (variant && len) snprintf(variant, len, "%s", kBatchVariants[B->variant].name);
     if (nitems) *nitems = B->nitems[B->variant];
     if (grid) *grid = B->grid[B->variant];
+    return DM_OK;
+}
+
+int dm_batch_set_time(dm_batch *B, double t) {
+    if (!B) return DM_ERR_ARG;
+    dm_ctx *ctx = B->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    set_time_slots<<<1, 1, 0, ctx->stream>>>(B->d.time, t);
+    DM_CUDA(ctx, cudaGetLastError());
+    return DM_OK;
+}
+
+int dm_batch_get_time(dm_batch *B, double *t) {
+    if (!B || !t) return DM_ERR_ARG;
+    dm_ctx *ctx = B->ctx;
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    double v = 0.0;
+    DM_CUDA(ctx, cudaMemcpyAsync(&v, B->d.time, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *t = v;
     return DM_OK;
 }
 

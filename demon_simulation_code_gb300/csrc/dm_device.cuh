@@ -24,11 +24,25 @@
 
 namespace dm {
 
+// ForceFlag bits (Force.h:75-91)
 constexpr long long kConfinement = 1;
 constexpr long long kDrag = 2;
 constexpr long long kShieldedCoulomb = 4;
+constexpr long long kGravitational = 8;
 constexpr long long kThermal = 16;
+constexpr long long kThermalLocalized = 32;
+constexpr long long kDriving = 64;
+constexpr long long kRotational = 128;
+constexpr long long kTimeVaryingDrag = 256;
+constexpr long long kTimeVaryingThermal = 512;
+constexpr long long kMagnetic = 1024;
+constexpr long long kConfinementVoid = 2048;
+constexpr long long kElectric = 4096;
 constexpr long long kRectConfinement = 8192;
+constexpr long long kVertElectric = 16384;
+constexpr long long kAllForces = 32767;
+// forces that read the force time
+constexpr long long kTimeForces = kDriving | kTimeVaryingDrag | kTimeVaryingThermal;
 
 constexpr float kPadPosition = 1.0e18f;
 
@@ -37,6 +51,9 @@ struct ForceParams {  // same layout as dm_force_params
     double shielding, confine, confine_x, confine_y, gamma, heat;
     int thermal_mode, reserved;
     unsigned long long seed;
+    double void_decay, drive_const, drive_amplitude, drive_shift, magnetic, rot_rmin, rot_rmax, rot_const;
+    double heat_in, heat_out, heat_radius, drag_scale, drag_offset, heat_scale, heat_offset;
+    double electric, electric_radius, gravity, vert_electric, vert_decay;
 };
 
 struct CloudDev {
@@ -50,6 +67,7 @@ struct CloudDev {
     float4 *gbox[2];               // [n_pad/32] FP32 box (x0, y0, x1, y1) of each 32-particle group
     unsigned long long *eval_pairs;  // ordered pairs the culling kernels swept (cumulative)
     unsigned long long *step_ctr;  // [2], see stage_step_index()
+    double *time;                  // [2] force time slots, see stage_time()
     int *err;                      // device error flags
     double rc2;                    // (10/kappa)^2 of the current force parameters
     double coulomb;                // 1/(4 pi eps0)
@@ -160,14 +178,16 @@ __device__ __forceinline__ void thermal_sincos(float u, float &sn, float &cs) {
     }
 }
 
-// Thermal kick for particle i at (step, stage).  Mode 0 is the reference's
-// form heatVal*U*(cos t, sin t), t ~ U(0, 2pi) (ThermalForce.cpp:118-140)
-// with counter-based uniforms; mode 1 is a Gaussian of standard deviation
-// `heat` per axis (Box-Muller).
-__device__ __forceinline__ void thermal_kick(const ForceParams &f, uint32_t i,
-                                             unsigned long long step, int stage,
+// Counter-based kick of scale `heat` for particle i: counter (i, step lo,
+// step hi, stream).  Mode 0 is the reference's form heatVal*U*(cos t, sin t),
+// t ~ U(0, 2pi) (ThermalForce.cpp:118-140) with counter-based uniforms; mode
+// 1 is a Gaussian of standard deviation `heat` per axis (Box-Muller).
+// Streams: stage for ThermalForce, stage + 16 for ThermalForceLocalized,
+// stage + 32 for TimeVaryingThermalForce.
+__device__ __forceinline__ void thermal_draw(const ForceParams &f, uint32_t i,
+                                             unsigned long long step, int stream, double heat,
                                              double &tx, double &ty) {
-    uint32_t c[4] = {i, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)stage};
+    uint32_t c[4] = {i, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)stream};
     philox4x32_10(c, (uint32_t)f.seed, (uint32_t)(f.seed >> 32));
     const float u1 = u24(c[0]);
     const float u2 = u24(c[1]);
@@ -176,8 +196,14 @@ __device__ __forceinline__ void thermal_kick(const ForceParams &f, uint32_t i,
     float amp;
     if (f.thermal_mode == 0) amp = u1;
     else amp = __fsqrt_rn(__fmul_rn(-2.0f, thermal_log(u1)));
-    tx = __dmul_rn(f.heat, (double)__fmul_rn(amp, cs));
-    ty = __dmul_rn(f.heat, (double)__fmul_rn(amp, sn));
+    tx = __dmul_rn(heat, (double)__fmul_rn(amp, cs));
+    ty = __dmul_rn(heat, (double)__fmul_rn(amp, sn));
+}
+
+__device__ __forceinline__ void thermal_kick(const ForceParams &f, uint32_t i,
+                                             unsigned long long step, int stage,
+                                             double &tx, double &ty) {
+    thermal_draw(f, i, step, stage, f.heat, tx, ty);
 }
 
 // RNG step index of the running stage.  Stage 1 reads slot 0 and copies it
@@ -187,11 +213,30 @@ __device__ __forceinline__ unsigned long long stage_step_index(const StageParams
     const int s = (P.mode == kModeForceOnly) ? 1 : P.stage;
     return (s == 1) ? P.c.step_ctr[0] : P.c.step_ctr[1];
 }
+// Force time of the running stage: t, t + dt/2.0, t + dt/2.0, t + dt for
+// stages 1-4 (Runge_Kutta4.cpp:30-88), t the time at the start of the step.
+// Same slot discipline as the step counter: stage 1 reads slot 0 and copies
+// it to slot 1, stages 2-4 read slot 1, stage 4 writes slot 0 = t + dt
+// (currentTime += dt, Runge_Kutta4.cpp:135).  Force-only launches use the
+// time in slot 0.
+__device__ __forceinline__ double stage_dt(const StageParams &P) {
+    return P.dt_dev ? *P.dt_dev : P.dt;
+}
+__device__ __forceinline__ double stage_time(const StageParams &P) {
+    if (P.mode == kModeForceOnly || P.stage == 1) return P.c.time[0];
+    const double t = P.c.time[1], dt = stage_dt(P);
+    return (P.stage == 4) ? __dadd_rn(t, dt) : __dadd_rn(t, __ddiv_rn(dt, 2.0));
+}
 __device__ __forceinline__ void stage_step_advance(const StageParams &P) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     if (P.mode == kModeForceOnly) return;
-    if (P.stage == 1) P.c.step_ctr[1] = P.c.step_ctr[0];
-    else if (P.stage == 4) P.c.step_ctr[0] = P.c.step_ctr[1] + 1ull;
+    if (P.stage == 1) {
+        P.c.step_ctr[1] = P.c.step_ctr[0];
+        P.c.time[1] = P.c.time[0];
+    } else if (P.stage == 4) {
+        P.c.step_ctr[0] = P.c.step_ctr[1] + 1ull;
+        P.c.time[0] = __dadd_rn(P.c.time[1], stage_dt(P));
+    }
 }
 
 // Two-float split of a position: x = hi + lo.
@@ -235,19 +280,6 @@ __device__ __forceinline__ bool ref_in_cutoff(double dx, double dy, double kappa
     return a < 10.0;
 }
 
-// The per-particle epilogue of one RK stage for particle i, given the
-// shielded-Coulomb pair sum (fpx, fpy) at the stage positions:
-//  - sums the enabled forces in the reference driver's order
-//    (driver.cpp:372-402): Confinement (ConfinementForce.cpp:48-54), Drag
-//    (DragForce.cpp:49-55), RectConfinement (RectConfinementForce.cpp:50-59),
-//    ShieldedCoulomb, Thermal;
-//  - stage increments k = (dt*Fx)/m, l = dt*Vx_stage (Runge_Kutta4.cpp:32-104);
-//  - the next stage's CacheOperator values (CacheOperator.cpp:28-73);
-//  - after stage 4 the combine v += (k1 + (2*(k2+k3) + k4))/6
-//    (Runge_Kutta4.cpp:107-133, 147-151).
-// Every FP64 operation is an explicit round-to-nearest intrinsic so nothing
-// is contracted into an FMA: given the same forces the state update is bit
-// for bit the reference's.
 // Thermal kick of particle i for the running stage (zero when the thermal
 // force is off); computed ahead of the epilogue by the pair kernels.
 __device__ __forceinline__ double2 stage_thermal(const StageParams &P, int i) {
@@ -258,6 +290,133 @@ __device__ __forceinline__ double2 stage_thermal(const StageParams &P, int i) {
     return make_double2(tx, ty);
 }
 
+// DrivingForce::waveNum, angFreq (DrivingForce.cpp:14-15)
+constexpr double kWaveNum = 2.0 * 3.14159265358979323846 / 0.002;
+constexpr double kAngFreq = 2.0 * 3.14159265358979323846 * 10.0;
+
+// One particle's per-particle forces, each added as the reference's force()
+// adds into forceX/forceY (plusEqual_pd / minusEqual_pd); every FP64
+// operation is an explicit round-to-nearest intrinsic so nothing is fused.
+struct ParticleAt {
+    double x, y, vx, vy, q, m;
+};
+
+// ConfinementForce::force (ConfinementForce.cpp:48-54)
+__device__ __forceinline__ void add_confinement(const ForceParams &f, const ParticleAt &s, double &Fx,
+                                                double &Fy) {
+    const double cq = __dmul_rn(s.q, f.confine);
+    Fx = __dadd_rn(Fx, __dmul_rn(cq, s.x));
+    Fy = __dadd_rn(Fy, __dmul_rn(cq, s.y));
+}
+
+// DragForce::force (DragForce.cpp:49-55) with dragConst
+__device__ __forceinline__ void add_drag(double dragConst, const ParticleAt &s, double &Fx, double &Fy) {
+    const double d = __dmul_rn(s.m, dragConst);
+    Fx = __dadd_rn(Fx, __dmul_rn(d, s.vx));
+    Fy = __dadd_rn(Fy, __dmul_rn(d, s.vy));
+}
+
+// sqrt(x*x + y*y) without contraction (length_pd, VectorCompatibility.h:290-292)
+__device__ __forceinline__ double radius_of(const ParticleAt &s) {
+    return __dsqrt_rn(__dadd_rn(__dmul_rn(s.x, s.x), __dmul_rn(s.y, s.y)));
+}
+
+// The forces the reference driver pushes before ShieldedCoulomb other than
+// Confinement and Drag (driver.cpp:375-386), in its order around them:
+// ConfinementVoid (ConfinementForceVoid.cpp:13-17, 48-55) after Confinement,
+// then Drag, Driving (DrivingForce.cpp:52-61), Magnetic
+// (MagneticForce.cpp:48-54), RectConfinement (RectConfinementForce.cpp:50-59),
+// Rotational (RotationalForce.cpp:50-66).
+__device__ __forceinline__ void add_forces_before_pairs(const ForceParams &f, const ParticleAt &s,
+                                                        double t, double &Fx, double &Fy) {
+    const long long fl = f.flags;
+    if (fl & kConfinement) add_confinement(f, s, Fx, Fy);
+    if (fl & kConfinementVoid) {
+        add_confinement(f, s, Fx, Fy);
+        const double decayV = __dmul_rn(s.q, -f.void_decay);
+        const double r = radius_of(s);
+        const double expR = __ddiv_rn(exp(__dmul_rn(r, -f.void_decay)), r);
+        Fx = __dadd_rn(Fx, __dmul_rn(__dmul_rn(decayV, expR), s.x));
+        Fy = __dadd_rn(Fy, __dmul_rn(__dmul_rn(decayV, expR), s.y));
+    }
+    if (fl & kDrag) add_drag(-f.gamma, s, Fx, Fy);  // dragConst = -gamma (DragForce.h:16-17)
+    if (fl & kDriving) {
+        // the stored driveConst is -drive_const (DrivingForce.h:17-18)
+        const double distV = __dsub_rn(s.x, f.drive_shift);
+        const double sinArg = __dsub_rn(__dmul_rn(s.x, kWaveNum), __dmul_rn(t, kAngFreq));
+        const double expArg = __ddiv_rn(__dsub_rn(distV, distV), f.drive_const);
+        Fx = __dadd_rn(Fx, __dmul_rn(__dmul_rn(sin(sinArg), exp(expArg)), f.drive_amplitude));
+    }
+    if (fl & kMagnetic) {
+        const double qB = __dmul_rn(s.q, f.magnetic);
+        Fx = __dadd_rn(Fx, __dmul_rn(qB, s.vy));
+        Fy = __dsub_rn(Fy, __dmul_rn(qB, s.vx));
+    }
+    if (fl & kRectConfinement) {
+        Fx = __dadd_rn(Fx, __dmul_rn(__dmul_rn(s.q, f.confine_x), s.x));
+        Fy = __dadd_rn(Fy, __dmul_rn(__dmul_rn(s.q, f.confine_y), s.y));
+    }
+    if (fl & kRotational) {
+        const double r = radius_of(s);
+        if (r > f.rot_rmin && r < f.rot_rmax) {
+            Fx = __dsub_rn(Fx, __ddiv_rn(__dmul_rn(f.rot_const, s.y), r));
+            Fy = __dadd_rn(Fy, __ddiv_rn(__dmul_rn(f.rot_const, s.x), r));
+        }
+    }
+}
+
+// The forces pushed after ShieldedCoulomb and Thermal (driver.cpp:391-402):
+// ThermalLocalized (ThermalForceLocalized.cpp:124-133), TimeVaryingDrag
+// (TimeVaryingDragForce.cpp:11-40), TimeVaryingThermal
+// (TimeVaryingThermalForce.cpp:14-42), Electric (ElectricForce.cpp:48-62),
+// Gravitational (GravitationalForce.cpp:46-50), VertElectric
+// (VertElectricForce.cpp:47-53).
+__device__ __forceinline__ void add_forces_after_pairs(const ForceParams &f, const ParticleAt &s,
+                                                       double t, uint32_t id, unsigned long long step,
+                                                       int stage, double &Fx, double &Fy) {
+    const long long fl = f.flags;
+    if (fl & kThermalLocalized) {
+        const double heat = (radius_of(s) < f.heat_radius) ? f.heat_in : f.heat_out;
+        double tx, ty;
+        thermal_draw(f, id, step, stage + 16, heat, tx, ty);
+        Fx = __dadd_rn(Fx, tx);
+        Fy = __dadd_rn(Fy, ty);
+    }
+    if (fl & kTimeVaryingDrag) add_drag(-__dadd_rn(__dmul_rn(f.drag_scale, t), f.drag_offset), s, Fx, Fy);
+    if (fl & kTimeVaryingThermal) {
+        double tx, ty;
+        thermal_draw(f, id, step, stage + 32, __dadd_rn(__dmul_rn(f.heat_scale, t), f.heat_offset), tx, ty);
+        Fx = __dadd_rn(Fx, tx);
+        Fy = __dadd_rn(Fy, ty);
+    }
+    if (fl & kElectric) {
+        const double cV = __dmul_rn(s.q, f.electric);
+        const double eV = __dmul_rn(cV, exp(__ddiv_rn(radius_of(s), -f.electric_radius)));
+        Fx = __dadd_rn(Fx, __dmul_rn(eV, s.x));
+        Fy = __dadd_rn(Fy, __dmul_rn(eV, s.y));
+    }
+    if (fl & kGravitational) Fy = __dadd_rn(Fy, __dmul_rn(s.m, f.gravity));
+    if (fl & kVertElectric) {
+        const double cV = __dmul_rn(s.q, f.vert_electric);
+        Fy = __dadd_rn(Fy, __dmul_rn(cV, exp(__ddiv_rn(s.y, f.vert_decay))));
+    }
+}
+
+// The per-particle epilogue of one RK stage for particle i, given the
+// shielded-Coulomb pair sum (fpx, fpy) at the stage positions:
+//  - sums the enabled forces in the reference driver's order
+//    (driver.cpp:372-402): Confinement, ConfinementVoid, Drag, Driving,
+//    Magnetic, RectConfinement, Rotational, ShieldedCoulomb, Thermal,
+//    ThermalLocalized, TimeVaryingDrag, TimeVaryingThermal, Electric,
+//    Gravitational, VertElectric, at the stage's force time;
+//  - stage increments k = (dt*Fx)/m, l = dt*Vx_stage (Runge_Kutta4.cpp:32-104);
+//  - the next stage's CacheOperator values (CacheOperator.cpp:28-73);
+//  - after stage 4 the combine v += (k1 + (2*(k2+k3) + k4))/6
+//    (Runge_Kutta4.cpp:107-133, 147-151).
+// Every FP64 operation is an explicit round-to-nearest intrinsic so nothing
+// is contracted into an FMA: given the same forces the state update is bit
+// for bit the reference's.  The forces other than Confinement, Drag,
+// RectConfinement, ShieldedCoulomb and Thermal sit behind one flag test.
 __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, double fpx,
                                                double fpy, double2 therm) {
     const CloudDev &c = P.c;
@@ -268,35 +427,51 @@ __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, doub
     const double vys = (s == 1) ? c.vy[i] : c.vyc[i];
     const double q = c.q[i], m = c.m[i];
     const long long fl = P.f.flags;
+    constexpr long long kBasic = kConfinement | kDrag | kRectConfinement | kShieldedCoulomb | kThermal;
     double Fx = 0.0, Fy = 0.0;
-    if (fl & kConfinement) {
-        const double cq = __dmul_rn(q, P.f.confine);
-        Fx = __dadd_rn(Fx, __dmul_rn(cq, xs));
-        Fy = __dadd_rn(Fy, __dmul_rn(cq, ys));
-    }
-    if (fl & kDrag) {
-        const double d = __dmul_rn(m, -P.f.gamma);
-        Fx = __dadd_rn(Fx, __dmul_rn(d, vxs));
-        Fy = __dadd_rn(Fy, __dmul_rn(d, vys));
-    }
-    if (fl & kRectConfinement) {
-        Fx = __dadd_rn(Fx, __dmul_rn(__dmul_rn(q, P.f.confine_x), xs));
-        Fy = __dadd_rn(Fy, __dmul_rn(__dmul_rn(q, P.f.confine_y), ys));
-    }
-    if (fl & kShieldedCoulomb) {
-        Fx = __dadd_rn(Fx, fpx);
-        Fy = __dadd_rn(Fy, fpy);
-    }
-    if (fl & kThermal) {
-        Fx = __dadd_rn(Fx, therm.x);
-        Fy = __dadd_rn(Fy, therm.y);
+    if (fl & ~kBasic) {
+        const ParticleAt pt{xs, ys, vxs, vys, q, m};
+        const double t = (fl & kTimeForces) ? stage_time(P) : 0.0;
+        add_forces_before_pairs(P.f, pt, t, Fx, Fy);
+        if (fl & kShieldedCoulomb) {
+            Fx = __dadd_rn(Fx, fpx);
+            Fy = __dadd_rn(Fy, fpy);
+        }
+        if (fl & kThermal) {
+            Fx = __dadd_rn(Fx, therm.x);
+            Fy = __dadd_rn(Fy, therm.y);
+        }
+        add_forces_after_pairs(P.f, pt, t, (uint32_t)c.orig[i], stage_step_index(P), P.therm_stage, Fx, Fy);
+    } else {
+        if (fl & kConfinement) {
+            const double cq = __dmul_rn(q, P.f.confine);
+            Fx = __dadd_rn(Fx, __dmul_rn(cq, xs));
+            Fy = __dadd_rn(Fy, __dmul_rn(cq, ys));
+        }
+        if (fl & kDrag) {
+            const double d = __dmul_rn(m, -P.f.gamma);
+            Fx = __dadd_rn(Fx, __dmul_rn(d, vxs));
+            Fy = __dadd_rn(Fy, __dmul_rn(d, vys));
+        }
+        if (fl & kRectConfinement) {
+            Fx = __dadd_rn(Fx, __dmul_rn(__dmul_rn(q, P.f.confine_x), xs));
+            Fy = __dadd_rn(Fy, __dmul_rn(__dmul_rn(q, P.f.confine_y), ys));
+        }
+        if (fl & kShieldedCoulomb) {
+            Fx = __dadd_rn(Fx, fpx);
+            Fy = __dadd_rn(Fy, fpy);
+        }
+        if (fl & kThermal) {
+            Fx = __dadd_rn(Fx, therm.x);
+            Fy = __dadd_rn(Fy, therm.y);
+        }
     }
     if (P.mode == kModeForceOnly) {  // outputs in the caller's order
         P.fx_out[c.orig[i]] = Fx;
         P.fy_out[c.orig[i]] = Fy;
         return;
     }
-    const double dt = P.dt_dev ? *P.dt_dev : P.dt;
+    const double dt = stage_dt(P);
     const double k = __ddiv_rn(__dmul_rn(dt, Fx), m);
     const double l = __dmul_rn(dt, vxs);
     const double mm = __ddiv_rn(__dmul_rn(dt, Fy), m);

@@ -29,6 +29,12 @@ static __global__ void init_positions(CloudDev c) {
 // For the autotuner: the positions squeezed about (cx, cy) by lam, written
 // as stage buffer 1 (which holds nothing live between steps), so kernels can
 // be timed on a denser copy of the cloud without touching its state.
+// Both force time slots = t (see stage_time()).
+static __global__ void set_time_slots(double *time, double t) {
+    time[0] = t;
+    time[1] = t;
+}
+
 static __global__ void tune_compress(CloudDev c, double cx, double cy, double lam) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < c.n) write_stage_position(c, 1, i, cx + lam * (c.x[i] - cx), cy + lam * (c.y[i] - cy));

@@ -15,7 +15,7 @@ public:
     void readForce(fitsfile *const file, int *const error) override;
     bool addDeviceParams(dm_force_params &p) const override;
 
-private:
+protected:
     double confine;  //!< strength of the confinement [V/m^2]
 };
 

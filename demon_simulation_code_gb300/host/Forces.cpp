@@ -4,7 +4,8 @@
  *
  * FITS keys follow the reference's writeForce/readForce: FORCES (bitmask,
  * e.g. ConfinementForce.cpp:60-84), confineConst, confineConstX/Y,
- * dragConst, shieldingConstant, heatingValue.
+ * dragConst, shieldingConstant, heatingValue.  The reference's other forces
+ * are in OtherForces.cpp.
  */
 #include <vector>
 
@@ -20,7 +21,6 @@ namespace F = demon_gb300::fits;
 int DeviceForce::precision = DM_FP64;
 
 void DeviceForce::evaluate(int stage, double currentTime) {
-    (void)currentTime;  // no in-scope force depends on time
     dm_force_params p{};
     if (!addDeviceParams(p))
         throw demon_gb300::Error(DM_ERR_UNSUPPORTED, "force cannot be evaluated on the device");
@@ -33,6 +33,7 @@ void DeviceForce::evaluate(int stage, double currentTime) {
                        ctx, "dm_cloud_upload");
     demon_gb300::check(dm_cloud_set_forces(s, &p), ctx, "dm_cloud_set_forces");
     demon_gb300::check(dm_cloud_set_step_counter(s, step), ctx, "dm_cloud_set_step_counter");
+    demon_gb300::check(dm_cloud_set_time(s, currentTime), ctx, "dm_cloud_set_time");
     std::vector<double> fx((size_t)cloud->n), fy((size_t)cloud->n);
     demon_gb300::check(dm_cloud_eval_forces_stage(s, precision, stage, fx.data(), fy.data()), ctx,
                        "dm_cloud_eval_forces_stage");
@@ -63,6 +64,9 @@ void ConfinementForce::readForce(fitsfile *const file, int *const error) {
 }
 
 bool ConfinementForce::addDeviceParams(dm_force_params &p) const {
+    // the device's ConfinementForceVoid term uses the same constant
+    if ((p.flags & DM_CONFINEMENT_VOID_FORCE) && !(p.flags & DM_CONFINEMENT_FORCE) && p.confine != confine)
+        return false;
     p.confine = (p.flags & DM_CONFINEMENT_FORCE) ? p.confine + confine : confine;
     p.flags |= DM_CONFINEMENT_FORCE;
     return true;
@@ -137,6 +141,10 @@ void ThermalForce::readForce(fitsfile *const file, int *const error) {
 
 bool ThermalForce::addDeviceParams(dm_force_params &p) const {
     if (p.flags & DM_THERMAL_FORCE) return false;
+    // every thermal force draws with one generator key and form
+    if ((p.flags & (DM_THERMAL_LOCALIZED_FORCE | DM_TIME_VARYING_THERMAL_FORCE)) &&
+        (p.thermal_mode != mode || p.seed != seed))
+        return false;
     p.flags |= DM_THERMAL_FORCE;
     p.heat = heatVal;
     p.thermal_mode = mode;

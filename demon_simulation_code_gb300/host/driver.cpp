@@ -4,10 +4,13 @@
  * library runs on the GPU, the same force set-up, output loop and time
  * accounting (driver.cpp:315-475), with the integration on the device.
  *
- * Forces: Confinement (unless -R), Drag and ShieldedCoulomb always, as in
- * the reference (driver.cpp:320-325); -R RectConfinement, -T Thermal.  The
- * reference's other forces (-B -D -E -F -G -L -S -v -V -w) and its RK2
- * integrator (-I) are refused with a message.
+ * Forces, as in the reference (driver.cpp:320-326, 372-402): Drag unless
+ * -D, Confinement unless -R or -V, ShieldedCoulomb always; -B Magnetic,
+ * -D TimeVaryingDrag, -E Electric, -F VertElectric, -G Gravitational,
+ * -L ThermalLocalized, -R RectConfinement, -S Rotational, -T Thermal,
+ * -v TimeVaryingThermal, -V ConfinementVoid, -w Driving, with the
+ * reference's conflict checks (driver.cpp:483-511).  The reference's RK2
+ * integrator (-I) is refused with a message.
  *
  * Options beyond the reference's:
  *   --precision fp64|fp32c   pair arithmetic (default fp64)
@@ -26,23 +29,37 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <initializer_list>
 #include <iostream>
 #include <string>
 #include <vector>
 
 #include "Cloud.h"
 #include "ConfinementForce.h"
+#include "ConfinementForceVoid.h"
 #include "Device.h"
 #include "DragForce.h"
+#include "DrivingForce.h"
+#include "ElectricForce.h"
+#include "GravitationalForce.h"
+#include "MagneticForce.h"
 #include "RectConfinementForce.h"
+#include "RotationalForce.h"
 #include "Runge_Kutta4.h"
 #include "ShieldedCoulombForce.h"
 #include "ThermalForce.h"
+#include "ThermalForceLocalized.h"
+#include "TimeVaryingDragForce.h"
+#include "TimeVaryingThermalForce.h"
+#include "VertElectricForce.h"
 
 namespace {
 
+// Defaults of the reference (driver.cpp:61-121).
 struct Settings {
     bool mach = false;
+    double voidDecay = 0.4;
+    double magneticFieldStrength = 1.0;
     double startTime = 0.0;
     double dataTimeStep = 0.01;
     double simTimeStep = 0.01 / 100.0;
@@ -53,12 +70,28 @@ struct Settings {
     double shieldingConstant = 2E4;
     double dragGamma = 10.0;
     double thermRed = 1E-14;
+    double thermRed1 = 1E-14;
+    double thermScale = 1E-14;
+    double thermOffset = 0.0;
+    double heatRadius = 0.001;
+    double driveConst = 0.00001;
+    double waveAmplitude = 1E-13;
+    double waveShift = 0.007;
     double machSpeed = 0.2;
     double massFactor = 100;
     double qMean = 6000.0;
     double qSigma = 100.0;
     double rMean = 1.45E-6;
     double rSigma = 0.0;
+    double rmin = 0.003 * 5.0;  // spacing*5 with the driver's spacing 0.003
+    double rmax = 0.003 * 10.0;
+    double rotConst = 1E-15;
+    double dragScale = -1.0;
+    double electricFieldStrength = 0;
+    double plasmaRadius = 1;
+    double vertElectricFieldStrength = 0;
+    double verticalDecay = 1;
+    double gravitationalFieldStrength = 0;
     force_flags usedForces = 0;
     cloud_index numParticles = 4;
     cloud_index row_x_particles = 4;
@@ -77,10 +110,43 @@ struct Settings {
     std::exit(1);
 }
 
-void refuseForce(char letter) {
-    fail(std::string("force option -") + letter +
-         " is not available in this build (GPU forces: Confinement, RectConfinement, Drag, "
-         "ShieldedCoulomb, Thermal)");
+// checkForce (driver.cpp:483-511): the first flag must not be set yet and
+// none of the others may be; then the first is set.
+void checkForce(Settings &s, char option, force_flags flag, const char *others = "",
+                std::initializer_list<force_flags> otherFlags = {}) {
+    if (s.usedForces & flag) fail(std::string("option -") + option + " already set");
+    size_t k = 0;
+    for (force_flags f : otherFlags) {
+        if (s.usedForces & f) fail(std::string("option -") + option + " conflicts with option -" + others[k]);
+        k++;
+    }
+    s.usedForces |= flag;
+}
+
+// The thermal options exclude one another (driver.cpp:908-915, 958-972).
+void checkThermal(Settings &s, char option) {
+    switch (option) {
+    case 'T': checkForce(s, 'T', ThermalForceFlag, "Lv", {ThermalForceLocalizedFlag, TimeVaryingThermalForceFlag}); break;
+    case 'L': checkForce(s, 'L', ThermalForceLocalizedFlag, "Tv", {ThermalForceFlag, TimeVaryingThermalForceFlag}); break;
+    default: checkForce(s, 'v', TimeVaryingThermalForceFlag, "LT", {ThermalForceLocalizedFlag, ThermalForceFlag}); break;
+    }
+}
+
+// The force letter of a forceFlags entry or command-line option.
+void useForce(Settings &s, char letter) {
+    switch (letter) {
+    case 'B': checkForce(s, 'B', MagneticForceFlag); break;
+    case 'D': checkForce(s, 'D', TimeVaryingDragForceFlag); break;
+    case 'E': checkForce(s, 'E', ElectricForceFlag); break;
+    case 'F': checkForce(s, 'F', VertElectricForceFlag); break;
+    case 'G': checkForce(s, 'G', GravitationalForceFlag); break;
+    case 'R': checkForce(s, 'R', RectConfinementForceFlag); break;
+    case 'S': checkForce(s, 'S', RotationalForceFlag); break;
+    case 'V': checkForce(s, 'V', ConfinementForceVoidFlag); break;
+    case 'w': checkForce(s, 'w', DrivingForceFlag); break;
+    case 'T': case 'L': case 'v': checkThermal(s, letter); break;
+    default: break;  // the reference ignores other entries
+    }
 }
 
 bool isNumber(const char *s) {
@@ -113,6 +179,16 @@ void help() {
               << " -s 2E4                 shielding constant [1/m]\n"
               << " -t 0.0001              simulation time step [s]\n"
               << " -T 1E-14               ThermalForce reduction factor [N]\n"
+              << " -B 1.0                 MagneticForce field [T]\n"
+              << " -D -1.0 10.0           TimeVaryingDragForce scale [Hz/s], offset [Hz]\n"
+              << " -E 0 1                 ElectricForce field [V/m^2], plasma radius [m]\n"
+              << " -F 0 1                 VertElectricForce field [V/m^2], decay [m]\n"
+              << " -G 0                   GravitationalForce field [m/s^2]\n"
+              << " -L 0.001 1E-14 1E-14   ThermalForceLocalized radius [m], inner, outer [N]\n"
+              << " -S 1E-15 0.015 0.03    RotationalForce strength [N], rmin, rmax [m]\n"
+              << " -v 1E-14 0             TimeVaryingThermalForce scale [N/s], offset [N]\n"
+              << " -V 0.4                 ConfinementForceVoid decay [1/m]\n"
+              << " -w 1E-13 0.007 1E-5    DrivingForce amplitude [N], shift [m], driving constant\n"
               << " --precision fp64|fp32c, --fixed-dt, --seed S, --thermal-mode 0|1,\n"
               << " --device D, --dry-run\n";
 }
@@ -136,6 +212,24 @@ void readParams(const std::string &path, Settings &s) {
         else if (name == "shieldingConstant") s.shieldingConstant = v;
         else if (name == "dragGamma") s.dragGamma = v;
         else if (name == "thermRed") s.thermRed = v;
+        else if (name == "thermRed1") s.thermRed1 = v;
+        else if (name == "thermScale") s.thermScale = v;
+        else if (name == "thermOffset") s.thermOffset = v;
+        else if (name == "heatRadius") s.heatRadius = v;
+        else if (name == "driveConst") s.driveConst = v;
+        else if (name == "waveAmplitude") s.waveAmplitude = v;
+        else if (name == "waveShift") s.waveShift = v;
+        else if (name == "voidDecay") s.voidDecay = v;
+        else if (name == "magneticFieldStrength") s.magneticFieldStrength = v;
+        else if (name == "rmin") s.rmin = v;
+        else if (name == "rmax") s.rmax = v;
+        else if (name == "rotConst") s.rotConst = v;
+        else if (name == "dragScale") s.dragScale = v;
+        else if (name == "electricFieldStrength") s.electricFieldStrength = v;
+        else if (name == "plasmaRadius") s.plasmaRadius = v;
+        else if (name == "vertElectricFieldStrength") s.vertElectricFieldStrength = v;
+        else if (name == "verticalDecay") s.verticalDecay = v;
+        else if (name == "gravitationalFieldStrength") s.gravitationalFieldStrength = v;
         else if (name == "machSpeed") s.machSpeed = v;
         else if (name == "massFactor") s.massFactor = v;
         else if (name == "qMean") s.qMean = v;
@@ -148,21 +242,18 @@ void readParams(const std::string &path, Settings &s) {
         else if (name == "velocityX") Cloud::velX = v;
         else if (name == "velocityY") Cloud::velY = v;
         else if (name == "forceFlags") {
-            // comma-separated letters, e.g. "R,T," (driver.cpp:756-822)
-            size_t start = 0;
-            while (start < value.size()) {
-                size_t comma = value.find(',', start);
-                const std::string f = value.substr(start, comma == std::string::npos ? std::string::npos
-                                                                                      : comma - start);
-                if (f == "R") s.usedForces |= RectConfinementForceFlag;
-                else if (f == "T") s.usedForces |= ThermalForceFlag;
-                else if (!f.empty()) refuseForce(f[0]);
+            // comma-terminated letters, e.g. "B,D," (driver.cpp:761-822): as in
+            // the reference an entry counts only while more than one
+            // character is left, so a last letter without its comma is dropped
+            std::string rest = value;
+            while (rest.size() > 1) {
+                const size_t comma = rest.find(',');
+                const std::string f = rest.substr(0, comma);
+                if (f.size() == 1) useForce(s, f[0]);
                 if (comma == std::string::npos) break;
-                start = comma + 1;
+                rest = rest.substr(comma + 1);
             }
         }
-        // the remaining keys parameterise forces this build does not run;
-        // they are accepted and ignored unless their force is requested
     }
 }
 
@@ -222,19 +313,66 @@ void parseArgs(int argc, char **argv, Settings &s) {
             case 'r': need(i, 2); s.rMean = std::atof(argv[++i]); s.rSigma = std::atof(argv[++i]); break;
             case 'R':
                 need(i, 2);
-                s.usedForces |= RectConfinementForceFlag;
+                useForce(s, 'R');
                 s.confinementConstX = std::atof(argv[++i]);
                 s.confinementConstY = std::atof(argv[++i]);
                 break;
             case 's': need(i, 1); s.shieldingConstant = std::atof(argv[++i]); break;
             case 't': need(i, 1); s.simTimeStep = std::atof(argv[++i]); break;
-            case 'T': need(i, 1); s.usedForces |= ThermalForceFlag; s.thermRed = std::atof(argv[++i]); break;
+            case 'T': need(i, 1); useForce(s, 'T'); s.thermRed = std::atof(argv[++i]); break;
             case 'd': need(i, 1); Cloud::dustParticleMassDensity = std::atof(argv[++i]); break;
             case 'i': need(i, 1); Cloud::interParticleSpacing = std::atof(argv[++i]); break;
             case 'p': need(i, 2); Cloud::justX = std::atof(argv[++i]); Cloud::justY = std::atof(argv[++i]); break;
             case 'k': need(i, 2); Cloud::velX = std::atof(argv[++i]); Cloud::velY = std::atof(argv[++i]); break;
-            case 'B': case 'D': case 'E': case 'F': case 'G': case 'L': case 'S': case 'v': case 'V': case 'w':
-                refuseForce(a[1]);
+            // the other forces' options (driver.cpp:878-1003)
+            case 'B': need(i, 1); useForce(s, 'B'); s.magneticFieldStrength = std::atof(argv[++i]); break;
+            case 'D':
+                need(i, 2);
+                useForce(s, 'D');
+                s.dragScale = std::atof(argv[++i]);
+                s.dragGamma = std::atof(argv[++i]);
+                break;
+            case 'E':
+                need(i, 2);
+                useForce(s, 'E');
+                s.electricFieldStrength = std::atof(argv[++i]);
+                s.plasmaRadius = std::atof(argv[++i]);
+                break;
+            case 'F':
+                need(i, 2);
+                useForce(s, 'F');
+                s.vertElectricFieldStrength = std::atof(argv[++i]);
+                s.verticalDecay = std::atof(argv[++i]);
+                break;
+            case 'G': need(i, 1); useForce(s, 'G'); s.gravitationalFieldStrength = std::atof(argv[++i]); break;
+            case 'L':
+                need(i, 3);
+                useForce(s, 'L');
+                s.heatRadius = std::atof(argv[++i]);
+                s.thermRed = std::atof(argv[++i]);
+                s.thermRed1 = std::atof(argv[++i]);
+                break;
+            case 'S':
+                need(i, 3);
+                useForce(s, 'S');
+                s.rotConst = std::atof(argv[++i]);
+                s.rmin = std::atof(argv[++i]);
+                s.rmax = std::atof(argv[++i]);
+                break;
+            case 'v':
+                need(i, 2);
+                useForce(s, 'v');
+                s.thermScale = std::atof(argv[++i]);
+                s.thermOffset = std::atof(argv[++i]);
+                break;
+            case 'V': need(i, 1); useForce(s, 'V'); s.voidDecay = std::atof(argv[++i]); break;
+            case 'w':
+                need(i, 3);
+                useForce(s, 'w');
+                s.waveAmplitude = std::atof(argv[++i]);
+                s.waveShift = std::atof(argv[++i]);
+                s.driveConst = std::atof(argv[++i]);
+                break;
             default: fail("unknown option " + a + " (-h for help)");
             }
         } else {
@@ -251,8 +389,11 @@ int main(int argc, char **argv) {
     parseArgs(argc, argv, s);
     RandomNumbers::seed = s.seed;
     if (s.device >= 0) demon_gb300::context(s.device);  // make it the process's device
-    if (!(s.usedForces & RectConfinementForceFlag)) s.usedForces |= ConfinementForceFlag;
-    s.usedForces |= DragForceFlag | ShieldedCoulombForceFlag;
+    // driver.cpp:322-326
+    if (!(s.usedForces & TimeVaryingDragForceFlag)) s.usedForces |= DragForceFlag;
+    if (!(s.usedForces & RectConfinementForceFlag) && !(s.usedForces & ConfinementForceVoidFlag))
+        s.usedForces |= ConfinementForceFlag;
+    s.usedForces |= ShieldedCoulombForceFlag;
 
     namespace F = demon_gb300::fits;
     int error = 0;
@@ -275,18 +416,35 @@ int main(int argc, char **argv) {
     if (s.continueFile.empty()) file = F::create(s.outputFile, error);
     if (error) fail("FITS error " + std::to_string(error) + " creating " + s.outputFile);
 
-    const force_flags known = ConfinementForceFlag | DragForceFlag | ShieldedCoulombForceFlag | ThermalForceFlag |
-                              RectConfinementForceFlag;
-    if (s.usedForces & ~known) fail("the input file uses forces this build does not run");
+    if (s.usedForces & ~(force_flags)32767) fail("the input file sets unknown force flags");
 
-    // driver.cpp:372-402 order
+    // driver.cpp:372-402, same order and constructor arguments; a continued
+    // file's FORCES picks them, so a file written with -D, -V or -v (which
+    // also set the Drag, Confinement or Thermal bit, TimeVaryingDragForce.cpp:51,
+    // ConfinementForceVoid.cpp:66, TimeVaryingThermalForce.cpp:53) continues
+    // with both forces, as in the reference
+    const force_flags u = s.usedForces;
     ForceArray forces;
-    if (s.usedForces & ConfinementForceFlag) forces.push_back(new ConfinementForce(cloud, s.confinementConst));
-    if (s.usedForces & DragForceFlag) forces.push_back(new DragForce(cloud, s.dragGamma));
-    if (s.usedForces & RectConfinementForceFlag)
+    if (u & ConfinementForceFlag) forces.push_back(new ConfinementForce(cloud, s.confinementConst));
+    if (u & ConfinementForceVoidFlag)
+        forces.push_back(new ConfinementForceVoid(cloud, s.confinementConst, s.voidDecay));
+    if (u & DragForceFlag) forces.push_back(new DragForce(cloud, s.dragGamma));
+    if (u & DrivingForceFlag) forces.push_back(new DrivingForce(cloud, s.driveConst, s.waveAmplitude, s.waveShift));
+    if (u & MagneticForceFlag) forces.push_back(new MagneticForce(cloud, s.magneticFieldStrength));
+    if (u & RectConfinementForceFlag)
         forces.push_back(new RectConfinementForce(cloud, s.confinementConstX, s.confinementConstY));
-    if (s.usedForces & ShieldedCoulombForceFlag) forces.push_back(new ShieldedCoulombForce(cloud, s.shieldingConstant));
-    if (s.usedForces & ThermalForceFlag) forces.push_back(new ThermalForce(cloud, s.thermRed, s.thermalMode, s.seed));
+    if (u & RotationalForceFlag) forces.push_back(new RotationalForce(cloud, s.rmin, s.rmax, s.rotConst));
+    if (u & ShieldedCoulombForceFlag) forces.push_back(new ShieldedCoulombForce(cloud, s.shieldingConstant));
+    if (u & ThermalForceFlag) forces.push_back(new ThermalForce(cloud, s.thermRed, s.thermalMode, s.seed));
+    if (u & ThermalForceLocalizedFlag)
+        forces.push_back(new ThermalForceLocalized(cloud, s.thermRed, s.thermRed1, s.heatRadius, s.thermalMode, s.seed));
+    if (u & TimeVaryingDragForceFlag) forces.push_back(new TimeVaryingDragForce(cloud, s.dragScale, s.dragGamma));
+    if (u & TimeVaryingThermalForceFlag)
+        forces.push_back(new TimeVaryingThermalForce(cloud, s.thermScale, s.thermOffset, s.thermalMode, s.seed));
+    if (u & ElectricForceFlag) forces.push_back(new ElectricForce(cloud, s.electricFieldStrength, s.plasmaRadius));
+    if (u & GravitationalForceFlag) forces.push_back(new GravitationalForce(cloud, s.gravitationalFieldStrength));
+    if (u & VertElectricForceFlag)
+        forces.push_back(new VertElectricForce(cloud, s.vertElectricFieldStrength, s.verticalDecay));
 
     if (!s.continueFile.empty()) {
         for (Force *const f : forces) f->readForce(file, &error);

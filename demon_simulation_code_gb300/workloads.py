@@ -26,11 +26,31 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+# ForceFlag bits (Force.h:75-91)
 CONFINEMENT = 1
 DRAG = 2
 SHIELDED_COULOMB = 4
+GRAVITATIONAL = 8
 THERMAL = 16
+THERMAL_LOCALIZED = 32
+DRIVING = 64
+ROTATIONAL = 128
+TIME_VARYING_DRAG = 256
+TIME_VARYING_THERMAL = 512
+MAGNETIC = 1024
+CONFINEMENT_VOID = 2048
+ELECTRIC = 4096
 RECT_CONFINEMENT = 8192
+VERT_ELECTRIC = 16384
+
+# Parameters of the reference's other forces for the parity cases: the
+# driver's defaults (driver.cpp:73-105) where they act on a 2 cm cloud, and
+# field strengths large enough to matter next to the confinement force.
+OTHER_FORCES = dict(void_decay=0.4, drive_const=1e-5, drive_amplitude=1e-13, drive_shift=0.007,
+                    magnetic=1.0, rot_rmin=0.005, rot_rmax=0.012, rot_const=1e-15, heat_in=1e-14,
+                    heat_out=3e-14, heat_radius=0.01, drag_scale=-1.0, drag_offset=3.0,
+                    heat_scale=1e-14, heat_offset=2e-14, electric=1e5, electric_radius=0.01,
+                    gravity=-9.8, vert_electric=1e5, vert_decay=0.02)
 
 Q_DUST = -1.6e-15
 M_DUST = 2.81e-14
@@ -55,6 +75,7 @@ class Cloud:
     heat: float = 0.0
     thermal_mode: int = 1
     seed: int = 0
+    extra: dict = field(default_factory=dict)  # the other forces' dm_force_params fields
 
     @property
     def n(self) -> int:
@@ -63,10 +84,10 @@ class Cloud:
     def params(self) -> dict:
         return dict(flags=self.flags, shielding=self.shielding, confine=self.confine,
                     confine_x=self.confine_x, confine_y=self.confine_y, gamma=self.gamma,
-                    heat=self.heat, thermal_mode=self.thermal_mode, seed=self.seed)
+                    heat=self.heat, thermal_mode=self.thermal_mode, seed=self.seed, **self.extra)
 
     def copy(self) -> "Cloud":
-        c = Cloud(**{k: (v.copy() if isinstance(v, np.ndarray) else v)
+        c = Cloud(**{k: (v.copy() if isinstance(v, (np.ndarray, dict)) else v)
                      for k, v in self.__dict__.items()})
         return c
 

@@ -57,10 +57,20 @@ typedef enum dm_precision {
 #define DM_CONFINEMENT_FORCE       1LL
 #define DM_DRAG_FORCE              2LL
 #define DM_SHIELDED_COULOMB_FORCE  4LL
+#define DM_GRAVITATIONAL_FORCE     8LL
 #define DM_THERMAL_FORCE           16LL
+#define DM_THERMAL_LOCALIZED_FORCE 32LL
+#define DM_DRIVING_FORCE           64LL
+#define DM_ROTATIONAL_FORCE        128LL
+#define DM_TIME_VARYING_DRAG_FORCE 256LL
+#define DM_TIME_VARYING_THERMAL_FORCE 512LL
+#define DM_MAGNETIC_FORCE          1024LL
+#define DM_CONFINEMENT_VOID_FORCE  2048LL
+#define DM_ELECTRIC_FORCE          4096LL
 #define DM_RECT_CONFINEMENT_FORCE  8192LL
+#define DM_VERT_ELECTRIC_FORCE     16384LL
 
-/* Parameters of the in-scope forces; one struct replaces the constructor
+/* Parameters of the forces; one struct replaces the constructor
  * arguments of ConfinementForce (ConfinementForce.h:15-16),
  * RectConfinementForce (RectConfinementForce.h:18-19), DragForce
  * (DragForce.h:16-17), ShieldedCoulombForce (ShieldedCoulombForce.h:17) and
@@ -77,6 +87,30 @@ typedef struct dm_force_params {
                                1: Gaussian N(0, heat^2) per axis */
     int reserved;           /* must be 0 */
     uint64_t seed;          /* thermal RNG key (Philox4x32-10, counter = particle, step, stage) */
+    /* the reference's other per-particle forces (driver.cpp:372-402), each
+     * evaluated at the substep's positions, velocities and force time */
+    double void_decay;      /* ConfinementForceVoid(C, confine, voidDecay): the confinement force
+                               plus F += q*(-decay)*exp(-decay*r)/r*(x, y)
+                               (ConfinementForceVoid.cpp:48-55) */
+    double drive_const;     /* DrivingForce(C, driveConst, amplitude, shift): */
+    double drive_amplitude; /*   F_x += amplitude*sin(x*2pi/2mm - t*2pi*10Hz)*exp(0/driveConst) */
+    double drive_shift;     /*   (DrivingForce.cpp:52-61) */
+    double magnetic;        /* MagneticForce(C, B): F += q*B*(vy, -vx) (MagneticForce.cpp:48-54) */
+    double rot_rmin;        /* RotationalForce(C, rmin, rmax, c): for rmin < r < rmax */
+    double rot_rmax;        /*   F += c*(-y, x)/r (RotationalForce.cpp:50-66) */
+    double rot_const;
+    double heat_in;         /* ThermalForceLocalized(C, heatIn, heatOut, radius): a thermal kick */
+    double heat_out;        /*   of scale heatIn for r < radius, heatOut beyond */
+    double heat_radius;     /*   (ThermalForceLocalized.cpp:124-133) */
+    double drag_scale;      /* TimeVaryingDragForce(C, scale, offset): DragForce with */
+    double drag_offset;     /*   dragConst = -(scale*t + offset) (TimeVaryingDragForce.cpp:11-40) */
+    double heat_scale;      /* TimeVaryingThermalForce(C, scale, offset): ThermalForce with */
+    double heat_offset;     /*   heat = scale*t + offset (TimeVaryingThermalForce.cpp:14-42) */
+    double electric;        /* ElectricForce(C, E, R): F += q*E*exp(r/(-R))*(x, y) */
+    double electric_radius; /*   (ElectricForce.cpp:48-62) */
+    double gravity;         /* GravitationalForce(C, g): F_y += m*g (GravitationalForce.cpp:46-50) */
+    double vert_electric;   /* VertElectricForce(C, E, d): F_y += q*E*exp(y/d) */
+    double vert_decay;      /*   (VertElectricForce.cpp:47-53) */
 } dm_force_params;
 
 typedef struct dm_ctx dm_ctx;
@@ -156,7 +190,9 @@ int dm_cloud_download(dm_cloud *cloud, double *x, double *y, double *vx,
 int dm_cloud_set_charge_mass(dm_cloud *cloud, const double *q, const double *m);
 
 /* Selects the forces and their parameters.  Replaces constructing the
- * ForceArray (driver.cpp:372-402, Force.h:71). */
+ * ForceArray (driver.cpp:372-402, Force.h:71): every ForceFlag of the
+ * reference is available and they are summed in the driver's order;
+ * bits outside the fifteen flags give DM_ERR_UNSUPPORTED. */
 int dm_cloud_set_forces(dm_cloud *cloud, const dm_force_params *params);
 
 /* One force evaluation of every enabled force at the current state, i.e.
@@ -178,8 +214,10 @@ int dm_cloud_eval_forces_device(dm_cloud *cloud, int precision, double *d_fx,
 /* Advances nsteps RK4 steps of fixed dt: Runge_Kutta4::moveParticles
  * (Runge_Kutta4.cpp:23-137) with CacheOperator (CacheOperator.cpp:18-73)
  * for an explicit step count, without the adaptive dt of line 25.
- * *t_inout (may be NULL) is advanced by dt per step with the reference's
- * accumulation (currentTime += dt). */
+ * With t_inout, the force time is set to *t_inout first and *t_inout is
+ * advanced by dt per step with the reference's accumulation (currentTime
+ * += dt); with NULL the steps continue from the cloud's force time
+ * (dm_cloud_set_time). */
 int dm_cloud_step(dm_cloud *cloud, int nsteps, double dt, int precision,
                   double *t_inout);
 
@@ -229,9 +267,18 @@ int dm_cloud_set_reorder_interval(dm_cloud *cloud, int steps);
  * N(N-1) ordered pairs per force evaluation either way.  No reference
  * counterpart (the reference tests every pair). */
 int dm_cloud_evaluated_pairs(dm_cloud *cloud, unsigned long long *pairs);
-/* RNG step counter used by ThermalForce (advanced by one per RK4 step). */
+/* RNG step counter used by the thermal forces (advanced by one per RK4 step). */
 int dm_cloud_set_step_counter(dm_cloud *cloud, uint64_t step);
 int dm_cloud_get_step_counter(dm_cloud *cloud, uint64_t *step);
+/* Force time, the reference's Integrator::currentTime (Integrator.h): RK4
+ * step k's stages see t, t + dt/2, t + dt/2, t + dt (Runge_Kutta4.cpp:30-88)
+ * and each step advances it by dt (Runge_Kutta4.cpp:135).  Only the
+ * time-dependent forces (DrivingForce, TimeVaryingDragForce,
+ * TimeVaryingThermalForce) read it; force-only evaluations
+ * (dm_cloud_eval_forces*) see the current time.  0 at creation;
+ * dm_cloud_move_particles sets it from *t_inout.  Set is stream-ordered. */
+int dm_cloud_set_time(dm_cloud *cloud, double t);
+int dm_cloud_get_time(dm_cloud *cloud, double *t);
 
 /* ---- many clouds in one launch --------------------------------------- */
 
@@ -262,6 +309,9 @@ int dm_batch_evaluated_pairs(dm_batch *batch, unsigned long long *pairs);
 /* The autotuned kernel variant, work-item count and persistent grid size. */
 int dm_batch_info(dm_batch *batch, char *variant, size_t len, int *nitems, int *grid);
 int dm_batch_set_step_counter(dm_batch *batch, uint64_t step);
+/* Force time shared by every cloud of the batch (see dm_cloud_set_time). */
+int dm_batch_set_time(dm_batch *batch, double t);
+int dm_batch_get_time(dm_batch *batch, double *t);
 
 /* ---- differentiable rollout ------------------------------------------ */
 

@@ -277,9 +277,13 @@ static void thermal_sincos(float u, float *sn, float *cs) {
     }
 }
 
-void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
-                    double *tx, double *ty) {
-    const uint32_t ctr[4] = {i, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)stage};
+/* One counter-based kick of magnitude scale `heat`: counter (i, step lo,
+ * step hi, stream).  Stream = stage for ThermalForce, stage + 16 for
+ * ThermalForceLocalized, stage + 32 for TimeVaryingThermalForce, so forces
+ * that are on together draw independent numbers. */
+static void thermal_draw(const or_params *p, uint32_t i, uint64_t step, int stream, double heat,
+                         double *tx, double *ty) {
+    const uint32_t ctr[4] = {i, (uint32_t)step, (uint32_t)(step >> 32), (uint32_t)stream};
     const uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
     uint32_t o[4];
     or_philox4x32_10(ctr, key, o);
@@ -287,11 +291,178 @@ void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
     const float u2 = u24(o[1]);
     float sn, cs;
     thermal_sincos(u2, &sn, &cs);
-    /* mode 0: ThermalForce::force (ThermalForce.cpp:118-122), heatVal*U*(cos, sin);
+    /* mode 0: ThermalForce::force (ThermalForce.cpp:118-140), heatVal*U*(cos, sin);
      * mode 1: Gaussian, sigma = heat per axis (Box-Muller) */
     const float amp = (p->thermal_mode == 0) ? u1 : sqrtf(-2.0f * thermal_log(u1));
-    *tx = p->heat * (double)(amp * cs);
-    *ty = p->heat * (double)(amp * sn);
+    *tx = heat * (double)(amp * cs);
+    *ty = heat * (double)(amp * sn);
+}
+
+void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
+                    double *tx, double *ty) {
+    thermal_draw(p, i, step, stage, p->heat, tx, ty);
+}
+
+/* ---------------------------------------------------------------------------
+ * The per-particle forces, one particle at a time.
+ *
+ * Each force adds into (*fx, *fy) exactly as the reference's force() adds
+ * into forceX/forceY with plusEqual_pd/minusEqual_pd; a particle's sum in
+ * the reference is the same sequence of additions whether the loops run
+ * force-major (the reference) or particle-major (here).
+ * ------------------------------------------------------------------------- */
+
+/* DrivingForce::waveNum, angFreq (DrivingForce.cpp:14-15). */
+static const double kWaveNum = 2.0 * M_PI / 0.002;
+static const double kAngFreq = 2.0 * M_PI * 10.0;
+
+typedef struct pstate {
+    uint32_t i;
+    double x, y, vx, vy, q, m;
+} pstate;
+
+/* ConfinementForce::force (ConfinementForce.cpp:48-54) */
+static inline void f_confinement(const or_params *p, const pstate *s, double *fx, double *fy) {
+    const double c = s->q * p->confine;
+    *fx += c * s->x;
+    *fy += c * s->y;
+}
+
+/* ConfinementForceVoid::force (ConfinementForceVoid.cpp:48-55), after the
+ * ConfinementForce term it inherits (ConfinementForceVoid.cpp:13-17):
+ * F += (q*(-decay)) * (exp(r*(-decay)) / r) * (x, y). */
+static inline void f_void(const or_params *p, const pstate *s, double *fx, double *fy) {
+    f_confinement(p, s, fx, fy);
+    const double decayV = s->q * -p->void_decay;
+    const double r = sqrt(s->x * s->x + s->y * s->y);
+    const double expR = exp(r * -p->void_decay) / r;
+    *fx += (decayV * expR) * s->x;
+    *fy += (decayV * expR) * s->y;
+}
+
+/* DragForce::force (DragForce.cpp:49-55) with dragConst */
+static inline void f_drag(double dragConst, const pstate *s, double *fx, double *fy) {
+    const double d = s->m * dragConst;
+    *fx += d * s->vx;
+    *fy += d * s->vy;
+}
+
+/* DrivingForce::force (DrivingForce.cpp:52-61): the stored driveConst is
+ * -drive_const (DrivingForce.h:17-18), so the exponent is
+ * (dist - dist) / drive_const: exp(+-0) = 1 for a finite position. */
+static inline void f_driving(const or_params *p, const pstate *s, double t, double *fx) {
+    const double driveConst = -p->drive_const;
+    const double distV = s->x - p->drive_shift;
+    const double sinArg = s->x * kWaveNum - t * kAngFreq;
+    const double expArg = (distV - distV) / -driveConst;
+    *fx += (sin(sinArg) * exp(expArg)) * p->drive_amplitude;
+}
+
+/* MagneticForce::force (MagneticForce.cpp:48-54): F = q*(v x B), B along z */
+static inline void f_magnetic(const or_params *p, const pstate *s, double *fx, double *fy) {
+    const double qB = s->q * p->magnetic;
+    *fx += qB * s->vy;
+    *fy -= qB * s->vx;
+}
+
+/* RectConfinementForce::force (RectConfinementForce.cpp:50-59) */
+static inline void f_rect(const or_params *p, const pstate *s, double *fx, double *fy) {
+    *fx += (s->q * p->confine_x) * s->x;
+    *fy += (s->q * p->confine_y) * s->y;
+}
+
+/* RotationalForce::force (RotationalForce.cpp:50-66): inside rmin < r < rmax,
+ * F -= c*y/r along x and F += c*x/r along y. */
+static inline void f_rotational(const or_params *p, const pstate *s, double *fx, double *fy) {
+    const double r = sqrt(s->x * s->x + s->y * s->y);
+    if (!(r > p->rot_rmin && r < p->rot_rmax)) return;
+    *fx -= (p->rot_const * s->y) / r;
+    *fy += (p->rot_const * s->x) / r;
+}
+
+/* ThermalForceLocalized::force (ThermalForceLocalized.cpp:124-133): heatVal1
+ * (heat_in) inside r < heatingRadius, heatVal2 (heat_out) outside. */
+static inline void f_thermal_localized(const or_params *p, const pstate *s, uint64_t step, int stage,
+                                       double *fx, double *fy) {
+    const double r = sqrt(s->x * s->x + s->y * s->y);
+    const double heat = (r < p->heat_radius) ? p->heat_in : p->heat_out;
+    double tx, ty;
+    thermal_draw(p, s->i, step, stage + 16, heat, &tx, &ty);
+    *fx += tx;
+    *fy += ty;
+}
+
+/* TimeVaryingThermalForce: heatVal = heatValScale*t + heatValOffset
+ * (TimeVaryingThermalForce.cpp:14-44), then ThermalForce's kick. */
+static inline void f_thermal_tv(const or_params *p, const pstate *s, double t, uint64_t step, int stage,
+                                double *fx, double *fy) {
+    const double heat = p->heat_scale * t + p->heat_offset;
+    double tx, ty;
+    thermal_draw(p, s->i, step, stage + 32, heat, &tx, &ty);
+    *fx += tx;
+    *fy += ty;
+}
+
+/* ElectricForce::force (ElectricForce.cpp:48-62): F = q*E*exp(r/(-R))*(x, y) */
+static inline void f_electric(const or_params *p, const pstate *s, double *fx, double *fy) {
+    const double cV = s->q * p->electric;
+    const double R = sqrt(s->x * s->x + s->y * s->y);
+    const double eV = cV * exp(R / (p->electric_radius * (-1)));
+    *fx += eV * s->x;
+    *fy += eV * s->y;
+}
+
+/* GravitationalForce::force (GravitationalForce.cpp:46-50): Fy += m*g */
+static inline void f_gravity(const or_params *p, const pstate *s, double *fy) {
+    *fy += s->m * p->gravity;
+}
+
+/* VertElectricForce::force (VertElectricForce.cpp:47-53): Fy += q*E*exp(y/d) */
+static inline void f_vert_electric(const or_params *p, const pstate *s, double *fy) {
+    const double cV = s->q * p->vert_electric;
+    *fy += cV * exp(s->y / p->vert_decay);
+}
+
+/* The forces the driver pushes before ShieldedCoulomb (driver.cpp:373-386):
+ * Confinement, ConfinementVoid, Drag, Driving, Magnetic, RectConfinement,
+ * Rotational. */
+static void forces_before_pairs(const or_params *p, const pstate *s, double t, double *fx, double *fy) {
+    const long long fl = p->flags;
+    if (fl & OR_CONFINEMENT_FORCE) f_confinement(p, s, fx, fy);
+    if (fl & OR_CONFINEMENT_VOID_FORCE) f_void(p, s, fx, fy);
+    if (fl & OR_DRAG_FORCE) f_drag(-p->gamma, s, fx, fy);  /* dragConst = -gamma (DragForce.h:16-17) */
+    if (fl & OR_DRIVING_FORCE) f_driving(p, s, t, fx);
+    if (fl & OR_MAGNETIC_FORCE) f_magnetic(p, s, fx, fy);
+    if (fl & OR_RECT_CONFINEMENT_FORCE) f_rect(p, s, fx, fy);
+    if (fl & OR_ROTATIONAL_FORCE) f_rotational(p, s, fx, fy);
+}
+
+/* The forces pushed after it (driver.cpp:389-402): Thermal,
+ * ThermalLocalized, TimeVaryingDrag, TimeVaryingThermal, Electric,
+ * Gravitational, VertElectric. */
+static void forces_after_pairs(const or_params *p, const pstate *s, double t, uint64_t step, int stage,
+                               double *fx, double *fy) {
+    const long long fl = p->flags;
+    if (fl & OR_THERMAL_FORCE) {
+        double tx, ty;
+        or_thermal_one(p, s->i, step, stage, &tx, &ty);
+        *fx += tx;
+        *fy += ty;
+    }
+    if (fl & OR_THERMAL_LOCALIZED_FORCE) f_thermal_localized(p, s, step, stage, fx, fy);
+    /* TimeVaryingDragForce: dragConst = -(scaleConst*t + offsetConst)
+     * (TimeVaryingDragForce.cpp:14-38), then DragForce's force */
+    if (fl & OR_TIME_VARYING_DRAG_FORCE) f_drag(-(p->drag_scale * t + p->drag_offset), s, fx, fy);
+    if (fl & OR_TIME_VARYING_THERMAL_FORCE) f_thermal_tv(p, s, t, step, stage, fx, fy);
+    if (fl & OR_ELECTRIC_FORCE) f_electric(p, s, fx, fy);
+    if (fl & OR_GRAVITATIONAL_FORCE) f_gravity(p, s, fy);
+    if (fl & OR_VERT_ELECTRIC_FORCE) f_vert_electric(p, s, fy);
+}
+
+static inline pstate particle(int i, const double *xs, const double *ys, const double *vxs,
+                              const double *vys, const double *q, const double *m) {
+    pstate s = {(uint32_t)i, xs[i], ys[i], vxs[i], vys[i], q[i], m[i]};
+    return s;
 }
 
 /* ---------------------------------------------------------------------------
@@ -301,27 +472,15 @@ void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
 void or_forces_rows(int n, const double *xs, const double *ys,
                     const double *vxs, const double *vys, const double *q,
                     const double *m, const or_params *p, uint64_t step,
-                    int stage, int nrows, const int *rows, double *fx,
+                    int stage, double t, int nrows, const int *rows, double *fx,
                     double *fy, int nthreads) {
     const double C = or_coulomb();
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads > 0 ? nthreads : 1)
     for (int k = 0; k < nrows; k++) {
         const int i = rows[k];
+        const pstate s = particle(i, xs, ys, vxs, vys, q, m);
         double sx = 0.0, sy = 0.0;
-        if (p->flags & OR_CONFINEMENT_FORCE) {
-            const double c = q[i] * p->confine;
-            sx += c * xs[i];
-            sy += c * ys[i];
-        }
-        if (p->flags & OR_DRAG_FORCE) {
-            const double d = m[i] * -p->gamma;
-            sx += d * vxs[i];
-            sy += d * vys[i];
-        }
-        if (p->flags & OR_RECT_CONFINEMENT_FORCE) {
-            sx += (q[i] * p->confine_x) * xs[i];
-            sy += (q[i] * p->confine_y) * ys[i];
-        }
+        forces_before_pairs(p, &s, t, &sx, &sy);
         if (p->flags & OR_SHIELDED_COULOMB_FORCE) {
             double px = 0.0, py = 0.0;
             for (int j = 0; j < n; j++) {
@@ -338,12 +497,7 @@ void or_forces_rows(int n, const double *xs, const double *ys,
             sx += px;
             sy += py;
         }
-        if (p->flags & OR_THERMAL_FORCE) {
-            double tx, ty;
-            or_thermal_one(p, (uint32_t)i, step, stage, &tx, &ty);
-            sx += tx;
-            sy += ty;
-        }
+        forces_after_pairs(p, &s, t, step, stage, &sx, &sy);
         fx[k] = sx;
         fy[k] = sy;
     }
@@ -351,34 +505,15 @@ void or_forces_rows(int n, const double *xs, const double *ys,
 
 void or_forces(int n, const double *xs, const double *ys, const double *vxs,
                const double *vys, const double *q, const double *m,
-               const or_params *p, uint64_t step, int stage, double *fx,
+               const or_params *p, uint64_t step, int stage, double t, double *fx,
                double *fy, int nthreads) {
-    for (int i = 0; i < n; i++) { fx[i] = 0.0; fy[i] = 0.0; }
-    /* driver.cpp:372-402 push order: Confinement, Drag, RectConfinement,
-     * ShieldedCoulomb, Thermal. */
-    if (p->flags & OR_CONFINEMENT_FORCE) {
-        /* ConfinementForce::force (ConfinementForce.cpp:48-54) */
-        for (int i = 0; i < n; i++) {
-            const double c = q[i] * p->confine;
-            fx[i] += c * xs[i];
-            fy[i] += c * ys[i];
-        }
-    }
-    if (p->flags & OR_DRAG_FORCE) {
-        /* DragForce::force (DragForce.cpp:49-55), dragConst = -gamma (DragForce.h:16-17) */
-        const double dragConst = -p->gamma;
-        for (int i = 0; i < n; i++) {
-            const double d = m[i] * dragConst;
-            fx[i] += d * vxs[i];
-            fy[i] += d * vys[i];
-        }
-    }
-    if (p->flags & OR_RECT_CONFINEMENT_FORCE) {
-        /* RectConfinementForce::force (RectConfinementForce.cpp:50-59) */
-        for (int i = 0; i < n; i++) {
-            fx[i] += (q[i] * p->confine_x) * xs[i];
-            fy[i] += (q[i] * p->confine_y) * ys[i];
-        }
+    /* driver.cpp:372-402 push order; the pair force adds pair by pair into
+     * the running sums (ShieldedCoulombForce.cpp:154-159, 193-198) */
+    for (int i = 0; i < n; i++) {
+        const pstate s = particle(i, xs, ys, vxs, vys, q, m);
+        fx[i] = 0.0;
+        fy[i] = 0.0;
+        forces_before_pairs(p, &s, t, &fx[i], &fy[i]);
     }
     if (p->flags & OR_SHIELDED_COULOMB_FORCE) {
         if (nthreads == 1)
@@ -386,13 +521,9 @@ void or_forces(int n, const double *xs, const double *ys, const double *vxs,
         else
             or_shielded_coulomb_omp(n, xs, ys, q, p->shielding, fx, fy, nthreads);
     }
-    if (p->flags & OR_THERMAL_FORCE) {
-        for (int i = 0; i < n; i++) {
-            double tx, ty;
-            or_thermal_one(p, (uint32_t)i, step, stage, &tx, &ty);
-            fx[i] += tx;
-            fy[i] += ty;
-        }
+    for (int i = 0; i < n; i++) {
+        const pstate s = particle(i, xs, ys, vxs, vys, q, m);
+        forces_after_pairs(p, &s, t, step, stage, &fx[i], &fy[i]);
     }
 }
 
@@ -434,8 +565,10 @@ static int rk_work_alloc(rk_work *w, int n) {
 /* One RK4 step with a given dt (Runge_Kutta4.cpp:26-135 after line 25). */
 static void rk4_one_step(int n, double *x, double *y, double *vx, double *vy,
                          const double *q, const double *m, const or_params *p,
-                         double dt, uint64_t step, int nthreads, rk_work *w) {
+                         double t, double dt, uint64_t step, int nthreads, rk_work *w) {
     for (int s = 0; s < 4; s++) {
+        /* force times t, t + dt/2.0, t + dt/2.0, t + dt (Runge_Kutta4.cpp:30-88) */
+        const double ts = (s == 0) ? t : (s == 3) ? t + dt : t + dt / 2.0;
         const double *xs, *ys, *vxs, *vys;
         if (s == 0) {
             /* operation1 is a no-op (CacheOperator.cpp:18-20): stage 1 reads x, Vx */
@@ -461,7 +594,7 @@ static void rk4_one_step(int n, double *x, double *y, double *vx, double *vy,
             }
             xs = w->xc; ys = w->yc; vxs = w->vxc; vys = w->vyc;
         }
-        or_forces(n, xs, ys, vxs, vys, q, m, p, step, s + 1, w->fx, w->fy, nthreads);
+        or_forces(n, xs, ys, vxs, vys, q, m, p, step, s + 1, ts, w->fx, w->fy, nthreads);
         /* stage kernels (Runge_Kutta4.cpp:32-47 etc.):
          * k = (dt*Fx)/m, l = dt*Vx_stage, m = (dt*Fy)/m, n = dt*Vy_stage */
         for (int i = 0; i < n; i++) {
@@ -482,11 +615,14 @@ static void rk4_one_step(int n, double *x, double *y, double *vx, double *vy,
 
 void or_rk4_fixed(int n, double *x, double *y, double *vx, double *vy,
                   const double *q, const double *m, const or_params *p,
-                  double dt, int nsteps, uint64_t step0, int nthreads) {
+                  double t0, double dt, int nsteps, uint64_t step0, int nthreads) {
     rk_work w;
     if (rk_work_alloc(&w, n)) return;
-    for (int s = 0; s < nsteps; s++)
-        rk4_one_step(n, x, y, vx, vy, q, m, p, dt, step0 + (uint64_t)s, nthreads, &w);
+    double t = t0;
+    for (int s = 0; s < nsteps; s++) {
+        rk4_one_step(n, x, y, vx, vy, q, m, p, t, dt, step0 + (uint64_t)s, nthreads, &w);
+        t += dt;  /* Runge_Kutta4.cpp:135 */
+    }
     free(w.block);
 }
 
@@ -553,7 +689,78 @@ int or_rk4_move_particles(int n, double *x, double *y, double *vx, double *vy,
     while (t < end_time) {
         const double dt = or_modify_timestep(n, x, y, 1.0e-4f, init_dt);
         if (dt < 0.0) break;
-        rk4_one_step(n, x, y, vx, vy, q, m, p, dt, step0 + (uint64_t)steps, nthreads, &w);
+        rk4_one_step(n, x, y, vx, vy, q, m, p, t, dt, step0 + (uint64_t)steps, nthreads, &w);
+        t += dt;
+        steps++;
+    }
+    *t_inout = t;
+    free(w.block);
+    return steps;
+}
+
+/* ---------------------------------------------------------------------------
+ * RK2 (the midpoint method of Runge_Kutta2.cpp).
+ * ------------------------------------------------------------------------- */
+
+/* Runge_Kutta2::moveParticles one step (Runge_Kutta2.cpp:24-76): stage 1 at
+ * (x, Vx, t), k1 = (dt*F)/m, l1 = dt*Vx; CacheOperator::operation2 cache =
+ * 0.5*tidbit + base; stage 2 at the cache and t + dt/2.0; then
+ * Vx += k2, x += l2, Vy += m2, y += n2. */
+static void rk2_one_step(int n, double *x, double *y, double *vx, double *vy,
+                         const double *q, const double *m, const or_params *p,
+                         double t, double dt, uint64_t step, int nthreads, rk_work *w) {
+    or_forces(n, x, y, vx, vy, q, m, p, step, 1, t, w->fx, w->fy, nthreads);
+    for (int i = 0; i < n; i++) {
+        w->k[0][i] = (dt * w->fx[i]) / m[i];
+        w->l[0][i] = dt * vx[i];
+        w->mm[0][i] = (dt * w->fy[i]) / m[i];
+        w->nn[0][i] = dt * vy[i];
+    }
+    for (int i = 0; i < n; i++) {
+        w->xc[i] = 0.5 * w->l[0][i] + x[i];
+        w->yc[i] = 0.5 * w->nn[0][i] + y[i];
+        w->vxc[i] = 0.5 * w->k[0][i] + vx[i];
+        w->vyc[i] = 0.5 * w->mm[0][i] + vy[i];
+    }
+    or_forces(n, w->xc, w->yc, w->vxc, w->vyc, q, m, p, step, 2, t + dt / 2.0, w->fx, w->fy, nthreads);
+    for (int i = 0; i < n; i++) {
+        const double k2 = (dt * w->fx[i]) / m[i];
+        const double l2 = dt * w->vxc[i];
+        const double m2 = (dt * w->fy[i]) / m[i];
+        const double n2 = dt * w->vyc[i];
+        vx[i] += k2;
+        x[i] += l2;
+        vy[i] += m2;
+        y[i] += n2;
+    }
+}
+
+void or_rk2_fixed(int n, double *x, double *y, double *vx, double *vy,
+                  const double *q, const double *m, const or_params *p,
+                  double t0, double dt, int nsteps, uint64_t step0, int nthreads) {
+    rk_work w;
+    if (rk_work_alloc(&w, n)) return;
+    double t = t0;
+    for (int s = 0; s < nsteps; s++) {
+        rk2_one_step(n, x, y, vx, vy, q, m, p, t, dt, step0 + (uint64_t)s, nthreads, &w);
+        t += dt;  /* Runge_Kutta2.cpp:76 */
+    }
+    free(w.block);
+}
+
+int or_rk2_move_particles(int n, double *x, double *y, double *vx, double *vy,
+                          const double *q, const double *m, const or_params *p,
+                          double init_dt, double *t_inout, double end_time,
+                          uint64_t step0, int nthreads) {
+    rk_work w;
+    if (rk_work_alloc(&w, n)) return -1;
+    int steps = 0;
+    double t = *t_inout;
+    /* Runge_Kutta2::moveParticles (Runge_Kutta2.cpp:23-78) */
+    while (t < end_time) {
+        const double dt = or_modify_timestep(n, x, y, 1.0e-4f, init_dt);
+        if (dt < 0.0) break;
+        rk2_one_step(n, x, y, vx, vy, q, m, p, t, dt, step0 + (uint64_t)steps, nthreads, &w);
         t += dt;
         steps++;
     }

@@ -28,11 +28,21 @@ extern "C" {
 #define OR_CONFINEMENT_FORCE       1LL
 #define OR_DRAG_FORCE              2LL
 #define OR_SHIELDED_COULOMB_FORCE  4LL
+#define OR_GRAVITATIONAL_FORCE     8LL
 #define OR_THERMAL_FORCE           16LL
+#define OR_THERMAL_LOCALIZED_FORCE 32LL
+#define OR_DRIVING_FORCE           64LL
+#define OR_ROTATIONAL_FORCE        128LL
+#define OR_TIME_VARYING_DRAG_FORCE 256LL
+#define OR_TIME_VARYING_THERMAL_FORCE 512LL
+#define OR_MAGNETIC_FORCE          1024LL
+#define OR_CONFINEMENT_VOID_FORCE  2048LL
+#define OR_ELECTRIC_FORCE          4096LL
 #define OR_RECT_CONFINEMENT_FORCE  8192LL
+#define OR_VERT_ELECTRIC_FORCE     16384LL
 
-/* Parameters of the in-scope forces.  Field layout is identical to
- * dm_force_params in include/demon_gb300.h. */
+/* Parameters of the forces.  Field layout is identical to dm_force_params
+ * in include/demon_gb300.h, which documents each field. */
 typedef struct or_params {
     long long flags;        /* ForceFlag bitmask */
     double shielding;       /* ShieldedCoulombForce::shielding, kappa [1/m] */
@@ -44,6 +54,10 @@ typedef struct or_params {
     int thermal_mode;       /* 0: heat*U(0,1)*(cos,sin)(U(0,2pi)); 1: N(0,heat^2) per axis */
     int reserved;
     uint64_t seed;          /* counter-based RNG key */
+    /* the reference's other per-particle forces (see dm_force_params) */
+    double void_decay, drive_const, drive_amplitude, drive_shift, magnetic, rot_rmin, rot_rmax, rot_const;
+    double heat_in, heat_out, heat_radius, drag_scale, drag_offset, heat_scale, heat_offset;
+    double electric, electric_radius, gravity, vert_electric, vert_decay;
 } or_params;
 
 /* Coulomb constant 1/(4 pi eps0) with eps0 = 8.8541878e-12
@@ -77,14 +91,18 @@ void or_thermal_one(const or_params *p, uint32_t i, uint64_t step, int stage,
 /* Philox4x32-10 block (exposed for known-answer tests). */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
-/* Sum of all enabled forces at the given stage positions/velocities, in the
- * reference driver's force order (driver.cpp:372-402): Confinement, Drag,
- * RectConfinement, ShieldedCoulomb, Thermal.  fx, fy are overwritten
- * (the reference zeroes forces after each stage, Runge_Kutta4.cpp:45-46). */
+/* Sum of all enabled forces at the given stage positions/velocities and
+ * force time t, in the reference driver's force order (driver.cpp:372-402):
+ * Confinement, ConfinementVoid, Drag, Driving, Magnetic, RectConfinement,
+ * Rotational, ShieldedCoulomb, Thermal, ThermalLocalized, TimeVaryingDrag,
+ * TimeVaryingThermal, Electric, Gravitational, VertElectric.  fx, fy are
+ * overwritten (the reference zeroes forces after each stage,
+ * Runge_Kutta4.cpp:45-46).  The three thermal forces draw counter-based
+ * kicks (or_thermal_one) on streams stage, stage + 16 and stage + 32. */
 void or_forces(int n, const double *xs, const double *ys,
                const double *vxs, const double *vys,
                const double *q, const double *m, const or_params *p,
-               uint64_t step, int stage, double *fx, double *fy, int nthreads);
+               uint64_t step, int stage, double t, double *fx, double *fy, int nthreads);
 
 /* The same total force for selected particles only (fx[k], fy[k] for
  * particle rows[k]), each row's pair sum in index order j = 0..n-1 with the
@@ -95,16 +113,17 @@ void or_forces(int n, const double *xs, const double *ys,
 void or_forces_rows(int n, const double *xs, const double *ys,
                     const double *vxs, const double *vys, const double *q,
                     const double *m, const or_params *p, uint64_t step,
-                    int stage, int nrows, const int *rows, double *fx,
+                    int stage, double t, int nrows, const int *rows, double *fx,
                     double *fy, int nthreads);
 
 /* Runge_Kutta4::moveParticles (Runge_Kutta4.cpp:23-137) with CacheOperator
  * (CacheOperator.cpp:18-73) and a FIXED dt (line 25's modifyTimeStep left out),
- * for an explicit step count.  x, y, vx, vy are updated in place.  step0 is
- * the RNG step index of the first step. */
+ * for an explicit step count from time t0 (stage force times t, t + dt/2,
+ * t + dt/2, t + dt; t += dt per step).  x, y, vx, vy are updated in place.
+ * step0 is the RNG step index of the first step. */
 void or_rk4_fixed(int n, double *x, double *y, double *vx, double *vy,
                   const double *q, const double *m, const or_params *p,
-                  double dt, int nsteps, uint64_t step0, int nthreads);
+                  double t0, double dt, int nsteps, uint64_t step0, int nthreads);
 
 /* Integrator::modifyTimeStep (Integrator.cpp:68-134): the FP32 distance test
  * over exactly the pairs the reference checks, returning the reduced dt.
@@ -119,6 +138,18 @@ float or_checked_min_dist(int n, const double *x, const double *y);
 /* Runge_Kutta4::moveParticles(endTime) including the adaptive dt, from
  * *t_inout until *t_inout >= end_time.  Returns the number of steps taken. */
 int or_rk4_move_particles(int n, double *x, double *y, double *vx, double *vy,
+                          const double *q, const double *m, const or_params *p,
+                          double init_dt, double *t_inout, double end_time,
+                          uint64_t step0, int nthreads);
+
+/* Runge_Kutta2::moveParticles (Runge_Kutta2.cpp:23-78), the midpoint
+ * method over the same forces and CacheOperator::operation2: fixed dt for an
+ * explicit step count from t0 (force times t, t + dt/2), and the adaptive
+ * form from *t_inout until end_time (returns the steps taken). */
+void or_rk2_fixed(int n, double *x, double *y, double *vx, double *vy,
+                  const double *q, const double *m, const or_params *p,
+                  double t0, double dt, int nsteps, uint64_t step0, int nthreads);
+int or_rk2_move_particles(int n, double *x, double *y, double *vx, double *vy,
                           const double *q, const double *m, const or_params *p,
                           double init_dt, double *t_inout, double end_time,
                           uint64_t step0, int nthreads);

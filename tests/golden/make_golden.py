@@ -24,6 +24,11 @@ from demon_simulation_code_gb300 import workloads as W  # noqa: E402
 Q = W.Q_DUST
 M = W.M_DUST
 
+OTHER_FORCES = W.OTHER_FORCES
+# ForceFlag bits of the forces the fixtures exercise one at a time (Force.h:75-91)
+EACH_FORCE = {"gravitational": 8, "driving": 64, "rotational": 128, "tv_drag": 256,
+              "magnetic": 1024, "void": 2048, "electric": 4096, "vert_electric": 16384}
+
 
 def disk(n, R, seed, vscale=0.0):
     rng = np.random.default_rng(seed)
@@ -81,6 +86,40 @@ def main():
                                         dt=np.float64(1e-4), end=np.float64(3e-4),
                                         steps=np.int64(steps), t1=np.float64(t1),
                                         x1=rx, y1=ry, vx1=rvx, vy1=rvy)
+    # 5. each of the reference's other deterministic forces alone, and two
+    # mixes with the pair force, at a non-zero force time
+    x, y, vx, vy = disk(256, 2e-2, 40, vscale=1e-3)
+    q = np.random.default_rng(41).normal(Q, abs(Q) * 0.05, 256)
+    m = np.full(256, M)
+    t = 0.0123
+    d = dict(x=x, y=y, vx=vx, vy=vy, q=q, m=m, t=np.float64(t))
+    mixes = {"mix_a": 2048 | 2 | 64 | 1024 | 128 | 4, "mix_b": 1 | 256 | 4096 | 8 | 16384 | 8192 | 4}
+    for name, flags in list(EACH_FORCE.items()) + list(mixes.items()):
+        p = oracle.make_params(flags=flags, shielding=2e4, confine=1e8, confine_x=1e8, confine_y=2e8,
+                               gamma=3.0, **OTHER_FORCES)
+        d[name + "_fx"], d[name + "_fy"] = ref.forces(x, y, vx, vy, q, m, p, t=t)
+        d[name + "_flags"] = np.int64(flags)
+    out["forces_other_t"] = d
+    # 6. fixed-dt RK4 from t0 = 0.05 with the time-dependent forces
+    c = W.calm_cloud(64, 3e-3, 30)
+    flags = 1 | 4 | 64 | 256 | 1024 | 128
+    p = oracle.make_params(flags=flags, shielding=c.shielding, confine=c.confine, **OTHER_FORCES)
+    rx, ry, rvx, rvy = ref.rk4_fixed(c.x, c.y, c.vx, c.vy, c.q, c.m, p, 1e-4, 25, t0=0.05)
+    out["rk4_fixed_time_n64"] = dict(x=c.x, y=c.y, vx=c.vx, vy=c.vy, q=c.q, m=c.m, dt=np.float64(1e-4),
+                                     steps=np.int64(25), t0=np.float64(0.05), flags=np.int64(flags),
+                                     kappa=np.float64(c.shielding), confine=np.float64(c.confine),
+                                     x1=rx, y1=ry, vx1=rvx, vy1=rvy)
+    # 7. the two other thermal forces' kicks from the reference itself (its
+    # RandomNumbers is clock-seeded, so only their distribution is pinned)
+    x, y, vx, vy = disk(4096, 2e-2, 50)
+    q = np.full(4096, Q)
+    m = np.full(4096, M)
+    d = dict(x=x, y=y)
+    for name, flags, tt in [("localized", 32, 0.0), ("tv", 512, 0.5)]:
+        p = oracle.make_params(flags=flags, **OTHER_FORCES)
+        d[name + "_fx"], d[name + "_fy"] = ref.forces(x, y, vx, vy, q, m, p, t=tt, thermal=True)
+        d[name + "_t"] = np.float64(tt)
+    out["thermal_other_ref"] = d
     for name, d in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(name, {k: np.shape(v) for k, v in d.items()})

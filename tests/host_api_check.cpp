@@ -1,12 +1,14 @@
 // host_api_check.cpp -- drives the C++ host classes the way the reference's
 // own code does, for tests/test_gpu_host.py.
 //
-//   host_api_check <in.bin> <out.bin> <mode> <nsteps> <dt> <precision>
+//   host_api_check <in.bin> <out.bin> <mode> <nsteps> <dt> <precision> [basic|other]
 //
-// in.bin: int32 n, then x, y, vx, vy, q, m (n doubles each).  Forces:
-// Confinement(1e4), Drag(3), ShieldedCoulomb(5e3), Thermal(1e-16, mode 1,
-// seed 5).  mode "fused": Runge_Kutta4::moveParticles with a fixed dt for
-// nsteps steps.  mode "host": the same steps written out as the reference's
+// in.bin: int32 n, then x, y, vx, vy, q, m (n doubles each).  Forces
+// "basic": Confinement(1e4), Drag(3), ShieldedCoulomb(5e3), Thermal(1e-16,
+// mode 1, seed 5), from t = 0.  Forces "other": the reference's other
+// forces around ShieldedCoulomb(5e3), from t = 0.3.  mode "fused":
+// Runge_Kutta4::moveParticles with a fixed dt for nsteps steps.  mode
+// "host": the same steps written out as the reference's
 // Runge_Kutta4::moveParticles loop (Runge_Kutta4.cpp:23-137) over the
 // per-force force1..4 calls and CacheOperator::operation1..4.  out.bin: x,
 // y, vx, vy after the steps (n doubles each).
@@ -18,16 +20,26 @@
 
 #include "CacheOperator.h"
 #include "ConfinementForce.h"
+#include "ConfinementForceVoid.h"
 #include "DragForce.h"
+#include "DrivingForce.h"
+#include "ElectricForce.h"
+#include "GravitationalForce.h"
+#include "MagneticForce.h"
+#include "RotationalForce.h"
 #include "Runge_Kutta4.h"
 #include "ShieldedCoulombForce.h"
 #include "ThermalForce.h"
+#include "ThermalForceLocalized.h"
+#include "TimeVaryingDragForce.h"
+#include "TimeVaryingThermalForce.h"
+#include "VertElectricForce.h"
 
 namespace {
 
-void host_rk4(Cloud *c, const ForceArray &forces, CacheOperator &op, double dt, int nsteps) {
+void host_rk4(Cloud *c, const ForceArray &forces, CacheOperator &op, double t0, double dt, int nsteps) {
     const int n = c->n;
-    double t = 0.0;
+    double t = t0;
     double *K[4] = {c->k1, c->k2, c->k3, c->k4}, *L[4] = {c->l1, c->l2, c->l3, c->l4};
     double *M[4] = {c->m1, c->m2, c->m3, c->m4}, *N[4] = {c->n1, c->n2, c->n3, c->n4};
     for (int s = 0; s < nsteps; s++) {
@@ -69,10 +81,11 @@ void host_rk4(Cloud *c, const ForceArray &forces, CacheOperator &op, double dt, 
 }  // namespace
 
 int main(int argc, char **argv) {
-    if (argc != 7) {
-        std::fprintf(stderr, "usage: %s in.bin out.bin fused|host nsteps dt fp64|fp32c\n", argv[0]);
+    if (argc != 7 && argc != 8) {
+        std::fprintf(stderr, "usage: %s in.bin out.bin fused|host nsteps dt fp64|fp32c [basic|other]\n", argv[0]);
         return 2;
     }
+    const bool other = argc == 8 && std::string(argv[7]) == "other";
     FILE *in = std::fopen(argv[1], "rb");
     int n = 0;
     if (!in || std::fread(&n, sizeof n, 1, in) != 1 || n < 1) return 2;
@@ -89,13 +102,27 @@ int main(int argc, char **argv) {
     DragForce drag(&cloud, 3.0);
     ShieldedCoulombForce coul(&cloud, 5e3);
     ThermalForce therm(&cloud, 1e-16, 1, 5);
-    ForceArray forces = {&conf, &drag, &coul, &therm};
+    // the reference's other forces, in driver.cpp:372-402 order
+    ConfinementForceVoid cvoid(&cloud, 1e4, 400.0);
+    DrivingForce drive(&cloud, 1e-5, 1e-15, 5e-4);
+    MagneticForce mag(&cloud, 0.5);
+    RotationalForce rot(&cloud, 2e-4, 1e-3, 1e-15);
+    ThermalForceLocalized tloc(&cloud, 1e-16, 3e-16, 5e-4, 1, 5);
+    TimeVaryingDragForce tvdrag(&cloud, -1.0, 3.0);
+    TimeVaryingThermalForce tvtherm(&cloud, 1e-16, 1e-16, 1, 5);
+    ElectricForce elec(&cloud, 1e3, 2e-3);
+    GravitationalForce grav(&cloud, -1.0);
+    VertElectricForce velec(&cloud, 1.0, 2e-3);
+    const ForceArray forces = other ? ForceArray{&cvoid, &drive, &mag, &rot, &coul, &tloc, &tvdrag, &tvtherm,
+                                                 &elec, &grav, &velec}
+                                    : ForceArray{&conf, &drag, &coul, &therm};
+    const double t0 = other ? 0.3 : 0.0;
     try {
         if (mode == "fused") {
-            Runge_Kutta4 I(&cloud, forces, dt, 0.0);
+            Runge_Kutta4 I(&cloud, forces, dt, t0);
             I.setAdaptiveTimeStep(false);
             I.setPrecision(prec);
-            I.moveParticles((nsteps - 0.5) * dt);
+            I.moveParticles(t0 + (nsteps - 0.5) * dt);
             if (I.stepsTaken() != nsteps) {
                 std::fprintf(stderr, "took %lld steps\n", I.stepsTaken());
                 return 3;
@@ -103,7 +130,7 @@ int main(int argc, char **argv) {
         } else {
             DeviceForce::precision = prec;
             CacheOperator op(&cloud);
-            host_rk4(&cloud, forces, op, dt, nsteps);
+            host_rk4(&cloud, forces, op, t0, dt, nsteps);
         }
     } catch (const demon_gb300::Error &e) {
         std::fprintf(stderr, "%s\n", e.what());

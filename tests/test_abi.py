@@ -43,8 +43,32 @@ def test_force_params_layout_matches_oracle():
 
     import oracle
 
-    assert ctypes.sizeof(_lib.ForceParams) == ctypes.sizeof(oracle.Params) == 72
+    assert ctypes.sizeof(_lib.ForceParams) == ctypes.sizeof(oracle.Params) == 232
     assert [f[0] for f in _lib.ForceParams._fields_] == [f[0] for f in oracle.Params._fields_]
+
+
+def test_force_params_layout_matches_c_header(tmp_path):
+    """ctypes' dm_force_params has the C compiler's size and field offsets."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = [f[0] for f in _lib.ForceParams._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "demon_gb300.h"\nint main(void) {\n'
+                   '  printf("%zu\\n", sizeof(dm_force_params));\n'
+                   + "".join(f'  printf("%zu\\n", offsetof(dm_force_params, {k}));\n' for k in names)
+                   + "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(_lib.ForceParams)
+    assert got[1:] == [getattr(_lib.ForceParams, k).offset for k in names]
 
 
 def test_workloads_are_seeded():

@@ -73,6 +73,28 @@ def test_driver_output_matches_oracle(host_build, oracle_lib, tmp_path):
     check_rows(ts, 1, rows)
 
 
+def test_driver_other_forces_match_oracle(host_build, oracle_lib, tmp_path):
+    """The reference's other force options through the driver, replayed on
+    the oracle with the same forces and the stage times of each step."""
+    _, driver = host_build
+    run(driver, *ARGS, "-V", "400", "-B", "0.5", "-D", "-1", "3", "-w", "1e-15", "5e-4", "1e-5", "-S", "1e-15",
+        "2e-4", "1e-3", "-G", "-1", "-E", "1e3", "2e-3", "-F", "1", "2e-3", "-e", "0.0016", "-O", "o.fits",
+        cwd=tmp_path)
+    keys, tables = read_fits(str(tmp_path / "o.fits"))
+    flags = 4 | 8 | 64 | 128 | 256 | 1024 | 2048 | 4096 | 16384
+    assert keys["FORCES"] == flags | 1 | 2  # -V and -D also set the Confinement and Drag bits
+    q, m = tables["CLOUD"]["CHARGE"].ravel(), tables["CLOUD"]["MASS"].ravel()
+    ts = tables["TIME_STEP"]
+    p = oracle.make_params(flags=flags, shielding=2e4, confine=1e4, void_decay=400.0, magnetic=0.5,
+                           drag_scale=-1.0, drag_offset=3.0, drive_amplitude=1e-15, drive_shift=5e-4,
+                           drive_const=1e-5, rot_const=1e-15, rot_rmin=2e-4, rot_rmax=1e-3, gravity=-1.0,
+                           electric=1e3, electric_radius=2e-3, vert_electric=1.0, vert_decay=2e-3)
+    state = [ts[k][0] for k in ("X_POSITION", "Y_POSITION", "X_VELOCITY", "Y_VELOCITY")]
+    rows = replay(oracle_lib, p, state, q, m, 0.0, 0.0016, 0.00053, 1e-4)
+    assert len(rows) == ts["TIME"].shape[0] - 1 == 4
+    check_rows(ts, 1, rows)
+
+
 def test_driver_continue_appends_like_the_reference(host_build, oracle_lib, tmp_path):
     _, driver = host_build
     run(driver, *ARGS, "-e", "0.001", "-O", "c.fits", cwd=tmp_path)
@@ -103,8 +125,9 @@ def api_check(host_build, tmp_path_factory):
     return exe
 
 
+@pytest.mark.parametrize("forces", ["basic", "other"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32c"])
-def test_per_force_calls_match_the_fused_step(api_check, tmp_path, prec):
+def test_per_force_calls_match_the_fused_step(api_check, tmp_path, prec, forces):
     c = W.calm_cloud(96)
     inp = tmp_path / "in.bin"
     with open(inp, "wb") as f:
@@ -114,7 +137,7 @@ def test_per_force_calls_match_the_fused_step(api_check, tmp_path, prec):
     out = {}
     for mode in ("fused", "host"):
         o = tmp_path / f"{mode}.bin"
-        r = subprocess.run([api_check, str(inp), str(o), mode, "8", "1e-4", prec], capture_output=True,
+        r = subprocess.run([api_check, str(inp), str(o), mode, "8", "1e-4", prec, forces], capture_output=True,
                            text=True, timeout=300)
         assert r.returncode == 0, r.stderr
         out[mode] = np.fromfile(o, dtype=np.float64).reshape(4, c.n)

@@ -1,7 +1,6 @@
 """The C++ host classes and the demon_gb300 driver, without a GPU: build,
 Params.cfg and command-line handling, the FITS output of the set-up, and the
-refusal of forces this build does not run (--dry-run stops before the first
-device call)."""
+force options' checks (--dry-run stops before the first device call)."""
 import os
 import subprocess
 
@@ -71,18 +70,67 @@ def test_command_line_overrides_and_defaults(host_build, tmp_path):
     assert tables["CLOUD"]["MASS"].shape == (16, 1)
 
 
-@pytest.mark.parametrize("args", [["-B", "1.0"], ["-I"], ["-V", "0.4"]])
-def test_driver_refuses_what_it_does_not_run(host_build, tmp_path, args):
+def test_driver_refuses_rk2(host_build, tmp_path):
     _, driver = host_build
-    r = run(driver, *args, "--dry-run", cwd=tmp_path)
+    r = run(driver, "-I", "--dry-run", cwd=tmp_path)
     assert r.returncode == 1 and "not available" in r.stderr
 
 
-def test_params_force_flag_outside_the_build_is_refused(host_build, tmp_path):
+def test_every_force_option_sets_its_flag_and_keys(host_build, tmp_path):
+    """The reference's force options (driver.cpp:878-1003) and the FITS keys
+    of each force's writeForce."""
     _, driver = host_build
-    (tmp_path / "p.cfg").write_text("forceFlags R,S,\n")
-    r = run(driver, "-P", "p.cfg", "--dry-run", cwd=tmp_path)
-    assert r.returncode == 1 and "-S" in r.stderr
+    r = run(driver, "-n", "16", "-B", "0.5", "-D", "-2.0", "7.0", "-E", "3.0", "0.02", "-F", "4.0", "0.03",
+            "-G", "-9.8", "-L", "0.002", "1e-14", "3e-14", "-S", "2e-15", "0.001", "0.004", "-V", "0.6",
+            "-w", "2e-13", "0.005", "2e-5", "-O", "f.fits", "--dry-run", cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    keys, _ = read_fits(str(tmp_path / "f.fits"))
+    # -D replaces Drag but its file entry sets the Drag bit too; -V replaces
+    # Confinement likewise (TimeVaryingDragForce.cpp:51, ConfinementForceVoid.cpp:66)
+    assert keys["FORCES"] == 1 | 2 | 4 | 8 | 32 | 64 | 128 | 256 | 1024 | 2048 | 4096 | 16384
+    assert keys["MAGNETICFIELD"] == 0.5
+    assert keys["TVDRAGSCALECONST"] == -2.0 and keys["TVDRAGOFFSETCONST"] == 7.0
+    assert keys["DRAGCONST"] == 7.0  # DragForce(C, -offset): dragConst = offset (TimeVaryingDragForce.h:16-17)
+    assert keys["ELECTRICFIELDSTRENGTH"] == 3.0 and keys["PLASMARADIUS"] == 0.02
+    assert keys["VERTELECTRICFIELDSTRENGTH"] == 4.0 and keys["VERTICALDECAY"] == 0.03
+    assert keys["GRAVITATIONALFIELDSTRENGTH"] == -9.8
+    assert keys["HEATINGVALUE1"] == 1e-14 and keys["HEATINGVALUE2"] == 3e-14 and keys["HEATINGRADIUS"] == 0.002
+    assert keys["ROTATIONALCONST"] == 2e-15 and keys["INNERRADIUS"] == 0.001 and keys["OUTERRADIUS"] == 0.004
+    assert keys["DECAY"] == 0.6 and "CONFINECONST" in keys
+    # the stored driving constant is minus the option's value (DrivingForce.h:17-18)
+    assert keys["DRIVINGAMPLITUDE"] == 2e-13 and keys["DRIVINGSHIFT"] == 0.005 and keys["DRIVINGCONST"] == -2e-5
+
+
+def test_time_varying_thermal_option(host_build, tmp_path):
+    _, driver = host_build
+    r = run(driver, "-n", "8", "-v", "2e-14", "1e-15", "-O", "v.fits", "--dry-run", cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    keys, _ = read_fits(str(tmp_path / "v.fits"))
+    assert keys["FORCES"] == 1 | 2 | 4 | 16 | 512
+    assert keys["HEATINGVALUESCALE"] == 2e-14 and keys["HEATINGVALUEOFFSET"] == 1e-15
+    assert keys["HEATINGVALUE"] == 1e-15
+
+
+@pytest.mark.parametrize("args,msg", [(["-T", "1e-14", "-L", "0.001", "1e-14", "1e-14"], "conflicts"),
+                                      (["-v", "1", "0", "-T", "1e-14"], "conflicts"),
+                                      (["-B", "1", "-B", "2"], "already set")])
+def test_force_option_conflicts_as_the_reference(host_build, tmp_path, args, msg):
+    _, driver = host_build
+    r = run(driver, *args, "--dry-run", cwd=tmp_path)
+    assert r.returncode == 1 and msg in r.stderr
+
+
+def test_params_force_flags_parse_like_the_reference(host_build, tmp_path):
+    """forceFlags entries are comma-terminated; as in the reference
+    (driver.cpp:764-769) a last letter without its comma is not read."""
+    _, driver = host_build
+    (tmp_path / "p.cfg").write_text("numParticles 8\nrotConst 3e-15\nrmin 0.002\nrmax 0.005\n"
+                                    "forceFlags R,S,G\n")
+    r = run(driver, "-P", "p.cfg", "-O", "p.fits", "--dry-run", cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    keys, _ = read_fits(str(tmp_path / "p.fits"))
+    assert keys["FORCES"] == 2 | 4 | 128 | 8192
+    assert keys["ROTATIONALCONST"] == 3e-15 and keys["INNERRADIUS"] == 0.002 and keys["OUTERRADIUS"] == 0.005
 
 
 def test_continue_reads_back_the_file(host_build, tmp_path):
@@ -92,6 +140,13 @@ def test_continue_reads_back_the_file(host_build, tmp_path):
     r = run(driver, "-c", "c.fits", "--dry-run", cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     assert (tmp_path / "c.fits").read_bytes() == before
+    # every force's keys read back
+    assert run(driver, "-n", "8", "-B", "2", "-S", "1e-15", "0.001", "0.002", "-D", "-1", "3", "-w", "1e-13",
+               "0.001", "1e-5", "-O", "d.fits", "--dry-run", cwd=tmp_path).returncode == 0
+    before = (tmp_path / "d.fits").read_bytes()
+    r = run(driver, "-c", "d.fits", "--dry-run", cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "d.fits").read_bytes() == before
 
 
 def test_host_api_check_compiles(host_build, tmp_path):

@@ -147,5 +147,108 @@ def test_modify_timestep_checked_pairs(oracle_lib):
     assert oracle_lib.modify_timestep(x, y, 1e-4) == pytest.approx(1e-4 / 1e3)
 
 
+# the reference's other forces (fixtures by tests/golden/make_golden.py)
+OTHER_FORCES = W.OTHER_FORCES
+OTHER_NAMES = ["gravitational", "driving", "rotational", "tv_drag", "magnetic", "void", "electric",
+               "vert_electric", "mix_a", "mix_b"]
+
+
+def other_params(flags):
+    return oracle.make_params(flags=flags, shielding=2e4, confine=1e8, confine_x=1e8, confine_y=2e8,
+                              gamma=3.0, **OTHER_FORCES)
+
+
+@pytest.mark.parametrize("name", OTHER_NAMES)
+def test_other_forces_match_reference_golden(oracle_lib, name):
+    g = load("forces_other_t")
+    p = other_params(int(g[name + "_flags"]))
+    fx, fy = oracle_lib.forces(g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"], p, t=float(g["t"]))
+    ex, ey = g[name + "_fx"], g[name + "_fy"]
+    assert np.any(ex != 0.0) or np.any(ey != 0.0)
+    # per-particle arithmetic in the reference's order: libm last-bit
+    # differences between machines at most
+    assert rel(fx, ex) < 1e-14 and rel(fy, ey) < 1e-14
+
+
+def test_other_forces_exercise_their_branches():
+    g = load("forces_other_t")
+    r = np.hypot(g["x"], g["y"])
+    inside = (r > OTHER_FORCES["rot_rmin"]) & (r < OTHER_FORCES["rot_rmax"])
+    assert 0 < inside.sum() < len(r)
+    # RotationalForce acts only inside its annulus
+    assert np.all(g["rotational_fx"][~inside] == 0.0) and np.all(g["rotational_fx"][inside] != 0.0)
+    # GravitationalForce is F_y = m*g, F_x = 0
+    assert np.all(g["gravitational_fx"] == 0.0)
+    np.testing.assert_array_equal(g["gravitational_fy"], g["m"] * OTHER_FORCES["gravity"])
+
+
+def test_rk4_with_force_time_matches_reference_golden(oracle_lib):
+    g = load("rk4_fixed_time_n64")
+    p = oracle.make_params(flags=int(g["flags"]), shielding=float(g["kappa"]), confine=float(g["confine"]),
+                           **OTHER_FORCES)
+    out = oracle_lib.rk4_fixed(g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"], p, float(g["dt"]),
+                               int(g["steps"]), t0=float(g["t0"]))
+    for a, k in zip(out, ("x1", "y1", "vx1", "vy1")):
+        assert rel(a, g[k]) < 1e-13, k
+    # the stage times matter: starting the same steps at t0 = 0 ends elsewhere
+    out0 = oracle_lib.rk4_fixed(g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"], p, float(g["dt"]),
+                                int(g["steps"]))
+    assert rel(out0[2], g["vx1"]) > 1e-6
+
+
+def test_other_forces_bit_exact_against_compiled_reference(oracle_lib, ref_lib):
+    rng = np.random.default_rng(9)
+    n = 128
+    x, y = W.uniform_disk(rng, n, 2e-2)
+    vx, vy = rng.normal(0, 1e-3, n), rng.normal(0, 1e-3, n)
+    q = rng.normal(W.Q_DUST, abs(W.Q_DUST) * 0.05, n)
+    m = np.full(n, W.M_DUST)
+    for flags in [8, 64, 128, 256, 1024, 2048, 4096, 16384, 32767 & ~(16 | 32 | 512)]:
+        for t in (0.0, 0.37):
+            p = other_params(flags)
+            a = ref_lib.forces(x, y, vx, vy, q, m, p, t=t)
+            b = oracle_lib.forces(x, y, vx, vy, q, m, p, t=t)
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (flags, t)
+    c = W.calm_cloud(64, 3e-3, 31)
+    p = oracle.make_params(flags=1 | 4 | 64 | 256 | 1024 | 128 | 2048, shielding=c.shielding,
+                           confine=c.confine, **OTHER_FORCES)
+    a = ref_lib.rk4_fixed(c.x, c.y, c.vx, c.vy, c.q, c.m, p, 1e-4, 12, t0=0.2)
+    b = oracle_lib.rk4_fixed(c.x, c.y, c.vx, c.vy, c.q, c.m, p, 1e-4, 12, t0=0.2)
+    assert all(np.array_equal(u, v) for u, v in zip(a, b))
+
+
+def _kick_stats(fx, fy, scale):
+    u = np.hypot(fx, fy) / scale
+    return u, np.arctan2(fy, fx)
+
+
+@pytest.mark.parametrize("kind", ["localized", "tv"])
+def test_other_thermal_kicks_match_reference_distribution(oracle_lib, kind):
+    """ThermalForceLocalized / TimeVaryingThermalForce: the reference's kicks
+    (clock-seeded) and the oracle's counter-based kicks have the same scale
+    per region / time and the same magnitude and angle distributions."""
+    from scipy import stats
+
+    g = load("thermal_other_ref")
+    n = len(g["x"])
+    flags = 32 if kind == "localized" else 512
+    t = float(g[kind + "_t"])
+    p = oracle.make_params(flags=flags, thermal_mode=0, seed=11, **OTHER_FORCES)
+    zeros = np.zeros(n)
+    fx, fy = oracle_lib.forces(g["x"], g["y"], zeros, zeros, np.full(n, W.Q_DUST), np.full(n, W.M_DUST),
+                               p, step=3, stage=2, t=t)
+    if kind == "localized":
+        inside = np.hypot(g["x"], g["y"]) < OTHER_FORCES["heat_radius"]
+        scale = np.where(inside, OTHER_FORCES["heat_in"], OTHER_FORCES["heat_out"])
+    else:
+        scale = np.full(n, OTHER_FORCES["heat_scale"] * t + OTHER_FORCES["heat_offset"])
+    ur, ar = _kick_stats(g[kind + "_fx"], g[kind + "_fy"], scale)
+    uo, ao = _kick_stats(fx, fy, scale)
+    for u in (ur, uo):
+        assert u.max() <= 1.0 + 1e-12 and abs(u.mean() - 0.5) < 0.03
+    assert stats.ks_2samp(ur, uo).pvalue > 1e-3
+    assert stats.ks_2samp(ar, ao).pvalue > 1e-3
+
+
 def test_golden_files_present():
-    assert len(glob.glob(os.path.join(GOLDEN, "*.npz"))) >= 9
+    assert len(glob.glob(os.path.join(GOLDEN, "*.npz"))) >= 12
