@@ -129,6 +129,7 @@ SIGNATURES = {
     "dm_cloud_set_reorder_interval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dm_cloud_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dm_cloud_get_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "dm_cloud_set_integrator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dm_cloud_set_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "dm_cloud_get_time": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "dm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp, _dp,
@@ -141,6 +142,7 @@ SIGNATURES = {
     "dm_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "dm_batch_set_step_counter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "dm_batch_set_integrator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dm_batch_set_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "dm_batch_get_time": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "dm_adjoint_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),

@@ -202,6 +202,10 @@ class DeviceCloud:
         self._chk(self.lib.dm_cloud_get_step_counter(self.h, ctypes.byref(v)))
         return v.value
 
+    def set_integrator(self, order: int):
+        """4: Runge_Kutta4 (default); 2: Runge_Kutta2, the midpoint method."""
+        self._chk(self.lib.dm_cloud_set_integrator(self.h, int(order)))
+
     def set_time(self, t: float):
         """Force time of the next step (Integrator::currentTime)."""
         self._chk(self.lib.dm_cloud_set_time(self.h, float(t)))
@@ -277,6 +281,9 @@ class DeviceBatch:
 
     def set_step_counter(self, step: int):
         check(self.lib.dm_batch_set_step_counter(self.h, int(step)), self.ctx.h)
+
+    def set_integrator(self, order: int):
+        check(self.lib.dm_batch_set_integrator(self.h, int(order)), self.ctx.h)
 
     def set_time(self, t: float):
         check(self.lib.dm_batch_set_time(self.h, float(t)), self.ctx.h)

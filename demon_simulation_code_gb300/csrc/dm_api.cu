@@ -84,6 +84,7 @@ struct dm_cloud {
     double *d_dt = nullptr;
     unsigned int *d_min = nullptr;
     float *d_dmin = nullptr;
+    int order = 4;               // integrator: 4 = Runge_Kutta4, 2 = Runge_Kutta2
     int eval_thermal_stage = 1;  // substep of the thermal kicks in force-only evaluations
     int fo_buf = 0;              // stage buffer force-only launches read (the autotuner's dense copy: 1)
     bool boxes_valid[2] = {false, false};  // group boxes (culling) match stage buffer b
@@ -157,6 +158,7 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     P.c = c->d;
     P.f = c->f;
     P.stage = stage;
+    P.order = c->order;
     P.mode = mode;
     P.therm_stage = (mode == kModeForceOnly) ? c->eval_thermal_stage : stage;
     P.fo_buf = (mode == kModeForceOnly) ? c->fo_buf : 0;
@@ -556,7 +558,7 @@ int enqueue_steps(dm_cloud *c, int nsteps, double dt, int precision) {
             int rc = reorder(c);
             if (rc) return rc;
         }
-        for (int st = 1; st <= 4; st++) {
+        for (int st = 1; st <= c->order; st++) {
             int rc = launch_stage(c, precision, st, kModeStep, dt, nullptr);
             if (rc) return rc;
         }
@@ -1062,7 +1064,7 @@ int dm_cloud_move_particles(dm_cloud *c, double end_time, double dt, int precisi
             double step_dt = 0.0;
             int rc = dm_cloud_modify_timestep(c, dt, nullptr, &step_dt);
             if (rc) return rc;
-            for (int st = 1; st <= 4; st++) {
+            for (int st = 1; st <= c->order; st++) {
                 rc = launch_stage(c, precision, st, kModeStep, 0.0, c->d_dt);
                 if (rc) return rc;
             }
@@ -1184,6 +1186,14 @@ int dm_cloud_set_step_counter(dm_cloud *c, uint64_t step) {
     return DM_OK;
 }
 
+int dm_cloud_set_integrator(dm_cloud *c, int order) {
+    if (!c) return DM_ERR_ARG;
+    if (order != 2 && order != 4) return c->ctx->fail(DM_ERR_ARG, "integrator order must be 2 or 4");
+    if (order != c->order) c->drop_graphs();
+    c->order = order;
+    return DM_OK;
+}
+
 int dm_cloud_set_time(dm_cloud *c, double t) {
     if (!c) return DM_ERR_ARG;
     dm_ctx *ctx = c->ctx;
@@ -1280,6 +1290,7 @@ struct dm_batch {
     int *dgseg = nullptr;       // [ngroups] cloud of each group
     int variant = -1;
     int reorder_interval = 4;
+    int order = 4;  // integrator: 4 = Runge_Kutta4, 2 = Runge_Kutta2
     bool order_dirty = true;
     unsigned long long host_steps = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -1305,6 +1316,7 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf =
     StageParams P{};
     P.c = B->d;
     P.stage = stage;
+    P.order = B->order;
     P.mode = mode;
     P.therm_stage = (mode == kModeForceOnly) ? 1 : stage;
     P.fo_buf = (mode == kModeForceOnly) ? fo_buf : 0;
@@ -1365,7 +1377,7 @@ int batch_enqueue_steps(dm_batch *B, int nsteps, double dt) {
             if (rc) return rc;
         }
         DM_CUDA(ctx, cudaMemsetAsync(B->dcounter, 0, 4 * sizeof(unsigned int), ctx->stream));
-        for (int st = 1; st <= 4; st++) {
+        for (int st = 1; st <= B->order; st++) {
             int rc = batch_launch_stage(B, st, kModeStep, dt);
             if (rc) return rc;
         }
@@ -1725,6 +1737,14 @@ int dm_batch_info(dm_batch *B, char *variant, size_t len, int *nitems, int *grid
     if (variant && len) snprintf(variant, len, "%s", kBatchVariants[B->variant].name);
     if (nitems) *nitems = B->nitems[B->variant];
     if (grid) *grid = B->grid[B->variant];
+    return DM_OK;
+}
+
+int dm_batch_set_integrator(dm_batch *B, int order) {
+    if (!B) return DM_ERR_ARG;
+    if (order != 2 && order != 4) return B->ctx->fail(DM_ERR_ARG, "integrator order must be 2 or 4");
+    if (order != B->order) B->drop_graphs();
+    B->order = order;
     return DM_OK;
 }
 

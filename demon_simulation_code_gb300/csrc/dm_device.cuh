@@ -80,7 +80,8 @@ enum StageMode : int { kModeStep = 0, kModeForceOnly = 1 };
 struct StageParams {
     CloudDev c;
     ForceParams f;
-    int stage;            // 1..4
+    int stage;            // 1..order
+    int order;            // 4: Runge_Kutta4; 2: Runge_Kutta2 (the midpoint method)
     int mode;             // StageMode
     int therm_stage;      // substep index of the thermal kicks (force-only: any of 1..4)
     int fo_buf;           // force-only launches: stage position buffer to read (0 = the state)
@@ -214,11 +215,12 @@ __device__ __forceinline__ unsigned long long stage_step_index(const StageParams
     return (s == 1) ? P.c.step_ctr[0] : P.c.step_ctr[1];
 }
 // Force time of the running stage: t, t + dt/2.0, t + dt/2.0, t + dt for
-// stages 1-4 (Runge_Kutta4.cpp:30-88), t the time at the start of the step.
-// Same slot discipline as the step counter: stage 1 reads slot 0 and copies
-// it to slot 1, stages 2-4 read slot 1, stage 4 writes slot 0 = t + dt
-// (currentTime += dt, Runge_Kutta4.cpp:135).  Force-only launches use the
-// time in slot 0.
+// RK4 stages 1-4 (Runge_Kutta4.cpp:30-88), t, t + dt/2.0 for RK2 stages 1-2
+// (Runge_Kutta2.cpp:28-50), t the time at the start of the step.  Same slot
+// discipline as the step counter: stage 1 reads slot 0 and copies it to
+// slot 1, later stages read slot 1, the last stage writes slot 0 = t + dt
+// (currentTime += dt, Runge_Kutta4.cpp:135, Runge_Kutta2.cpp:76).
+// Force-only launches use the time in slot 0.
 __device__ __forceinline__ double stage_dt(const StageParams &P) {
     return P.dt_dev ? *P.dt_dev : P.dt;
 }
@@ -233,7 +235,7 @@ __device__ __forceinline__ void stage_step_advance(const StageParams &P) {
     if (P.stage == 1) {
         P.c.step_ctr[1] = P.c.step_ctr[0];
         P.c.time[1] = P.c.time[0];
-    } else if (P.stage == 4) {
+    } else if (P.stage == P.order) {
         P.c.step_ctr[0] = P.c.step_ctr[1] + 1ull;
         P.c.time[0] = __dadd_rn(P.c.time[1], stage_dt(P));
     }
@@ -412,7 +414,8 @@ __device__ __forceinline__ void add_forces_after_pairs(const ForceParams &f, con
 //  - stage increments k = (dt*Fx)/m, l = dt*Vx_stage (Runge_Kutta4.cpp:32-104);
 //  - the next stage's CacheOperator values (CacheOperator.cpp:28-73);
 //  - after stage 4 the combine v += (k1 + (2*(k2+k3) + k4))/6
-//    (Runge_Kutta4.cpp:107-133, 147-151).
+//    (Runge_Kutta4.cpp:107-133, 147-151); for RK2 (order 2) stage 2 ends
+//    the step with v += k2, x += l2 (Runge_Kutta2.cpp:68-75).
 // Every FP64 operation is an explicit round-to-nearest intrinsic so nothing
 // is contracted into an FMA: given the same forces the state update is bit
 // for bit the reference's.  The forces other than Confinement, Drag,
@@ -478,7 +481,16 @@ __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, doub
     const double nn = __dmul_rn(dt, vys);
     const double x = c.x[i], y = c.y[i], vx = c.vx[i], vy = c.vy[i];
     double nx, ny, nvx = 0.0, nvy = 0.0;
-    if (s == 1 || s == 2) {
+    const bool last = (s == P.order);
+    if (last && s == 2) {  // Runge_Kutta2: x += l2, Vx += k2
+        const double xn = __dadd_rn(x, l), yn = __dadd_rn(y, nn);
+        c.vx[i] = __dadd_rn(vx, k);
+        c.x[i] = xn;
+        c.vy[i] = __dadd_rn(vy, mm);
+        c.y[i] = yn;
+        nx = xn;
+        ny = yn;
+    } else if (s == 1 || s == 2) {
         if (s == 1) {
             c.a1[0][i] = k; c.a1[1][i] = l; c.a1[2][i] = mm; c.a1[3][i] = nn;
         } else {
@@ -514,7 +526,7 @@ __device__ __forceinline__ void stage_epilogue(const StageParams &P, int i, doub
         ny = yn;
     }
     write_stage_position(c, b ^ 1, i, nx, ny);
-    if (s < 4) {
+    if (!last) {
         c.vxc[i] = nvx;
         c.vyc[i] = nvy;
     }

@@ -1,5 +1,6 @@
 /**
- * Runge_Kutta4.cpp -- the device-stepped moveParticles.
+ * Runge_Kutta4.cpp -- the device-stepped moveParticles of Runge_Kutta4 and
+ * Runge_Kutta2.
  */
 #include "Runge_Kutta4.h"
 
@@ -9,15 +10,12 @@
 
 #include "Device.h"
 
-Runge_Kutta4::Runge_Kutta4(Cloud *const C, const ForceArray &FA, const double timeStep, const double startTime)
-    : Integrator(C, FA, timeStep, startTime) {}
-
-void Runge_Kutta4::moveParticles(const double endTime) {
+void DeviceIntegrator::moveParticles(const double endTime) {
     if (!(currentTime < endTime)) return;
     dm_force_params p{};
     for (const Force *f : forces)
         if (!f->addDeviceParams(p))
-            throw demon_gb300::Error(DM_ERR_UNSUPPORTED, std::string("Runge_Kutta4: ") + typeid(*f).name() +
+            throw demon_gb300::Error(DM_ERR_UNSUPPORTED, std::string("moveParticles: ") + typeid(*f).name() +
                                                              " cannot run in the fused device step");
     dm_ctx *ctx = demon_gb300::context();
     dm_cloud *d = cloud->deviceState();
@@ -28,6 +26,7 @@ void Runge_Kutta4::moveParticles(const double endTime) {
         last_ = p;
         have_last_ = true;
     }
+    demon_gb300::check(dm_cloud_set_integrator(d, order_), ctx, "dm_cloud_set_integrator");
     int steps = 0;
     demon_gb300::check(dm_cloud_move_particles(d, endTime, init_dt, precision_, adaptive_ ? 1 : 0, &currentTime,
                                                &steps),

@@ -19,10 +19,16 @@
 
 #include "Integrator.h"
 
-class Runge_Kutta4 : public Integrator {
+/**
+ * The device-stepped integrators' shared machinery (no reference
+ * counterpart: the reference's Runge_Kutta2 and Runge_Kutta4 each loop on
+ * the host).  moveParticles(endTime) of the subclasses runs their order's
+ * stages on the device.
+ */
+class DeviceIntegrator : public Integrator {
 public:
-    Runge_Kutta4(Cloud *const C, const ForceArray &FA, const double timeStep, const double startTime);
-    ~Runge_Kutta4() {}
+    DeviceIntegrator(Cloud *const C, const ForceArray &FA, const double timeStep, const double startTime, int order)
+        : Integrator(C, FA, timeStep, startTime), order_(order) {}
     void moveParticles(const double endTime) override;
 
     /// Pair arithmetic: DM_FP64 (default) or DM_FP32C.
@@ -30,15 +36,23 @@ public:
     /// false: fixed dt = timeStep (no modifyTimeStep), as in the fixed-step
     /// benchmarks; true (default): the reference's adaptive dt.
     void setAdaptiveTimeStep(bool on) { adaptive_ = on; }
-    /// RK4 steps taken so far.
+    /// Steps taken so far.
     long long stepsTaken() const { return steps_; }
 
 private:
+    int order_;
     int precision_ = DM_FP64;
     bool adaptive_ = true;
     long long steps_ = 0;
     dm_force_params last_{};  // parameters the device copy holds
     bool have_last_ = false;
+};
+
+class Runge_Kutta4 : public DeviceIntegrator {
+public:
+    Runge_Kutta4(Cloud *const C, const ForceArray &FA, const double timeStep, const double startTime)
+        : DeviceIntegrator(C, FA, timeStep, startTime, 4) {}
+    ~Runge_Kutta4() {}
 };
 
 #endif  // RUNGA_KUTTA4_H

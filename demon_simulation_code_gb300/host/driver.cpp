@@ -9,8 +9,8 @@
  * -D TimeVaryingDrag, -E Electric, -F VertElectric, -G Gravitational,
  * -L ThermalLocalized, -R RectConfinement, -S Rotational, -T Thermal,
  * -v TimeVaryingThermal, -V ConfinementVoid, -w Driving, with the
- * reference's conflict checks (driver.cpp:483-511).  The reference's RK2
- * integrator (-I) is refused with a message.
+ * reference's conflict checks (driver.cpp:483-511).  -I selects the
+ * Runge_Kutta2 integrator (driver.cpp:904-907, 437-438).
  *
  * Options beyond the reference's:
  *   --precision fp64|fp32c   pair arithmetic (default fp64)
@@ -45,6 +45,7 @@
 #include "MagneticForce.h"
 #include "RectConfinementForce.h"
 #include "RotationalForce.h"
+#include "Runge_Kutta2.h"
 #include "Runge_Kutta4.h"
 #include "ShieldedCoulombForce.h"
 #include "ThermalForce.h"
@@ -58,6 +59,7 @@ namespace {
 // Defaults of the reference (driver.cpp:61-121).
 struct Settings {
     bool mach = false;
+    bool rk4 = true;
     double voidDecay = 0.4;
     double magneticFieldStrength = 1.0;
     double startTime = 0.0;
@@ -166,6 +168,7 @@ void help() {
               << " -g 10.0                dragGamma [Hz]\n"
               << " -h                     this help\n"
               << " -i 0.003               initial inter-particle spacing [m]\n"
+              << " -I                     use the second-order Runge-Kutta integrator\n"
               << " -k 0 0                 initial x;y velocity [m/s]\n"
               << " -M 0.2 100             Mach cone: bullet velocity [m/s], mass factor\n"
               << " -n 4 4                 number of particles [, particles per x row]\n"
@@ -301,7 +304,7 @@ void parseArgs(int argc, char **argv, Settings &s) {
             case 'e': need(i, 1); s.endTime = std::atof(argv[++i]); break;
             case 'g': need(i, 1); s.dragGamma = std::atof(argv[++i]); break;
             case 'h': help(); std::exit(0);
-            case 'I': fail("-I (Runge_Kutta2) is not available in this build");
+            case 'I': s.rk4 = false; break;
             case 'M':
                 need(i, 2);
                 s.mach = true;
@@ -464,7 +467,10 @@ int main(int argc, char **argv) {
 
     int rc = 0;
     try {
-        Runge_Kutta4 I(cloud, forces, s.simTimeStep, s.startTime);
+        // driver.cpp:437-438
+        Runge_Kutta4 rk4(cloud, forces, s.simTimeStep, s.startTime);
+        Runge_Kutta2 rk2(cloud, forces, s.simTimeStep, s.startTime);
+        DeviceIntegrator &I = s.rk4 ? static_cast<DeviceIntegrator &>(rk4) : rk2;
         I.setPrecision(s.precision);
         I.setAdaptiveTimeStep(s.adaptive);
         double t = s.startTime;
@@ -475,7 +481,8 @@ int main(int argc, char **argv) {
             cloud->writeTimeStep(file, error, I.currentTime);
             if (error) fail("FITS error " + std::to_string(error) + " writing a time step");
         }
-        if (!s.dryRun) std::cout << "\r" << I.stepsTaken() << " RK4 steps to t = " << I.currentTime << " s";
+        if (!s.dryRun)
+            std::cout << "\r" << I.stepsTaken() << (s.rk4 ? " RK4" : " RK2") << " steps to t = " << I.currentTime << " s";
     } catch (const demon_gb300::Error &e) {
         std::cerr << "\ndemon_gb300: " << e.what() << std::endl;
         rc = 1;

@@ -270,6 +270,13 @@ int dm_cloud_evaluated_pairs(dm_cloud *cloud, unsigned long long *pairs);
 /* RNG step counter used by the thermal forces (advanced by one per RK4 step). */
 int dm_cloud_set_step_counter(dm_cloud *cloud, uint64_t step);
 int dm_cloud_get_step_counter(dm_cloud *cloud, uint64_t *step);
+/* Integrator of dm_cloud_step and dm_cloud_move_particles: 4 =
+ * Runge_Kutta4 (the default), 2 = Runge_Kutta2, the midpoint method
+ * (Runge_Kutta2.cpp:23-78, the reference driver's -I): stage 1 at (x, v, t),
+ * CacheOperator::operation2, stage 2 at the midpoint and t + dt/2, then
+ * v += k2, x += l2.  Same forces, thermal counters and adaptive dt. */
+int dm_cloud_set_integrator(dm_cloud *cloud, int order);
+
 /* Force time, the reference's Integrator::currentTime (Integrator.h): RK4
  * step k's stages see t, t + dt/2, t + dt/2, t + dt (Runge_Kutta4.cpp:30-88)
  * and each step advances it by dt (Runge_Kutta4.cpp:135).  Only the
@@ -309,6 +316,8 @@ int dm_batch_evaluated_pairs(dm_batch *batch, unsigned long long *pairs);
 /* The autotuned kernel variant, work-item count and persistent grid size. */
 int dm_batch_info(dm_batch *batch, char *variant, size_t len, int *nitems, int *grid);
 int dm_batch_set_step_counter(dm_batch *batch, uint64_t step);
+/* Integrator of dm_batch_step (see dm_cloud_set_integrator). */
+int dm_batch_set_integrator(dm_batch *batch, int order);
 /* Force time shared by every cloud of the batch (see dm_cloud_set_time). */
 int dm_batch_set_time(dm_batch *batch, double t);
 int dm_batch_get_time(dm_batch *batch, double *t);

@@ -5,7 +5,7 @@ serial build, so the summation order is the reference's single-thread
 order) on seeded inputs and records inputs and outputs.  Needs the
 reference checkout (read at build time only) and an x86-64 host.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names]   # all, or only these
 """
 from __future__ import annotations
 
@@ -109,7 +109,18 @@ def main():
                                      steps=np.int64(25), t0=np.float64(0.05), flags=np.int64(flags),
                                      kappa=np.float64(c.shielding), confine=np.float64(c.confine),
                                      x1=rx, y1=ry, vx1=rvx, vy1=rvy)
-    # 7. the two other thermal forces' kicks from the reference itself (its
+    # 7. the reference's own Runge_Kutta2::moveParticles (adaptive dt) from
+    # t0 = 0.1 with a time-dependent force, disk512 workload
+    c = W.disk512().clouds[0]
+    flags = 1 | 2 | 4 | 64 | 1024
+    p = oracle.make_params(flags=flags, shielding=2e4, confine=1e8, gamma=3.0, **OTHER_FORCES)
+    rx, ry, rvx, rvy, steps, t1 = ref.rk2_move_particles(c.x, c.y, c.vx, c.vy, c.q, c.m, p, 1e-4, 0.1,
+                                                         0.1 + 5e-4)
+    out["rk2_move_adaptive_disk512"] = dict(x=c.x, y=c.y, vx=c.vx, vy=c.vy, q=c.q, m=c.m, dt=np.float64(1e-4),
+                                            t0=np.float64(0.1), end=np.float64(0.1 + 5e-4),
+                                            flags=np.int64(flags), steps=np.int64(steps), t1=np.float64(t1),
+                                            x1=rx, y1=ry, vx1=rvx, vy1=rvy)
+    # 8. the two other thermal forces' kicks from the reference itself (its
     # RandomNumbers is clock-seeded, so only their distribution is pinned)
     x, y, vx, vy = disk(4096, 2e-2, 50)
     q = np.full(4096, Q)
@@ -120,7 +131,10 @@ def main():
         d[name + "_fx"], d[name + "_fy"] = ref.forces(x, y, vx, vy, q, m, p, t=tt, thermal=True)
         d[name + "_t"] = np.float64(tt)
     out["thermal_other_ref"] = d
+    only = sys.argv[1:]
     for name, d in out.items():
+        if only and name not in only:
+            continue
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(name, {k: np.shape(v) for k, v in d.items()})
 

@@ -34,14 +34,15 @@ def run(driver, *args, cwd):
     return r
 
 
-def replay(oracle_lib, params, state, q, m, t0, end, data_dt, init_dt):
+def replay(oracle_lib, params, state, q, m, t0, end, data_dt, init_dt, rk2=False):
     """The reference's output loop on the oracle: rows (time, x, y, vx, vy)."""
     x, y, vx, vy = state
+    move = oracle_lib.rk2_move_particles if rk2 else oracle_lib.rk4_move_particles
     rows = []
     te, t = t0, t0
     while te < end:
         te += data_dt
-        x, y, vx, vy, _, t = oracle_lib.rk4_move_particles(x, y, vx, vy, q, m, params, init_dt, t, te)
+        x, y, vx, vy, _, t = move(x, y, vx, vy, q, m, params, init_dt, t, te)
         rows.append((t, x, y, vx, vy))
     return rows
 
@@ -69,6 +70,21 @@ def test_driver_output_matches_oracle(host_build, oracle_lib, tmp_path):
     p = oracle.make_params(flags=1 | 2 | 4, shielding=2e4, confine=1e4, gamma=3.0)
     state = [ts[k][0] for k in ("X_POSITION", "Y_POSITION", "X_VELOCITY", "Y_VELOCITY")]
     rows = replay(oracle_lib, p, state, q, m, 0.0, 0.002, 0.00053, 1e-4)
+    assert len(rows) == ts["TIME"].shape[0] - 1 == 4
+    check_rows(ts, 1, rows)
+
+
+def test_driver_rk2_matches_oracle(host_build, oracle_lib, tmp_path):
+    _, driver = host_build
+    run(driver, *ARGS, "-I", "-w", "1e-15", "5e-4", "1e-5", "-e", "0.002", "-O", "rk2.fits", cwd=tmp_path)
+    keys, tables = read_fits(str(tmp_path / "rk2.fits"))
+    assert keys["FORCES"] == 1 | 2 | 4 | 64
+    q, m = tables["CLOUD"]["CHARGE"].ravel(), tables["CLOUD"]["MASS"].ravel()
+    ts = tables["TIME_STEP"]
+    p = oracle.make_params(flags=1 | 2 | 4 | 64, shielding=2e4, confine=1e4, gamma=3.0, drive_amplitude=1e-15,
+                           drive_shift=5e-4, drive_const=1e-5)
+    state = [ts[k][0] for k in ("X_POSITION", "Y_POSITION", "X_VELOCITY", "Y_VELOCITY")]
+    rows = replay(oracle_lib, p, state, q, m, 0.0, 0.002, 0.00053, 1e-4, rk2=True)
     assert len(rows) == ts["TIME"].shape[0] - 1 == 4
     check_rows(ts, 1, rows)
 

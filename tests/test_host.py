@@ -27,7 +27,7 @@ def test_host_library_exports_the_reference_classes(host_build):
     lib, _ = host_build
     syms = subprocess.run(["nm", "-DC", "--defined-only", lib], capture_output=True, text=True).stdout
     for s in ("Cloud::initializeGrid", "Cloud::writeTimeStep", "Cloud::initializeFromFile",
-              "Runge_Kutta4::moveParticles", "Integrator::modifyTimeStep", "CacheOperator::operation2",
+              "DeviceIntegrator::moveParticles", "Integrator::modifyTimeStep", "CacheOperator::operation2",
               "DeviceForce::evaluate", "ShieldedCoulombForce::writeForce", "ThermalForce::addDeviceParams"):
         assert s in syms, s
 
@@ -70,10 +70,10 @@ def test_command_line_overrides_and_defaults(host_build, tmp_path):
     assert tables["CLOUD"]["MASS"].shape == (16, 1)
 
 
-def test_driver_refuses_rk2(host_build, tmp_path):
+def test_driver_accepts_rk2(host_build, tmp_path):
     _, driver = host_build
-    r = run(driver, "-I", "--dry-run", cwd=tmp_path)
-    assert r.returncode == 1 and "not available" in r.stderr
+    r = run(driver, "-n", "8", "-I", "-O", "i.fits", "--dry-run", cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
 
 
 def test_every_force_option_sets_its_flag_and_keys(host_build, tmp_path):

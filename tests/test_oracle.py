@@ -217,6 +217,30 @@ def test_other_forces_bit_exact_against_compiled_reference(oracle_lib, ref_lib):
     assert all(np.array_equal(u, v) for u, v in zip(a, b))
 
 
+def test_rk2_matches_reference_golden(oracle_lib):
+    """Runge_Kutta2::moveParticles, adaptive dt, from t0 = 0.1 with a
+    time-dependent force (the reference's own run)."""
+    g = load("rk2_move_adaptive_disk512")
+    p = oracle.make_params(flags=int(g["flags"]), shielding=2e4, confine=1e8, gamma=3.0, **OTHER_FORCES)
+    x, y, vx, vy, steps, t1 = oracle_lib.rk2_move_particles(g["x"], g["y"], g["vx"], g["vy"], g["q"], g["m"], p,
+                                                            float(g["dt"]), float(g["t0"]), float(g["end"]))
+    assert steps == int(g["steps"]) and t1 == float(g["t1"])
+    for a, k in zip((x, y, vx, vy), ("x1", "y1", "vx1", "vy1")):
+        assert rel(a, g[k]) < 1e-13, k
+
+
+def test_rk2_bit_exact_against_compiled_reference(oracle_lib, ref_lib):
+    c = W.calm_cloud(64, 3e-3, 32)
+    p = oracle.make_params(flags=1 | 2 | 4 | 64 | 256, shielding=c.shielding, confine=c.confine, **OTHER_FORCES)
+    a = ref_lib.rk2_move_particles(c.x, c.y, c.vx, c.vy, c.q, c.m, p, 1e-4, 0.2, 0.2 + 11.5e-4)
+    b = oracle_lib.rk2_move_particles(c.x, c.y, c.vx, c.vy, c.q, c.m, p, 1e-4, 0.2, 0.2 + 11.5e-4)
+    assert a[4] == b[4] == 12 and a[5] == b[5]
+    assert all(np.array_equal(u, v) for u, v in zip(a[:4], b[:4]))
+    # a calm cloud keeps dt: the fixed-dt restatement takes the same steps
+    f = oracle_lib.rk2_fixed(c.x, c.y, c.vx, c.vy, c.q, c.m, p, 1e-4, 12, t0=0.2)
+    assert all(np.array_equal(u, v) for u, v in zip(a[:4], f))
+
+
 def _kick_stats(fx, fy, scale):
     u = np.hypot(fx, fy) / scale
     return u, np.arctan2(fy, fx)
