@@ -153,6 +153,13 @@ const ExpConsts &exp_consts() {
     return E;
 }
 
+// kappa*log2(e) as a float pair (hi + lo to ~2^-48 relative).
+void kappa_log2e(double kappa, float &hi, float &lo) {
+    const double k = kappa * 1.4426950408889634;
+    hi = (float)k;
+    lo = (float)(k - (double)hi);
+}
+
 StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const double *dt_dev) {
     StageParams P{};
     P.c = c->d;
@@ -174,6 +181,7 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     P.rc2_lo = (float)(P.rc2 * (1.0 - 4e-6));
     P.rc2_hi = (float)(P.rc2 * (1.0 + 4e-6));
     P.kappa_f = (float)kappa;
+    kappa_log2e(kappa, P.kl2e_hi, P.kl2e_lo);
     return P;
 }
 
@@ -426,15 +434,9 @@ int tune_precision(dm_cloud *c, int precision) {
         const bool big = (double)c->n * c->n > 4e9;  // ~64k particles: keep tuning short
         int nstates = 1;
         if (!big && c->d.rc2 > 0.0 && std::isfinite(c->d.rc2)) {
-            unsigned long long hb[4];
-            DM_CUDA(ctx, cudaMemcpyAsync(hb, c->sort.bbox, sizeof hb, cudaMemcpyDeviceToHost, ctx->stream));
+            double v[4];  // bounding box min x, min y, max x, max y
+            DM_CUDA(ctx, cudaMemcpyAsync(v, c->sort.box + 4, sizeof v, cudaMemcpyDeviceToHost, ctx->stream));
             DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            double v[4];
-            for (int k = 0; k < 4; k++) {
-                const unsigned long long o = hb[k];
-                const unsigned long long bits = (o & 0x8000000000000000ull) ? (o & 0x7fffffffffffffffull) : ~o;
-                std::memcpy(&v[k], &bits, sizeof bits);
-            }
             const double half = 0.5 * std::max(v[2] - v[0], v[3] - v[1]);
             const double lam = 1.8 * std::sqrt(c->d.rc2) / half;
             if (std::isfinite(half) && half > 0.0 && lam < 0.9) {
@@ -529,10 +531,10 @@ int reorder(dm_cloud *c) {
     const int n = c->n;
     const int grid = (n + 255) / 256;
     SortScratch &z = c->sort;
-    DM_CUDA(ctx, cudaMemsetAsync(z.bbox, 0xFF, 2 * sizeof(unsigned long long), s));
-    DM_CUDA(ctx, cudaMemsetAsync(z.bbox + 2, 0x00, 2 * sizeof(unsigned long long), s));
-    sort_bbox<<<std::min(grid, ctx->num_sms), 256, 0, s>>>(c->d.x, c->d.y, n, z.bbox);
-    sort_keys<<<grid, 256, 0, s>>>(c->d.x, c->d.y, n, z.bbox, z.keys[0], z.vals[0]);
+    const int mblocks = std::min(grid, kMomentBlocks);
+    sort_moments<<<mblocks, 256, 0, s>>>(c->d.x, c->d.y, n, z.moments);
+    sort_box<<<1, 32, 0, s>>>(z.moments, mblocks, c->d.x, c->d.y, z.box);
+    sort_keys<<<grid, 256, 0, s>>>(c->d.x, c->d.y, n, z.box, z.keys[0], z.vals[0]);
     int cur = 0;
     for (int shift = 0; shift < kSortBits; shift += kSortDigitBits) {
         radix_hist<<<c->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], n, shift, z.hist);
@@ -546,7 +548,7 @@ int reorder(dm_cloud *c) {
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
     c->boxes_valid[0] = c->boxes_valid[1] = false;
     DM_CUDA(ctx, cudaGetLastError());
-    ctx->launches += 5 + 3 * (kSortBits / kSortDigitBits);
+    ctx->launches += 6 + 3 * (kSortBits / kSortDigitBits);
     c->order_dirty = false;
     return DM_OK;
 }
@@ -786,7 +788,8 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->sort_blocks = (n + kSortPerBlock - 1) / kSortPerBlock;
     const size_t nh = align256((size_t)kSortBuckets * c->sort_blocks * sizeof(uint32_t));
     const size_t ngb = align256((size_t)(c->n_pad / 32) * sizeof(float4));
-    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ngb * 2 + ni * 6 + nh + 1024 + 512;
+    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ngb * 2 + ni * 6 + nh + 1024 + 512 +
+                         align256(sizeof(double) * kMomentBlocks * kMomentFields);
     cudaError_t e = cudaMalloc(&c->block, total);
     if (e != cudaSuccess) {
         delete c;
@@ -822,7 +825,8 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->sort.orig_stage = takeI();
     for (int k = 0; k < 6; k++) c->sort.stage[k] = takeD();
     c->sort.hist = (uint32_t *)p; p += nh;
-    c->sort.bbox = (unsigned long long *)p; p += 256;
+    c->sort.box = (double *)p; p += 256;
+    c->sort.moments = (double *)p; p += align256(sizeof(double) * kMomentBlocks * kMomentFields);
     cudaStream_t s = ctx->stream;
     const size_t bytes = (size_t)n * sizeof(double);
     e = cudaMemsetAsync(c->block, 0, total, s);
@@ -1281,7 +1285,7 @@ struct dm_batch {
     int2 *ditems[kNumBatchVariants] = {nullptr};
     int nitems[kNumBatchVariants] = {0};
     int grid[kNumBatchVariants] = {0};
-    unsigned long long *dbbox = nullptr;
+    double *dbox = nullptr;  // [nclouds][8] key box and bounding box (batch_boxes)
     SortScratch sort{};
     int sort_blocks = 0;
     int mbits = 24;
@@ -1344,11 +1348,8 @@ int batch_reorder(dm_batch *B) {
     const int n = B->total;
     const int grid = (n + 255) / 256;
     SortScratch &z = B->sort;
-    // min entries to all-ones, max entries to zero: bbox layout [cloud][4]
-    DM_CUDA(ctx, cudaMemsetAsync(B->dbbox, 0xFF, 4 * sizeof(unsigned long long) * B->nclouds, s));
-    batch_init_bbox_max<<<(B->nclouds + 127) / 128, 128, 0, s>>>(B->dbbox, B->nclouds);
-    batch_bbox<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbbox);
-    batch_keys<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbbox, B->mbits, z.keys[0], z.vals[0]);
+    batch_boxes<<<B->nclouds, 256, 0, s>>>(B->d.x, B->d.y, B->ddesc, B->dbox);
+    batch_keys<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbox, B->mbits, z.keys[0], z.vals[0]);
     int cur = 0;
     int passes = 0;
     const int bits = B->mbits + 32 - __builtin_clz((unsigned)std::max(B->nclouds - 1, 1));
@@ -1364,7 +1365,7 @@ int batch_reorder(dm_batch *B) {
     permute_commit<<<grid, 256, 0, s>>>(B->d, z);
     batch_init_positions<<<(B->total_pad + 255) / 256, 256, 0, s>>>(B->d, B->ddesc, B->dseg);
     DM_CUDA(ctx, cudaGetLastError());
-    ctx->launches += 6 + 3 * passes;
+    ctx->launches += 5 + 3 * passes;
     B->order_dirty = false;
     return DM_OK;
 }
@@ -1418,7 +1419,7 @@ int batch_tune(dm_batch *B) {
         }
         // two states, as for one cloud: the batch as it is (buffer 0) and
         // every cloud squeezed to ~30% in-cutoff pairs (buffer 1)
-        batch_tune_compress<<<(B->total + 255) / 256, 256, 0, ctx->stream>>>(B->d, B->ddesc, B->dseg, B->dbbox);
+        batch_tune_compress<<<(B->total + 255) / 256, 256, 0, ctx->stream>>>(B->d, B->ddesc, B->dseg, B->dbox);
         DM_CUDA(ctx, cudaGetLastError());
         cudaEvent_t a, b;
         DM_CUDA(ctx, cudaEventCreate(&a));
@@ -1497,7 +1498,7 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     B->sort_blocks = (B->total + kSortPerBlock - 1) / kSortPerBlock;
     const size_t nh = align256((size_t)kSortBuckets * B->sort_blocks * sizeof(uint32_t));
     const size_t ndesc = align256((size_t)nclouds * sizeof(BatchCloud));
-    const size_t nbb = align256((size_t)nclouds * 4 * sizeof(unsigned long long));
+    const size_t nbb = align256((size_t)nclouds * 8 * sizeof(double));
     const size_t bytes_total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ni * 7 + nh + ndesc + nbb + 1024;
     cudaError_t e = cudaMalloc(&B->block, bytes_total);
     if (e != cudaSuccess) {
@@ -1530,7 +1531,7 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     B->sort.orig_stage = takeI();
     B->sort.hist = (uint32_t *)p; p += nh;
     B->ddesc = (BatchCloud *)p; p += ndesc;
-    B->dbbox = (unsigned long long *)p; p += nbb;
+    B->dbox = (double *)p; p += nbb;
     d.step_ctr = (unsigned long long *)p; p += 256;
     d.time = (double *)(d.step_ctr + 4);  // same 256-byte slot, bytes 32-47
     d.err = (int *)p; p += 256;
@@ -1552,6 +1553,7 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
         bc.rc2_lo = (float)(bc.rc2 * (1.0 - 4e-6));
         bc.rc2_hi = (float)(bc.rc2 * (1.0 + 4e-6));
         bc.kappa_f = (float)kappa;
+        kappa_log2e(kappa, bc.kl2e_hi, bc.kl2e_lo);
         for (int i = 0; i < n[c]; i++) {
             seg[off + i] = c;
             orig[off + i] = off + i;

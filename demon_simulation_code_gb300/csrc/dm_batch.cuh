@@ -24,6 +24,7 @@ struct BatchCloud {
     ForceParams f;
     double rc2;
     float rc2_lo, rc2_hi, kappa_f;
+    float kl2e_hi, kl2e_lo;  // kappa*log2(e) as a float pair
 };
 
 // A StageParams view of one cloud: pointers offset to the cloud's particles.
@@ -47,6 +48,8 @@ __device__ __forceinline__ void batch_view(StageParams &V, const StageParams &P0
     V.rc2_lo = d.rc2_lo;
     V.rc2_hi = d.rc2_hi;
     V.kappa_f = d.kappa_f;
+    V.kl2e_hi = d.kl2e_hi;
+    V.kl2e_lo = d.kl2e_lo;
 }
 
 template <int NW, int ILP, int TC, bool CULL = false>
@@ -112,40 +115,29 @@ static __global__ void batch_group_bounds(CloudDev c, const BatchCloud *__restri
 
 // bbox rows are (min x, min y, max x, max y) in ordered bits: the min
 // entries start at all-ones (memset), the max entries at zero.
-static __global__ void batch_init_bbox_max(unsigned long long *bbox, int nclouds) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < nclouds) {
-        bbox[4 * c + 2] = 0ull;
-        bbox[4 * c + 3] = 0ull;
-    }
-}
-
-static __global__ void batch_bbox(const double *__restrict__ x, const double *__restrict__ y, int n,
-                                  const int *__restrict__ seg, unsigned long long *bbox) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double a = x[i], b = y[i];
-    if (!(isfinite(a) && isfinite(b))) return;
-    unsigned long long *bb = bbox + 4 * seg[i];
-    atomicMin(&bb[0], ordered_bits(a));
-    atomicMin(&bb[1], ordered_bits(b));
-    atomicMax(&bb[2], ordered_bits(a));
-    atomicMax(&bb[3], ordered_bits(b));
+// One block per cloud: the cloud's key box (the bounding box clipped to
+// mean +- 4 sigma per axis) and bounding box, box[8 * cloud ...] as in
+// moments_to_box.  Deterministic (fixed partition and order).
+static __global__ void __launch_bounds__(256) batch_boxes(const double *__restrict__ x,
+                                                          const double *__restrict__ y,
+                                                          const BatchCloud *__restrict__ desc, double *box) {
+    const BatchCloud &d = desc[blockIdx.x];
+    const double ox = finite_or_zero(x[d.off]), oy = finite_or_zero(y[d.off]);
+    const Moments m = block_moments(x, y, d.off, d.off + d.n, blockDim.x, ox, oy);
+    if (threadIdx.x == 0) moments_to_box(m, ox, oy, box + 8 * blockIdx.x);
 }
 
 // key = cloud index (high bits) | the top `mbits` bits of the 24-bit Morton
 // code within the cloud's box, so a stable sort keeps every cloud in its own
 // contiguous range.
 static __global__ void batch_keys(const double *__restrict__ x, const double *__restrict__ y, int n,
-                                  const int *__restrict__ seg, const unsigned long long *bbox,
+                                  const int *__restrict__ seg, const double *__restrict__ box,
                                   int mbits, uint32_t *keys, int *vals) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int sg = seg[i];
-    const unsigned long long *bb = bbox + 4 * sg;
-    const double x0 = from_ordered_bits(bb[0]), y0 = from_ordered_bits(bb[1]);
-    const double x1 = from_ordered_bits(bb[2]), y1 = from_ordered_bits(bb[3]);
-    const double ext = fmax(x1 - x0, y1 - y0);
+    const double *bb = box + 8 * sg;
+    const double x0 = bb[0], y0 = bb[1], ext = bb[2];
     const double scale = (ext > 0.0 && isfinite(ext)) ? 4095.0 / ext : 0.0;
     const double fx = (x[i] - x0) * scale, fy = (y[i] - y0) * scale;
     const uint32_t qx = (fx > 0.0) ? (uint32_t)fmin(fx, 4095.0) : 0u;
@@ -160,13 +152,12 @@ static __global__ void batch_keys(const double *__restrict__ x, const double *__
 // are copied as they are), written as stage buffer 1 (nothing live there
 // between steps).
 static __global__ void batch_tune_compress(CloudDev c, const BatchCloud *__restrict__ desc,
-                                           const int *__restrict__ seg, const unsigned long long *bbox) {
+                                           const int *__restrict__ seg, const double *__restrict__ box) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const int sg = seg[i];
-    const unsigned long long *bb = bbox + 4 * sg;
-    const double x0 = from_ordered_bits(bb[0]), y0 = from_ordered_bits(bb[1]);
-    const double x1 = from_ordered_bits(bb[2]), y1 = from_ordered_bits(bb[3]);
+    const double *bb = box + 8 * sg;  // bounding box in bb[4..7]
+    const double x0 = bb[4], y0 = bb[5], x1 = bb[6], y1 = bb[7];
     const double half = 0.5 * fmax(x1 - x0, y1 - y0);
     double lam = 1.8 * sqrt(desc[sg].rc2) / half;
     if (!(isfinite(lam) && lam > 0.0 && lam < 1.0)) lam = 1.0;

@@ -93,6 +93,7 @@ struct StageParams {
     double rc2;           // (10/kappa)^2
     float rc2_lo, rc2_hi; // FP32 certain-in / certain-out bounds on r^2
     float kappa_f;
+    float kl2e_hi, kl2e_lo;  // kappa*log2(e) as a float pair
     // j split without clusters: rank r of tile t is block t*split + r and
     // writes its partial sums to partial[r*n_pad + i]; stage_finish sums them
     int split;

@@ -54,14 +54,14 @@ __device__ __forceinline__ float exp_neg(float a, const ExpConsts &E) {
     return p * scale;
 }
 
-// e^{-a} for a >= 0 on the SFU: t = a*log2(e) is rounded to FP32 (absolute
-// error up to ~1e-6 at a = 10, i.e. a relative error of the result of
-// ~6e-7); the rounding residue t_lo (exact to ~2^-48) is put back to first
-// order, 2^{-(t + t_lo)} = 2^{-t} (1 - t_lo ln 2).  Relative error: that of
-// the hardware ex2.approx (a few ulp) plus ~(t_lo ln 2)^2 / 2 < 1e-12.
-__device__ __forceinline__ float exp_neg_sfu(float a, const ExpConsts &E) {
-    const float t = a * E.l2e_hi;
-    const float t_lo = fmaf(a, E.l2e_lo, fmaf(a, E.l2e_hi, -t));
+// e^{-kappa r} on the SFU with kappa*log2(e) = k_hi + k_lo given as a float
+// pair: t = k_hi r rounded to FP32 (absolute error up to ~1e-6 at kappa r =
+// 10), and its residue t_lo (exact to ~2^-48) put back to first order,
+// 2^{-(t + t_lo)} = 2^{-t} (1 - t_lo ln 2).  Relative error: the hardware
+// ex2.approx (a few ulp) plus (t_lo ln 2)^2 / 2 < 1e-12, for the FP32 r given.
+__device__ __forceinline__ float exp_neg_kr(float r, float k_hi, float k_lo) {
+    const float t = k_hi * r;
+    const float t_lo = fmaf(k_lo, r, fmaf(k_hi, r, -t));
     float e;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(-t));
     return e * fmaf(-t_lo, 0.693147182f, 1.0f);
@@ -178,7 +178,7 @@ struct PairCtx {
 
 // The pair force on i from j (added into px, py; nothing for j == i or a
 // pair outside the cutoff).
-__device__ __forceinline__ void precise_pair(const StageParams &P, const ExpConsts &E, int b,
+__device__ __forceinline__ void precise_pair(const StageParams &P, int b,
                                              float xh_i, float yh_i, const PairCtx &ic,
                                              const float4 &A, const float4 &Bj, int jg, float &px,
                                              float &py) {
@@ -199,32 +199,27 @@ __device__ __forceinline__ void precise_pair(const StageParams &P, const ExpCons
     const float h = r2 * y;
     const float ee = fmaf(-h, y, 1.0f);
     y = fmaf(0.5f * ee, y, y);
-    const float r = r2 * y;
-    const float kr = P.kappa_f * r;
-    const float ex = exp_neg_sfu(kr, E);
-    // C q_i q_j (1 + kr) e^{-kr} / r^3
-    const float s = ((ic.qc * A.w) * (1.0f + kr)) * ex * ((y * y) * y);
+    const float ex = exp_neg_kr(r2 * y, P.kl2e_hi, P.kl2e_lo);
+    // C q_i q_j (1 + kappa r) e^{-kappa r} / r^3 = C q_i q_j e^{-kappa r} y^2 (y + kappa), y = 1/r
+    const float s = ((ic.qc * A.w) * ex) * ((y * y) * (y + P.kappa_f));
     px = fmaf(s, dx, px);
     py = fmaf(s, dy, py);
 }
 
 // The pair force on i from j for a pair known to be inside the cutoff (a
-// j group entirely within reach of the i tile): the precise arithmetic with
-// no cutoff test; the pair j == i (its own tile) gives zero by selection.
-__device__ __forceinline__ void inside_pair(const StageParams &P, const ExpConsts &E, float xh_i, float yh_i,
-                                            const PairCtx &ic, float xj, float yj, const float4 &Bj, float &px,
-                                            float &py) {
+// j group entirely within reach of the i tile, never one of the tile's own
+// groups, so j != i): the precise arithmetic with no cutoff test.
+__device__ __forceinline__ void inside_pair(const StageParams &P, float xh_i, float yh_i, const PairCtx &ic,
+                                            float xj, float yj, const float4 &Bj, float &px, float &py) {
     const float dx = (xh_i - xj) + (ic.xl - Bj.x);
     const float dy = (yh_i - yj) + (ic.yl - Bj.y);
-    const bool self = __float_as_int(Bj.w) == ic.ii;
-    const float r2 = self ? 1.0f : fmaf(dx, dx, dy * dy);
+    const float r2 = fmaf(dx, dx, dy * dy);
     float y = rsqrtf(r2);
     const float h = r2 * y;
     const float ee = fmaf(-h, y, 1.0f);
     y = fmaf(0.5f * ee, y, y);
-    const float kr = P.kappa_f * (r2 * y);
-    const float ex = exp_neg_sfu(kr, E);
-    const float s = self ? 0.0f : ((ic.qc * Bj.z) * (1.0f + kr)) * ex * ((y * y) * y);
+    const float ex = exp_neg_kr(r2 * y, P.kl2e_hi, P.kl2e_lo);
+    const float s = ((ic.qc * Bj.z) * ex) * ((y * y) * (y + P.kappa_f));
     px = fmaf(s, dx, px);
     py = fmaf(s, dy, py);
 }
@@ -315,7 +310,7 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
                     const float4 Bj = s_pb[jj];
                     const float xj = reinterpret_cast<const float *>(s_x4)[jj];
                     const float yj = reinterpret_cast<const float *>(s_y4)[jj];
-                    precise_pair(P, E, b, xh, yh, ic, make_float4(xj, yj, 0.0f, Bj.z), Bj,
+                    precise_pair(P, b, xh, yh, ic, make_float4(xj, yj, 0.0f, Bj.z), Bj,
                                  __float_as_int(Bj.w), px, py);
                 }
                 kahan_add(acc.x, acc.z, px);
@@ -378,29 +373,38 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         __syncthreads();
         if constexpr (DENSE) {
             // every pair of these groups is inside the cutoff: no filter, no
-            // queue; each lane evaluates its own i against the chunk's 4 j
+            // queue; each lane evaluates its own i against the chunk's 4 j,
+            // with its i data and Kahan sums in registers for the whole tile
+            PairCtx ic[ILP];
+            float xhk[ILP], yhk[ILP];
+            float4 acc[ILP];
+#pragma unroll
+            for (int k = 0; k < ILP; k++) {
+                const float4 c4 = s_cold[k * 32 + lane];
+                ic[k].xl = c4.x;
+                ic[k].yl = c4.y;
+                ic[k].qc = c4.z;
+                ic[k].ii = __float_as_int(c4.w);
+                xhk[k] = -0.5f * mx2[k].x;
+                yhk[k] = -0.5f * my2[k].x;
+                acc[k] = my_acc[k * 32 + lane];
+            }
             for (int c = warp; c < tcn; c += NW) {
                 const float4 X = s_x4[c], Y = s_y4[c];
                 const float xs[4] = {X.x, X.y, X.z, X.w};
                 const float ys[4] = {Y.x, Y.y, Y.z, Y.w};
-                static_for<ILP>([&](auto kc) {
-                    constexpr int k = decltype(kc)::value;
-                    const float4 c4 = s_cold[k * 32 + lane];
-                    PairCtx ic;
-                    ic.xl = c4.x;
-                    ic.yl = c4.y;
-                    ic.qc = c4.z;
-                    ic.ii = __float_as_int(c4.w);
-                    const float xh = -0.5f * mx2[k].x, yh = -0.5f * my2[k].x;
+#pragma unroll
+                for (int k = 0; k < ILP; k++) {
                     float px = 0.0f, py = 0.0f;
 #pragma unroll 1
-                    for (int u = 0; u < 4; u++) inside_pair(P, E, xh, yh, ic, xs[u], ys[u], s_pb[4 * c + u], px, py);
-                    float4 acc = my_acc[k * 32 + lane];
-                    kahan_add(acc.x, acc.z, px);
-                    kahan_add(acc.y, acc.w, py);
-                    my_acc[k * 32 + lane] = acc;
-                });
+                    for (int u = 0; u < 4; u++)
+                        inside_pair(P, xhk[k], yhk[k], ic[k], xs[u], ys[u], s_pb[4 * c + u], px, py);
+                    kahan_add(acc[k].x, acc[k].z, px);
+                    kahan_add(acc[k].y, acc[k].w, py);
+                }
             }
+#pragma unroll
+            for (int k = 0; k < ILP; k++) my_acc[k * 32 + lane] = acc[k];
         } else {
         for (int c = warp; c < tcn; c += NW) {
             const float4 X = s_x4[c], Y = s_y4[c], Bq = s_b4[c];
@@ -480,7 +484,8 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
             if (t < my_ng) {
                 const float4 gbox = gb[g];
                 near = boxes_near(tb, gbox, P.rc2_hi);
-                inside = near && boxes_inside(tb, gbox, P.rc2_lo);
+                // the tile's own groups hold the pairs j == i: filtered path
+                inside = near && g / ILP != tile && boxes_inside(tb, gbox, P.rc2_lo);
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, near && !inside);
             const uint32_t bal2 = __ballot_sync(0xffffffffu, inside);

@@ -10,10 +10,17 @@
 // (used for the thermal RNG counter, for downloads and for the adaptive-dt
 // pair pattern, all of which are defined on the caller's order).
 //
-// Sort: 24-bit Morton keys (12 bits per axis over the cloud's bounding box)
-// and a deterministic, stable LSD radix sort with 8-bit digits (per-block
-// digit histograms, one scan, stable scatter ranked with __match_any_sync).
-// No atomics decide any order; the result depends only on the positions.
+// Sort: 24-bit Morton keys (12 bits per axis) and a deterministic, stable
+// LSD radix sort with 8-bit digits (per-block digit histograms, one scan,
+// stable scatter ranked with __match_any_sync).  No atomics decide any
+// order; the result depends only on the positions.
+//
+// The key box is the bounding box clipped to mean +- 4 standard deviations
+// per axis.  A confined cloud that collapses and re-expands throws a few
+// particles metres out while the rest stay within centimetres; over the
+// plain bounding box a 12-bit cell is then wider than the cutoff and
+// thousands of core particles share one key, so 32-particle groups are no
+// longer compact.  Particles outside the clipped box take the edge cells.
 #pragma once
 
 #include "dm_device.cuh"
@@ -26,8 +33,12 @@ constexpr int kSortBits = 24;
 constexpr int kSortDigitBits = 8;  // 24-bit keys: 3 passes
 constexpr int kSortBuckets = 1 << kSortDigitBits;
 
+constexpr int kMomentBlocks = 64;  // fixed partition of the moment reduction
+constexpr int kMomentFields = 9;   // count, sum dx, sum dy, sum dx^2, sum dy^2, min x, min y, max x, max y
+
 struct SortScratch {
-    unsigned long long *bbox;  // [4]: ordered-bit min x, min y, max x, max y
+    double *moments;           // [kMomentBlocks][kMomentFields] per-block partials
+    double *box;               // [8]: key box x0, y0, extent; -; bounding box min x, min y, max x, max y
     uint32_t *keys[2];
     int *vals[2];
     uint32_t *hist;            // [kSortBuckets * nblocks]
@@ -35,38 +46,112 @@ struct SortScratch {
     int *orig_stage;
 };
 
-// Order-preserving map of a double to uint64 (for atomicMin/atomicMax).
-__device__ __forceinline__ unsigned long long ordered_bits(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double from_ordered_bits(unsigned long long o) {
-    const unsigned long long b = (o & 0x8000000000000000ull) ? (o & 0x7fffffffffffffffull) : ~o;
-    return __longlong_as_double((long long)b);
-}
-
-static __global__ void sort_bbox(const double *__restrict__ x, const double *__restrict__ y, int n,
-                                 unsigned long long *bbox) {
-    double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double a = x[i], b = y[i];
-        if (isfinite(a) && isfinite(b)) {
-            mnx = fmin(mnx, a); mxx = fmax(mxx, a);
-            mny = fmin(mny, b); mxy = fmax(mxy, b);
+// Moments of finite positions: count, sums of the offsets (dx, dy) from an
+// origin and of their squares (the origin keeps the second moments well
+// conditioned), and the bounding box.
+struct Moments {
+    double v[kMomentFields];
+    __device__ __forceinline__ void clear() {
+        for (int k = 0; k < 5; k++) v[k] = 0.0;
+        v[5] = v[6] = INFINITY;
+        v[7] = v[8] = -INFINITY;
+    }
+    __device__ __forceinline__ void add(double a, double b, double ox, double oy) {
+        if (!(isfinite(a) && isfinite(b))) return;
+        const double da = a - ox, db = b - oy;
+        v[0] += 1.0;
+        v[1] += da;
+        v[2] += db;
+        v[3] += da * da;
+        v[4] += db * db;
+        v[5] = fmin(v[5], a);
+        v[6] = fmin(v[6], b);
+        v[7] = fmax(v[7], a);
+        v[8] = fmax(v[8], b);
+    }
+    __device__ __forceinline__ void merge(const double *o) {
+        for (int k = 0; k < 5; k++) v[k] += o[k];
+        v[5] = fmin(v[5], o[5]);
+        v[6] = fmin(v[6], o[6]);
+        v[7] = fmax(v[7], o[7]);
+        v[8] = fmax(v[8], o[8]);
+    }
+    // butterfly over the warp; lane 0's result has a fixed evaluation order
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            double o[kMomentFields];
+#pragma unroll
+            for (int k = 0; k < kMomentFields; k++) o[k] = __shfl_xor_sync(0xffffffffu, v[k], off);
+            merge(o);
         }
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        mnx = fmin(mnx, __shfl_xor_sync(0xffffffffu, mnx, off));
-        mny = fmin(mny, __shfl_xor_sync(0xffffffffu, mny, off));
-        mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, off));
-        mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, off));
+};
+
+// Block-wide moments of positions i0, i0 + stride, ... < i1 (fixed
+// partition and order: deterministic); the result is valid in thread 0.
+__device__ __forceinline__ Moments block_moments(const double *__restrict__ x, const double *__restrict__ y,
+                                                 int i0, int i1, int stride, double ox, double oy) {
+    __shared__ double s[32][kMomentFields];
+    Moments m;
+    m.clear();
+    for (int i = i0 + (int)threadIdx.x; i < i1; i += stride) m.add(x[i], y[i], ox, oy);
+    m.warp_reduce();
+    const int warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < kMomentFields; k++) s[warp][k] = m.v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < nw; w++) m.merge(s[w]);
+    __syncthreads();  // s is reused by the next call
+    return m;
+}
+
+// Key box of a cloud from its moments: the bounding box clipped to mean +-
+// 4 standard deviations per axis, as (x0, y0, extent); then the bounding
+// box itself.  box[8]: x0, y0, extent, 0, min x, min y, max x, max y.
+__device__ __forceinline__ void moments_to_box(const Moments &m, double ox, double oy, double *box) {
+    double lo[2] = {0.0, 0.0}, hi[2] = {0.0, 0.0};
+    const double n = m.v[0];
+    if (n > 0.0) {
+        const double org[2] = {ox, oy};
+        for (int a = 0; a < 2; a++) {
+            const double mean = m.v[1 + a] / n;
+            const double sd = sqrt(fmax(m.v[3 + a] / n - mean * mean, 0.0));
+            lo[a] = fmax(m.v[5 + a], org[a] + mean - 4.0 * sd);
+            hi[a] = fmin(m.v[7 + a], org[a] + mean + 4.0 * sd);
+            if (!(lo[a] <= hi[a])) {  // degenerate: fall back to the bounding box
+                lo[a] = m.v[5 + a];
+                hi[a] = m.v[7 + a];
+            }
+        }
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMin(&bbox[0], ordered_bits(mnx));
-        atomicMin(&bbox[1], ordered_bits(mny));
-        atomicMax(&bbox[2], ordered_bits(mxx));
-        atomicMax(&bbox[3], ordered_bits(mxy));
-    }
+    box[0] = lo[0];
+    box[1] = lo[1];
+    box[2] = fmax(hi[0] - lo[0], hi[1] - lo[1]);
+    box[3] = 0.0;
+    for (int k = 0; k < 4; k++) box[4 + k] = (n > 0.0) ? m.v[5 + k] : 0.0;
+}
+
+__device__ __forceinline__ double finite_or_zero(double v) { return isfinite(v) ? v : 0.0; }
+
+// Per-block moments of one cloud's positions (origin: its first particle).
+static __global__ void __launch_bounds__(256) sort_moments(const double *__restrict__ x,
+                                                           const double *__restrict__ y, int n, double *part) {
+    const double ox = finite_or_zero(x[0]), oy = finite_or_zero(y[0]);
+    const Moments m = block_moments(x, y, blockIdx.x * blockDim.x, n, gridDim.x * blockDim.x, ox, oy);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < kMomentFields; k++) part[blockIdx.x * kMomentFields + k] = m.v[k];
+}
+
+// One warp: the per-block moments summed in fixed order, then the key box.
+static __global__ void sort_box(const double *__restrict__ part, int nparts, const double *__restrict__ x,
+                                const double *__restrict__ y, double *box) {
+    Moments m;
+    m.clear();
+    for (int b = (int)threadIdx.x; b < nparts; b += 32) m.merge(part + b * kMomentFields);
+    m.warp_reduce();
+    if (threadIdx.x == 0) moments_to_box(m, finite_or_zero(x[0]), finite_or_zero(y[0]), box);
 }
 
 // Spreads the low 12 bits of v to the even bit positions.
@@ -80,12 +165,10 @@ __device__ __forceinline__ uint32_t spread_bits12(uint32_t v) {
 }
 
 static __global__ void sort_keys(const double *__restrict__ x, const double *__restrict__ y, int n,
-                                 const unsigned long long *bbox, uint32_t *keys, int *vals) {
+                                 const double *__restrict__ box, uint32_t *keys, int *vals) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double x0 = from_ordered_bits(bbox[0]), y0 = from_ordered_bits(bbox[1]);
-    const double x1 = from_ordered_bits(bbox[2]), y1 = from_ordered_bits(bbox[3]);
-    const double ext = fmax(x1 - x0, y1 - y0);
+    const double x0 = box[0], y0 = box[1], ext = box[2];
     const double scale = (ext > 0.0 && isfinite(ext)) ? 4095.0 / ext : 0.0;
     const double fx = (x[i] - x0) * scale, fy = (y[i] - y0) * scale;
     const uint32_t qx = (fx > 0.0) ? (uint32_t)fmin(fx, 4095.0) : 0u;
