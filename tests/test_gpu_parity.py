@@ -323,6 +323,25 @@ def test_every_kernel_variant_and_split_is_correct(gpu_ctx, oracle_lib, prec, n)
             assert np.all(np.isfinite(c.download()[0]))
 
 
+@pytest.mark.parametrize("name", ["fp32c<8,4,256,false,cull>", "fp32c<4,2,128,false,cull>",
+                                  "fp32c<8,4,256,true,cull>"])
+def test_culled_variants_on_a_collapsed_cloud(gpu_ctx, oracle_lib, name):
+    """A cloud a few cutoffs across: many j groups lie entirely inside the
+    cutoff of an i tile (the path without filter or queue), the rest near it."""
+    c0 = W.disk_cloud(2048, 1.2e-3, 23)
+    rx, ry = oracle_lib.forces(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m, oracle.make_params(**c0.params()))
+    for split in (1, 4, 16):
+        c = DeviceCloud.from_cloud(gpu_ctx, c0)
+        try:
+            c.set_kernel(name, split)
+        except Exception:  # a cluster size the device cannot schedule
+            c.close()
+            continue
+        fx, fy = c.eval_forces("fp32c")
+        assert e_F(fx, fy, rx, ry) <= TOL["fp32c"], (name, split)
+        c.close()
+
+
 def test_autotuner_reports_a_variant(gpu_ctx):
     c = DeviceCloud.from_cloud(gpu_ctx, W.disk_cloud(4096, 4e-3, 2))
     name, split = c.autotune("fp32c")
