@@ -104,14 +104,13 @@ struct Fp32cSmem {
     // j tile: TC 4-j chunks as structure of arrays (x, y, |p|^2) + precise data
     static constexpr size_t tile = (size_t)TC * (3 * sizeof(float4) + 4 * sizeof(float4));
     static constexpr size_t cold = (size_t)ILP * 32 * sizeof(float4);
-    static constexpr size_t queue = (size_t)NW * ILP * 32 * sizeof(int2);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
     // culling: near and inside group lists (NT each) and their per-warp counts
     static constexpr size_t glist = 2 * ((size_t)NW * 32 * sizeof(int) + NW * sizeof(int));
-    static constexpr size_t bytes = tile + cold + queue + acc + red + glist;
+    static constexpr size_t bytes = tile + cold + acc + red + glist;
     // s_red, in float4 units from the start of shared memory
-    static constexpr size_t red_offset = (tile + cold + queue + acc) / sizeof(float4);
+    static constexpr size_t red_offset = (tile + cold + acc) / sizeof(float4);
 };
 
 // Conservative FP32 test: can any point of box a come within the cutoff of
@@ -235,14 +234,13 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
                                             int rank, int S, unsigned char *smem_raw) {
     constexpr int NT = NW * 32;
     constexpr int TILE = 32 * ILP;  // particles per i tile
-    static_assert(ILP <= 4, "queue counts are packed in one 32-bit word");
+    static_assert(ILP <= 4, "the i slots of a lane are selected with unrolled compares");
     float4 *s_x4 = reinterpret_cast<float4 *>(smem_raw);  // [TC] xh of 4 j
     float4 *s_y4 = s_x4 + TC;                              // [TC] yh
     float4 *s_b4 = s_y4 + TC;                              // [TC] xh^2 + yh^2
     float4 *s_pb = s_b4 + TC;                              // [4*TC] (xl, yl, q, j)
     float4 *s_cold = s_pb + 4 * TC;                        // [ILP][32]
-    int2 *s_queue = reinterpret_cast<int2 *>(s_cold + ILP * 32);           // [NW][ILP][32]
-    float4 *s_acc = reinterpret_cast<float4 *>(s_queue + NW * ILP * 32);    // [NW][ILP][32]
+    float4 *s_acc = s_cold + ILP * 32;                     // [NW][ILP][32]
     float4 *s_red = s_acc + NW * ILP * 32;                                 // [TILE]
     int *s_glist = reinterpret_cast<int *>(s_red + TILE);                  // [NT] surviving groups
     int *s_wcount = s_glist + NT;                                          // [NW]
@@ -253,7 +251,6 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
     const int b = (P.mode == kModeForceOnly) ? P.fo_buf : (P.stage - 1) & 1;
     const float4 *__restrict__ pa = P.c.pa[b];
     const float4 *__restrict__ pb = P.c.pb[b];
-    int2 *my_queue = s_queue + warp * ILP * 32;
     float4 *my_acc = s_acc + warp * ILP * 32;
 
     // every warp owns the same TILE particles: lane l, slot k -> i = tile*TILE + k*32 + l.
@@ -280,63 +277,56 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         my_acc[k * 32 + lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 
-    uint32_t qn = 0u;  // queue fill per slot, 8 bits per slot (warp-uniform)
-
-    // Run the precise path on the queued entries of slot K, then empty it.
-    // K is a runtime value (the slot's i position comes in xh, yh), so the
-    // precise path exists once in the kernel's code.
-    auto flush = [&](int K, float xh, float yh) {
-        __syncwarp();
-        const int fill = (int)((qn >> (8 * K)) & 0xFFu);
-        const int2 ent = (lane < fill) ? my_queue[K * 32 + lane] : make_int2(0, 0);
-        uint32_t mask = warp_transpose32((uint32_t)ent.y);
-        if (mask) {
-            const float4 c4 = s_cold[K * 32 + lane];
+    // Filter hits are recorded per lane: bit 4*g + u of hits[k] is the pair
+    // (slot k's i, j = 4*(cbase + g*NW) + u of the staged tile), for the
+    // last (up to 8) chunks this warp swept.  The flush runs the precise
+    // path on every lane's own hits, slot by slot (the slot is a runtime
+    // value, so the precise path exists once in the kernel's code).
+    uint32_t hits[ILP];
+#pragma unroll
+    for (int k = 0; k < ILP; k++) hits[k] = 0u;
+    const float *s_xf = reinterpret_cast<const float *>(s_x4);
+    const float *s_yf = reinterpret_cast<const float *>(s_y4);
+    auto flush_hits = [&](int cbase) {
+#pragma unroll 1
+        for (int k = 0; k < ILP; k++) {
+            uint32_t m = hits[0];
+            float xh = -0.5f * mx2[0].x, yh = -0.5f * my2[0].x;
+#pragma unroll
+            for (int t = 1; t < ILP; t++) {
+                m = (k == t) ? hits[t] : m;
+                xh = (k == t) ? -0.5f * mx2[t].x : xh;
+                yh = (k == t) ? -0.5f * my2[t].x : yh;
+            }
+            if (!__any_sync(0xffffffffu, m != 0u)) continue;
+            const float4 c4 = s_cold[k * 32 + lane];
             PairCtx ic;
             ic.xl = c4.x;
             ic.yl = c4.y;
             ic.qc = c4.z;
             ic.ii = __float_as_int(c4.w);
-            float4 acc = my_acc[K * 32 + lane];
+            float4 acc = my_acc[k * 32 + lane];
+            const int jbase = 4 * cbase;  // j of bit 0
             // up to 4 pair terms are summed plainly, each group then added to
             // the compensated sums (the group's rounding is that of one pair term)
-            do {
+            while (m) {
                 float px = 0.0f, py = 0.0f;
 #pragma unroll 1
-                for (int g = 0; g < 4 && mask; g++) {
-                    const int e = __ffs(mask) - 1;
-                    mask &= mask - 1u;
-                    const int jj = my_queue[K * 32 + e].x;  // index into the tile's j
+                for (int g = 0; g < 4 && m; g++) {
+                    const int e = __ffs(m) - 1;
+                    m &= m - 1u;
+                    const int jj = jbase + (e >> 2) * (4 * NW) + (e & 3);  // index into the tile's j
                     const float4 Bj = s_pb[jj];
-                    const float xj = reinterpret_cast<const float *>(s_x4)[jj];
-                    const float yj = reinterpret_cast<const float *>(s_y4)[jj];
-                    precise_pair(P, b, xh, yh, ic, make_float4(xj, yj, 0.0f, Bj.z), Bj,
+                    precise_pair(P, b, xh, yh, ic, make_float4(s_xf[jj], s_yf[jj], 0.0f, Bj.z), Bj,
                                  __float_as_int(Bj.w), px, py);
                 }
                 kahan_add(acc.x, acc.z, px);
                 kahan_add(acc.y, acc.w, py);
-            } while (mask);
-            my_acc[K * 32 + lane] = acc;
-        }
-        __syncwarp();
-        qn &= ~(0xFFu << (8 * K));
-    };
-
-    // Flushes every slot holding at least `lim` entries (runtime loop: one
-    // copy of the flush in the code).
-    auto flush_slots = [&](int lim) {
-#pragma unroll 1
-        for (int k = 0; k < ILP; k++) {
-            if ((int)((qn >> (8 * k)) & 0xFFu) >= lim) {
-                float xh = -0.5f * mx2[0].x, yh = -0.5f * my2[0].x;
-#pragma unroll
-                for (int t = 1; t < ILP; t++) {
-                    xh = (k == t) ? -0.5f * mx2[t].x : xh;
-                    yh = (k == t) ? -0.5f * my2[t].x : yh;
-                }
-                flush(k, xh, yh);
             }
+            my_acc[k * 32 + lane] = acc;
         }
+#pragma unroll
+        for (int k = 0; k < ILP; k++) hits[k] = 0u;
     };
 
     // Sweeps the `count` chunks (4 consecutive j) of this CTA's list through
@@ -406,48 +396,48 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
 #pragma unroll
             for (int k = 0; k < ILP; k++) my_acc[k * 32 + lane] = acc[k];
         } else {
-        for (int c = warp; c < tcn; c += NW) {
-            const float4 X = s_x4[c], Y = s_y4[c], Bq = s_b4[c];
-            const float2 X01 = make_float2(X.x, X.y), X23 = make_float2(X.z, X.w);
-            const float2 Y01 = make_float2(Y.x, Y.y), Y23 = make_float2(Y.z, Y.w);
-            const float2 B01 = make_float2(Bq.x, Bq.y), B23 = make_float2(Bq.z, Bq.w);
-            // d = |p_j|^2 - 2 p_i.p_j - threshold_i: pair (i, j) passes iff d < 0
-            uint32_t sgn = 0u;
+        // one flush site: the loop runs one step past the tile's last chunk
+        int nb = 0, cbase = warp;  // chunks recorded in hits, chunk of bit group 0
+        bool any_hit = false;      // warp-uniform
+        for (int c = warp;; c += NW) {
+            const bool live = c < tcn;  // warp-uniform
+            if (live) {
+                const float4 X = s_x4[c], Y = s_y4[c], Bq = s_b4[c];
+                const float2 X01 = make_float2(X.x, X.y), X23 = make_float2(X.z, X.w);
+                const float2 Y01 = make_float2(Y.x, Y.y), Y23 = make_float2(Y.z, Y.w);
+                const float2 B01 = make_float2(Bq.x, Bq.y), B23 = make_float2(Bq.z, Bq.w);
+                // d = |p_j|^2 - 2 p_i.p_j - threshold_i: pair (i, j) passes iff d < 0
+                float2 d01[ILP], d23[ILP];
+                uint32_t sgn = 0u;
 #pragma unroll
-            for (int k = 0; k < ILP; k++) {
-                const float2 d01 = __ffma2_rn(mx2[k], X01, __ffma2_rn(my2[k], Y01, __fadd2_rn(B01, nu2[k])));
-                const float2 d23 = __ffma2_rn(mx2[k], X23, __ffma2_rn(my2[k], Y23, __fadd2_rn(B23, nu2[k])));
-                sgn |= __float_as_uint(d01.x) | __float_as_uint(d01.y) | __float_as_uint(d23.x) |
-                       __float_as_uint(d23.y);
-            }
-            if (__any_sync(0xffffffffu, (int)sgn < 0)) {
-                // rare: recompute per j (scalar FMA rounds exactly like the
-                // packed one), ballot per slot, queue the hits
-                const float xs[4] = {X.x, X.y, X.z, X.w};
-                const float ys[4] = {Y.x, Y.y, Y.z, Y.w};
-                const float bs[4] = {Bq.x, Bq.y, Bq.z, Bq.w};
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    static_for<ILP>([&](auto kc) {
-                        constexpr int k = decltype(kc)::value;
-                        const float dk = fmaf(mx2[k].x, xs[u], fmaf(my2[k].x, ys[u], bs[u] + nu2[k].x));
-                        const uint32_t bal = __ballot_sync(0xffffffffu, (int)__float_as_uint(dk) < 0);
-                        if (bal) {
-                            const int fill = (int)((qn >> (8 * k)) & 0xFFu);
-                            if (lane == 0) my_queue[k * 32 + fill] = make_int2(4 * c + u, (int)bal);
-                            qn += 1u << (8 * k);
-                        }
-                    });
+                for (int k = 0; k < ILP; k++) {
+                    d01[k] = __ffma2_rn(mx2[k], X01, __ffma2_rn(my2[k], Y01, __fadd2_rn(B01, nu2[k])));
+                    d23[k] = __ffma2_rn(mx2[k], X23, __ffma2_rn(my2[k], Y23, __fadd2_rn(B23, nu2[k])));
+                    sgn |= __float_as_uint(d01[k].x) | __float_as_uint(d01[k].y) | __float_as_uint(d23[k].x) |
+                           __float_as_uint(d23[k].y);
                 }
-                // a chunk adds at most 4 entries to a slot: keep each slot at
-                // <= 28 so the next chunk fits its 32.  The fills are 8-bit
-                // fields of qn (<= 32 each); adding 99 to every field sets its
-                // top bit exactly when the fill is >= 29.
-                if ((qn + 0x63636363u) & 0x80808080u) flush_slots(29);
+                if (__any_sync(0xffffffffu, (int)sgn < 0)) {
+                    // record this lane's hits: the sign bits of the 4 j
+#pragma unroll
+                    for (int k = 0; k < ILP; k++) {
+                        const uint32_t bits = (__float_as_uint(d01[k].x) >> 31) |
+                                              ((__float_as_uint(d01[k].y) >> 30) & 2u) |
+                                              ((__float_as_uint(d23[k].x) >> 29) & 4u) |
+                                              ((__float_as_uint(d23[k].y) >> 28) & 8u);
+                        hits[k] |= bits << (4 * nb);
+                    }
+                    any_hit = true;
+                }
+                nb++;
+            }
+            if (!live || nb == 8) {  // bits full, or the tile is done: its j are overwritten next
+                if (any_hit) flush_hits(cbase);
+                any_hit = false;
+                nb = 0;
+                cbase = c + NW;
+                if (!live) break;
             }
         }
-        // queued entries index into this tile: drain before it is overwritten
-        flush_slots(1);
         }
     }
     };
