@@ -94,7 +94,7 @@ struct dm_cloud {
     int partial_cap = 0;
     SortScratch sort{};
     int sort_blocks = 0;
-    int reorder_interval = 4;   // steps between Morton re-sorts (0 = never)
+    int reorder_interval = 4;   // steps between Morton re-sorts (0 = never); 1 for n <= kSmallSortMax
     bool order_dirty = true;    // re-sort before the next step
     unsigned long long host_steps = 0;  // RK4 steps enqueued so far
     long long graph_launches = 0;       // kernels in one replay of the step graph
@@ -129,6 +129,8 @@ int check_device_errors(dm_ctx *ctx, dm_cloud *c) {
     if (h) {
         DM_CUDA(ctx, cudaMemsetAsync(c->d.err, 0, sizeof(int), ctx->stream));
         if (h & 2) return ctx->fail(DM_ERR_NUMERIC, "zero particle separation in the adaptive time step test");
+        if (h & kErrSortPermutation)
+            return ctx->fail(DM_ERR_CUDA, "internal error: the Morton sort produced an invalid permutation");
         return ctx->fail(DM_ERR_NUMERIC, "non-finite particle position after a stage (error bits 0x%x)", h);
     }
     return DM_OK;
@@ -250,6 +252,7 @@ int ensure_kernel_attrs(dm_ctx *ctx) {
             DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
     }
+    DM_CUDA(ctx, cudaFuncSetAttribute(sort_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortClusterSmem));
     done[dev] = true;
     return DM_OK;
 }
@@ -531,24 +534,37 @@ int reorder(dm_cloud *c) {
     const int n = c->n;
     const int grid = (n + 255) / 256;
     SortScratch &z = c->sort;
-    const int mblocks = std::min(grid, kMomentBlocks);
-    sort_moments<<<mblocks, 256, 0, s>>>(c->d.x, c->d.y, n, z.moments);
-    sort_box<<<1, 32, 0, s>>>(z.moments, mblocks, c->d.x, c->d.y, z.box);
-    sort_keys<<<grid, 256, 0, s>>>(c->d.x, c->d.y, n, z.box, z.keys[0], z.vals[0]);
     int cur = 0;
-    for (int shift = 0; shift < kSortBits; shift += kSortDigitBits) {
-        radix_hist<<<c->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], n, shift, z.hist);
-        radix_scan<<<1, 1024, 0, s>>>(z.hist, kSortBuckets * c->sort_blocks);
-        radix_scatter<<<c->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], z.vals[cur], z.keys[cur ^ 1],
-                                                               z.vals[cur ^ 1], n, shift, z.hist);
-        cur ^= 1;
+    if (n <= kSmallSortMax) {  // one cluster launch sorts and gathers; one more commits
+        int rc = ensure_kernel_attrs(ctx);
+        if (rc) return rc;
+        sort_cluster<<<kSortClusterCtas, kSortClusterThreads, kSortClusterSmem, s>>>(c->d.pa[0], c->d, z);
+        permute_commit_init<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d, z);
+        c->boxes_valid[0] = c->boxes_valid[1] = false;
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches += 2;
+        c->order_dirty = false;
+        return DM_OK;
+    } else {
+        const int mblocks = std::min(grid, kMomentBlocks);
+        sort_moments<<<mblocks, 256, 0, s>>>(c->d.x, c->d.y, n, z.moments);
+        sort_box<<<1, 32, 0, s>>>(z.moments, mblocks, c->d.x, c->d.y, z.box);
+        sort_keys<<<grid, 256, 0, s>>>(c->d.x, c->d.y, n, z.box, z.keys[0], z.vals[0]);
+        for (int shift = 0; shift < kSortBits; shift += kSortDigitBits) {
+            radix_hist<<<c->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], n, shift, z.hist);
+            radix_scan<<<1, 1024, 0, s>>>(z.hist, kSortBuckets * c->sort_blocks);
+            radix_scatter<<<c->sort_blocks, kSortThreads, 0, s>>>(z.keys[cur], z.vals[cur], z.keys[cur ^ 1],
+                                                                   z.vals[cur ^ 1], n, shift, z.hist);
+            cur ^= 1;
+        }
+        ctx->launches += 3 + 3 * (kSortBits / kSortDigitBits);
     }
     permute_gather<<<grid, 256, 0, s>>>(c->d, z.vals[cur], z);
     permute_commit<<<grid, 256, 0, s>>>(c->d, z);
     init_positions<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d);
     c->boxes_valid[0] = c->boxes_valid[1] = false;
     DM_CUDA(ctx, cudaGetLastError());
-    ctx->launches += 6 + 3 * (kSortBits / kSortDigitBits);
+    ctx->launches += 3;
     c->order_dirty = false;
     return DM_OK;
 }
@@ -779,6 +795,10 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->ctx = ctx;
     c->n = n;
     c->n_pad = (n + 63) & ~63;
+    // the one-block sort costs less than the pair sweeps it saves every step
+    // (a confined cloud's particles cross many cutoffs per step while it
+    // collapses, and a stale order inflates every group box)
+    c->reorder_interval = (n <= kSmallSortMax) ? 1 : 4;
     c->coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);
     c->d.coulomb = c->coulomb;
     c->d.rc2 = (10.0 / 2e4) * (10.0 / 2e4);  // default kappa until set_forces

@@ -67,6 +67,19 @@ __device__ __forceinline__ float exp_neg_kr(float r, float k_hi, float k_lo) {
     return e * fmaf(-t_lo, 0.693147182f, 1.0f);
 }
 
+// Sum kept as an unevaluated pair hi + lo: Knuth's TwoSum gives the exact
+// rounding error of each addition, accumulated in lo (error ~ n eps^2 of the
+// sum of magnitudes).
+struct TwoFloatSum {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float t = hi + v;
+        const float bp = t - hi;
+        lo += (hi - (t - bp)) + (v - bp);
+        hi = t;
+    }
+};
+
 // Kahan (compensated) accumulation: true sum ~= s - c.
 __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
     const float y = v - c;
@@ -573,7 +586,12 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
 static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P.c.n) {
-        double fx = 0.0, fy = 0.0;
+        // each partial (s, c) stands for s - c; the s are summed exactly as
+        // an unevaluated float pair (TwoSum), the small c plainly, in rank
+        // order, and FP64 is used once: FP64 runs at ~1/64 of the FP32 rate
+        // here and an FP64 sum over the ranks dominated this kernel
+        TwoFloatSum sx, sy;
+        float cx = 0.0f, cy = 0.0f;
         const float4 *p = P.partial + i;
         const size_t stride = (size_t)P.c.n_pad;
         int r = 0;
@@ -583,15 +601,21 @@ static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
             for (int u = 0; u < 8; u++) v[u] = p[(size_t)(r + u) * stride];
 #pragma unroll
             for (int u = 0; u < 8; u++) {
-                fx += (double)v[u].x - (double)v[u].z;
-                fy += (double)v[u].y - (double)v[u].w;
+                sx.add(v[u].x);
+                sy.add(v[u].y);
+                cx += v[u].z;
+                cy += v[u].w;
             }
         }
         for (; r < P.split; r++) {
             const float4 v = p[(size_t)r * stride];
-            fx += (double)v.x - (double)v.z;
-            fy += (double)v.y - (double)v.w;
+            sx.add(v.x);
+            sy.add(v.y);
+            cx += v.z;
+            cy += v.w;
         }
+        const double fx = (double)sx.hi + ((double)sx.lo - (double)cx);
+        const double fy = (double)sy.hi + ((double)sy.lo - (double)cy);
         stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
     }
     if (P.box_out) {  // a warp is one 32-particle group: its box in the buffer just written

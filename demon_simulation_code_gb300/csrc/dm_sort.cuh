@@ -12,7 +12,7 @@
 //
 // Sort: 24-bit Morton keys (12 bits per axis) and a deterministic, stable
 // LSD radix sort with 8-bit digits (per-block digit histograms, one scan,
-// stable scatter ranked with __match_any_sync).  No atomics decide any
+// stable scatter ranked by a ballot-based digit match).  No atomics decide any
 // order; the result depends only on the positions.
 //
 // The key box is the bounding box clipped to mean +- 4 standard deviations
@@ -23,9 +23,12 @@
 // longer compact.  Particles outside the clipped box take the edge cells.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "dm_device.cuh"
 
 namespace dm {
+namespace cg = cooperative_groups;
 
 constexpr int kSortThreads = 256;
 constexpr int kSortPerBlock = 4 * kSortThreads;  // keys per block
@@ -164,6 +167,21 @@ __device__ __forceinline__ uint32_t spread_bits12(uint32_t v) {
     return v;
 }
 
+// Lanes of the warp holding the same 8-bit digit as this one, among the
+// lanes with `valid` set: one ballot per digit bit.  Eight ballots cost far
+// less than __match_any_sync when 32 warps of one block issue them (the
+// match unit's throughput, not the ballots', bounds a one-block sort).
+__device__ __forceinline__ uint32_t match_digit8(uint32_t d, bool valid) {
+    uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < kSortDigitBits; b++) {
+        const bool bit = (d >> b) & 1u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+        m &= bit ? bal : ~bal;
+    }
+    return m;
+}
+
 static __global__ void sort_keys(const double *__restrict__ x, const double *__restrict__ y, int n,
                                  const double *__restrict__ box, uint32_t *keys, int *vals) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -228,8 +246,8 @@ static __global__ void __launch_bounds__(kSortThreads) radix_scatter(
         const int e = blockIdx.x * kSortPerBlock + k * kSortThreads + threadIdx.x;
         const bool valid = e < n;
         const uint32_t key = valid ? kin[e] : 0u;
-        const int d = valid ? (int)((key >> shift) & (kSortBuckets - 1)) : kSortBuckets;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const int d = (int)((key >> shift) & (kSortBuckets - 1));
+        const uint32_t peers = match_digit8((uint32_t)d, valid);
         const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
         if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
         __syncthreads();
@@ -246,6 +264,277 @@ static __global__ void __launch_bounds__(kSortThreads) radix_scatter(
             base[threadIdx.x] += add;
         }
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One-launch sort for clouds of up to kSmallSortMax particles: a cluster of
+// kSortClusterCtas blocks, block r owning sorted positions [r*P, (r+1)*P),
+// P = kSmallSortMax / kSortClusterCtas.  Key box, keys, the three 8-bit LSD
+// passes and the gather of the cloud's arrays in the new order run in one
+// launch: per pass each block counts its digits per warp, the blocks'
+// digit totals meet through distributed shared memory, and every element is
+// stored straight into the shared memory of the block owning its new
+// position.  The multi-kernel path above needs fifteen dependent launches
+// (~0.1 ms at n = 16384); a single block was no better (one SM's issue rate).
+//
+// Element order: block r, warp w, round k, lane l is element r*P +
+// w*32*kSortClusterRounds + k*32 + l.  Digits are ranked in that order (lanes with equal digits found
+// by match_digit8) and bases are laid out digit-major over (digit, block,
+// warp), so the sort is stable and depends only on the positions.  The key
+// box and keys are FP32 functions of the positions' hi parts: GB300's FP64
+// rate (~2 FMA per clock per SM) would dominate a pass over 16384 doubles,
+// and any order is correct (the permutation moves every array together).
+// ---------------------------------------------------------------------------
+constexpr int kSmallSortMax = 16384;
+constexpr int kErrSortPermutation = 8;  // error bit: the cluster sort's ranks were inconsistent
+constexpr int kSortClusterCtas = 8;  // portable cluster size
+constexpr int kSortClusterThreads = 512;
+constexpr int kSortClusterWarps = kSortClusterThreads / 32;
+constexpr int kSortClusterPer = kSmallSortMax / kSortClusterCtas;        // 2048 elements per block
+constexpr int kSortClusterRounds = kSortClusterPer / kSortClusterThreads;  // 4 per thread
+
+struct SortClusterSmem {
+    uint32_t keys[2][kSortClusterPer];
+    uint16_t slot[2][kSortClusterPer];
+    uint32_t wcnt[kSortClusterWarps][kSortBuckets];  // per-warp digit counts, then offsets within the block
+    uint32_t ctot[kSortBuckets];      // this block's digit totals (read by the whole cluster)
+    uint32_t dbase[kSortBuckets];     // first sorted position of (digit, this block)
+    uint32_t part[kSortBuckets / 32];
+    float wmom[kSortClusterWarps][kMomentFields];
+    float mom[kMomentFields];  // this block's moments (read by the whole cluster)
+    float box[3];
+};
+constexpr size_t kSortClusterSmem = sizeof(SortClusterSmem);
+
+__device__ __forceinline__ void moments_f32_add(float *v, float4 a, float ox, float oy) {
+    if (!(isfinite(a.x) && isfinite(a.y))) return;
+    const float dx = a.x - ox, dy = a.y - oy;
+    v[0] += 1.0f;
+    v[1] += dx;
+    v[2] += dy;
+    v[3] = fmaf(dx, dx, v[3]);
+    v[4] = fmaf(dy, dy, v[4]);
+    v[5] = fminf(v[5], a.x);
+    v[6] = fminf(v[6], a.y);
+    v[7] = fmaxf(v[7], a.x);
+    v[8] = fmaxf(v[8], a.y);
+}
+
+__device__ __forceinline__ void moments_f32_merge(float *v, const float *o) {
+    for (int k = 0; k < 5; k++) v[k] += o[k];
+    v[5] = fminf(v[5], o[5]);
+    v[6] = fminf(v[6], o[6]);
+    v[7] = fmaxf(v[7], o[7]);
+    v[8] = fmaxf(v[8], o[8]);
+}
+
+// pa0: the FP32 hi parts of the current positions (stage buffer 0 holds them
+// at every step boundary).  perm (optional): new slot -> old slot.  The
+// cloud's x, y, vx, vy, q, m and orig are gathered in the new order into the
+// staging arrays of z (permute_commit_init copies them back).
+static __global__ void __cluster_dims__(kSortClusterCtas, 1, 1) __launch_bounds__(kSortClusterThreads, 1)
+    sort_cluster(const float4 *__restrict__ pa0, CloudDev c, SortScratch z) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SortClusterSmem &S = *reinterpret_cast<SortClusterSmem *>(smem_raw);
+    cg::cluster_group cl = cg::this_cluster();
+    const int r = (int)cl.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = c.n;
+    const int e0 = r * kSortClusterPer;
+
+    // this block's positions, loaded once (moments, then keys)
+    float4 pos[kSortClusterRounds];
+#pragma unroll
+    for (int k = 0; k < kSortClusterRounds; k++) {
+        const int e = e0 + k * kSortClusterThreads + tid;
+        pos[k] = (e < n) ? pa0[e] : make_float4(NAN, NAN, 0.0f, 0.0f);
+    }
+    // moments of this block's slice, then of the cloud: lanes 0..7 of warp 0
+    // fetch the eight blocks' moments and merge them in a fixed butterfly
+    // (commutative steps), so every block derives the same key box
+    const float4 p0 = pa0[0];
+    const float ox = isfinite(p0.x) ? p0.x : 0.0f, oy = isfinite(p0.y) ? p0.y : 0.0f;
+    {
+        float v[kMomentFields] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, INFINITY, INFINITY, -INFINITY, -INFINITY};
+#pragma unroll
+        for (int k = 0; k < kSortClusterRounds; k++) moments_f32_add(v, pos[k], ox, oy);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            float o[kMomentFields];
+#pragma unroll
+            for (int k = 0; k < kMomentFields; k++) o[k] = __shfl_xor_sync(0xffffffffu, v[k], off);
+            moments_f32_merge(v, o);
+        }
+        if (lane == 0)
+            for (int k = 0; k < kMomentFields; k++) S.wmom[warp][k] = v[k];
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < kSortClusterWarps; w++) moments_f32_merge(v, S.wmom[w]);
+            for (int k = 0; k < kMomentFields; k++) S.mom[k] = v[k];
+        }
+    }
+    cl.sync();
+    if (warp == 0) {
+        float v[kMomentFields];
+        const float *mb = cl.map_shared_rank(S.mom, lane & (kSortClusterCtas - 1));
+#pragma unroll
+        for (int k = 0; k < kMomentFields; k++) v[k] = mb[k];
+#pragma unroll
+        for (int off = 1; off < kSortClusterCtas; off <<= 1) {
+            float o[kMomentFields];
+#pragma unroll
+            for (int k = 0; k < kMomentFields; k++) o[k] = __shfl_xor_sync(0xffffffffu, v[k], off);
+            moments_f32_merge(v, o);
+        }
+        if (lane == 0) {
+            // bounding box clipped to mean +- 4 sd per axis
+            float lo[2] = {0.0f, 0.0f}, hi[2] = {0.0f, 0.0f};
+            if (v[0] > 0.0f) {
+                const float org[2] = {ox, oy};
+                for (int a = 0; a < 2; a++) {
+                    const float mean = v[1 + a] / v[0];
+                    const float sd = sqrtf(fmaxf(v[3 + a] / v[0] - mean * mean, 0.0f));
+                    lo[a] = fmaxf(v[5 + a], org[a] + mean - 4.0f * sd);
+                    hi[a] = fminf(v[7 + a], org[a] + mean + 4.0f * sd);
+                    if (!(lo[a] <= hi[a])) {
+                        lo[a] = v[5 + a];
+                        hi[a] = v[7 + a];
+                    }
+                }
+            }
+            S.box[0] = lo[0];
+            S.box[1] = lo[1];
+            S.box[2] = fmaxf(hi[0] - lo[0], hi[1] - lo[1]);
+            if (r == 0) {  // the key box and the bounding box, as the multi-kernel path writes them
+                z.box[0] = S.box[0];
+                z.box[1] = S.box[1];
+                z.box[2] = S.box[2];
+                z.box[3] = 0.0;
+                for (int k = 0; k < 4; k++) z.box[4 + k] = (v[0] > 0.0f) ? (double)v[5 + k] : 0.0;
+            }
+        }
+    }
+    __syncthreads();
+    {
+        const float x0 = S.box[0], y0 = S.box[1], ext = S.box[2];
+        const float scale = (ext > 0.0f && isfinite(ext)) ? 4095.0f / ext : 0.0f;
+#pragma unroll
+        for (int k = 0; k < kSortClusterRounds; k++) {
+            const int li = k * kSortClusterThreads + tid, e = e0 + li;
+            uint32_t key = 0u;
+            if (e < n) {
+                const float fx = (pos[k].x - x0) * scale, fy = (pos[k].y - y0) * scale;
+                const uint32_t qx = (fx > 0.0f) ? (uint32_t)fminf(fx, 4095.0f) : 0u;  // NaN: 0
+                const uint32_t qy = (fy > 0.0f) ? (uint32_t)fminf(fy, 4095.0f) : 0u;
+                key = spread_bits12(qx) | (spread_bits12(qy) << 1);
+            }
+            S.keys[0][li] = key;
+            S.slot[0][li] = (uint16_t)e;
+        }
+    }
+    __syncthreads();
+
+    const uint32_t lower = (1u << lane) - 1u;
+    int cur = 0;
+    for (int shift = 0; shift < kSortBits; shift += kSortDigitBits) {
+        for (int d = lane; d < kSortBuckets; d += 32) S.wcnt[warp][d] = 0u;
+        __syncwarp();
+        uint32_t dk[kSortClusterRounds], rk[kSortClusterRounds];
+#pragma unroll
+        for (int k = 0; k < kSortClusterRounds; k++) {
+            const int li = warp * (32 * kSortClusterRounds) + k * 32 + lane;
+            const bool valid = e0 + li < n;
+            const uint32_t d = (S.keys[cur][li] >> shift) & (kSortBuckets - 1);
+            const uint32_t peers = match_digit8(d, valid);
+            rk[k] = S.wcnt[warp][d] + __popc(peers & lower);  // rank within the warp
+            dk[k] = valid ? d : kSortBuckets;
+            __syncwarp();
+            if (valid && (peers & lower) == 0u) S.wcnt[warp][d] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        if (tid < kSortBuckets) {  // per digit: offsets of the warps, block total
+            uint32_t run = 0u;
+            for (int w = 0; w < kSortClusterWarps; w++) {
+                const uint32_t v = S.wcnt[w][tid];
+                S.wcnt[w][tid] = run;
+                run += v;
+            }
+            S.ctot[tid] = run;
+        }
+        cl.sync();  // every block's totals are complete
+        uint32_t tot = 0u, pre = 0u, inc = 0u;
+        if (tid < kSortBuckets) {
+            for (int b = 0; b < kSortClusterCtas; b++) {
+                const uint32_t v = *cl.map_shared_rank(&S.ctot[tid], b);
+                tot += v;
+                pre += (b < r) ? v : 0u;
+            }
+            inc = tot;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, off);
+                if (lane >= off) inc += v;
+            }
+            if (lane == 31) S.part[warp] = inc;
+        }
+        __syncthreads();
+        if (tid < kSortBuckets) {
+            uint32_t wb = 0u;
+            for (int w = 0; w < warp; w++) wb += S.part[w];
+            S.dbase[tid] = wb + inc - tot + pre;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortClusterRounds; k++) {
+            if (dk[k] < (uint32_t)kSortBuckets) {
+                const int li = warp * (32 * kSortClusterRounds) + k * 32 + lane;
+                const uint32_t pos = S.dbase[dk[k]] + S.wcnt[warp][dk[k]] + rk[k];
+                if (pos >= (uint32_t)n) {  // cannot happen for a consistent count; never store out of range
+                    atomicOr(c.err, kErrSortPermutation);
+                    continue;
+                }
+                const int dst = (int)(pos / kSortClusterPer), off = (int)(pos % kSortClusterPer);
+                *cl.map_shared_rank(&S.keys[cur ^ 1][off], dst) = S.keys[cur][li];
+                *cl.map_shared_rank(&S.slot[cur ^ 1][off], dst) = S.slot[cur][li];
+            }
+        }
+        cl.sync();  // all elements placed; all remote reads of this pass done
+        cur ^= 1;
+    }
+
+    // gather: new slot s takes old slot S.slot[cur][s - e0]; every load is
+    // issued before any store (the arrays do not alias)
+    int src[kSortClusterRounds];
+#pragma unroll
+    for (int k = 0; k < kSortClusterRounds; k++) {
+        const int li = k * kSortClusterThreads + tid, s = e0 + li;
+        int o = (s < n) ? (int)S.slot[cur][li] : 0;
+        if (s < n && o >= n) {  // as above: flag and keep the slot rather than read out of range
+            atomicOr(c.err, kErrSortPermutation);
+            o = s;
+        }
+        src[k] = o;
+    }
+    const double *__restrict__ in[6] = {c.x, c.y, c.vx, c.vy, c.q, c.m};
+    double val[6][kSortClusterRounds];
+    int ov[kSortClusterRounds];
+#pragma unroll
+    for (int k = 0; k < kSortClusterRounds; k++) {
+        const bool ok = e0 + k * kSortClusterThreads + tid < n;
+#pragma unroll
+        for (int a = 0; a < 6; a++) val[a][k] = ok ? __ldg(in[a] + src[k]) : 0.0;
+        ov[k] = ok ? __ldg(c.orig + src[k]) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kSortClusterRounds; k++) {
+        const int s = e0 + k * kSortClusterThreads + tid;
+        if (s < n) {
+#pragma unroll
+            for (int a = 0; a < 6; a++) z.stage[a][s] = val[a][k];
+            z.orig_stage[s] = ov[k];
+        }
     }
 }
 
@@ -275,6 +564,33 @@ static __global__ void permute_commit(CloudDev c, SortScratch z) {
     c.q[s] = z.stage[4][s];
     c.m[s] = z.stage[5][s];
     c.orig[s] = z.orig_stage[s];
+}
+
+// permute_commit and init_positions in one launch: copy the gathered arrays
+// back, and write stage buffer 0 from the new positions.
+static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= c.n_pad) return;
+    if (s < c.n) {
+        const double x = z.stage[0][s], y = z.stage[1][s];
+        c.x[s] = x;
+        c.y[s] = y;
+        c.vx[s] = z.stage[2][s];
+        c.vy[s] = z.stage[3][s];
+        c.q[s] = z.stage[4][s];
+        c.m[s] = z.stage[5][s];
+        c.orig[s] = z.orig_stage[s];
+        write_stage_position(c, 0, s, x, y);
+    } else {
+        for (int b = 0; b < 2; b++) {
+            c.px[b][s] = (double)kPadPosition;
+            c.py[b][s] = (double)kPadPosition;
+            c.pa[b][s] = make_float4(kPadPosition, kPadPosition, kPadPosition * kPadPosition, 0.0f);
+            c.pb[b][s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        c.q[s] = 0.0;
+        c.m[s] = 1.0;
+    }
 }
 
 static __global__ void set_identity(int *orig, int n) {
