@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -454,6 +455,8 @@ int tune_precision(dm_cloud *c, int precision) {
         DM_CUDA(ctx, cudaEventCreate(&a));
         DM_CUDA(ctx, cudaEventCreate(&b));
         float best_ms = 1e30f;
+        const char *ev = getenv("DM_TUNE_VERBOSE");  // per-candidate timings on stderr
+        const bool verbose = ev && ev[0] && ev[0] != '0';
         for (int vi = 0; vi < kNumVariants; vi++) {
             const Variant &k = kVariants[vi];
             if (k.precision != precision) continue;
@@ -482,7 +485,7 @@ int tune_precision(dm_cloud *c, int precision) {
                     if (rc) return rc;
                 }
                 const int reps = big ? 1 : 3;
-                float ms = 0.0f;
+                float ms = 0.0f, ms_state[2] = {0.0f, 0.0f};
                 for (int st = 0; st < nstates; st++) {
                     c->fo_buf = st;
                     int rc = launch_variant(c, vi, S, 1, kModeForceOnly, 0.0, nullptr);  // warm-up
@@ -495,8 +498,12 @@ int tune_precision(dm_cloud *c, int precision) {
                     float one = 0.0f;
                     DM_CUDA(ctx, cudaEventElapsedTime(&one, a, b));
                     ms += one;
+                    ms_state[st] = one / reps;
                 }
                 ms /= reps;
+                if (verbose)
+                    fprintf(stderr, "dm autotune n=%d %s split %d: %.4f ms (state) %.4f ms (dense copy)\n", c->n,
+                            k.name, S, ms_state[0], ms_state[1]);
                 if (ms < best_ms) {
                     best_ms = ms;
                     best_v = vi;
@@ -1313,7 +1320,8 @@ struct dm_batch {
     int ngroups = 0;            // 32-particle groups over all clouds
     int *dgseg = nullptr;       // [ngroups] cloud of each group
     int variant = -1;
-    int reorder_interval = 4;
+    int reorder_interval = 4;  // 1 when every cloud fits batch_sort_clouds
+    int max_n = 0;             // largest cloud
     int order = 4;  // integrator: 4 = Runge_Kutta4, 2 = Runge_Kutta2
     bool order_dirty = true;
     unsigned long long host_steps = 0;
@@ -1368,6 +1376,17 @@ int batch_reorder(dm_batch *B) {
     const int n = B->total;
     const int grid = (n + 255) / 256;
     SortScratch &z = B->sort;
+    if (B->max_n <= kBatchSortMax) {  // one block per cloud sorts and gathers; two more commit
+        DM_CUDA(ctx, cudaFuncSetAttribute(batch_sort_clouds, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kBatchSortSmem));
+        batch_sort_clouds<<<B->nclouds, kBatchSortThreads, kBatchSortSmem, s>>>(B->d, B->ddesc, B->dbox, z);
+        permute_commit<<<grid, 256, 0, s>>>(B->d, z);
+        batch_init_positions<<<(B->total_pad + 255) / 256, 256, 0, s>>>(B->d, B->ddesc, B->dseg);
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches += 3;
+        B->order_dirty = false;
+        return DM_OK;
+    }
     batch_boxes<<<B->nclouds, 256, 0, s>>>(B->d.x, B->d.y, B->ddesc, B->dbox);
     batch_keys<<<grid, 256, 0, s>>>(B->d.x, B->d.y, n, B->dseg, B->dbox, B->mbits, z.keys[0], z.vals[0]);
     int cur = 0;
@@ -1445,6 +1464,8 @@ int batch_tune(dm_batch *B) {
         DM_CUDA(ctx, cudaEventCreate(&a));
         DM_CUDA(ctx, cudaEventCreate(&b));
         float best_ms = 1e30f;
+        const char *ev = getenv("DM_TUNE_VERBOSE");  // per-candidate timings on stderr
+        const bool verbose = ev && ev[0] && ev[0] != '0';
         for (int v = 0; v < kNumBatchVariants; v++) {
             B->variant = v;
             float total = 0.0f;
@@ -1508,6 +1529,10 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     B->total = (int)total;
     B->total_pad = ((int)total + 63) & ~63;
     B->hn.assign(n, n + nclouds);
+    B->max_n = *std::max_element(n, n + nclouds);
+    // per-cloud sort in one launch: cheap enough to keep every cloud's order
+    // fresh each step (confined clouds collapse and their groups spread)
+    B->reorder_interval = (B->max_n <= kBatchSortMax) ? 1 : 4;
     const int cbits = 32 - __builtin_clz((unsigned)std::max(nclouds - 1, 1));
     B->mbits = std::min(24, (32 - cbits) & ~1);
     const double coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);

@@ -147,6 +147,205 @@ static __global__ void batch_keys(const double *__restrict__ x, const double *__
     vals[i] = i;
 }
 
+// ---------------------------------------------------------------------------
+// Per-cloud sort for batches whose clouds all hold at most kBatchSortMax
+// particles: block b sorts cloud b on its own -- key box, 24-bit Morton keys,
+// three stable 8-bit LSD passes in shared memory -- and gathers the cloud's
+// state in the new order into the staging arrays (permute_commit copies it
+// back).  One launch replaces the batch-wide path (per-cloud boxes, keys with
+// the cloud index in the high bits, four radix passes over every particle of
+// every cloud, gather: fifteen dependent launches).  As in sort_cluster the
+// key box and keys are FP32 functions of the positions' hi parts (stage
+// buffer 0), lanes with equal digits are found by match_digit8, and the
+// element order (warp, round, lane) makes every pass stable.
+// ---------------------------------------------------------------------------
+constexpr int kBatchSortMax = 4096;
+constexpr int kBatchSortThreads = 1024;
+constexpr int kBatchSortWarps = kBatchSortThreads / 32;
+constexpr int kBatchSortRounds = kBatchSortMax / kBatchSortThreads;  // 4 per thread
+
+struct BatchSortSmem {
+    uint32_t keys[2][kBatchSortMax];
+    uint16_t slot[2][kBatchSortMax];
+    uint32_t wcnt[kBatchSortWarps][kSortBuckets];  // per-warp digit counts, then offsets
+    uint32_t dbase[kSortBuckets];
+    uint32_t part[kSortBuckets / 32];
+    float wmom[kBatchSortWarps][kMomentFields];
+    float box[3];
+};
+constexpr size_t kBatchSortSmem = sizeof(BatchSortSmem);
+
+// box_out[8 * cloud]: key box x0, y0, extent, 0, bounding box min x, min y,
+// max x, max y (as batch_boxes writes them; the batch autotuner reads it).
+static __global__ void __launch_bounds__(kBatchSortThreads, 1)
+    batch_sort_clouds(CloudDev c, const BatchCloud *__restrict__ desc, double *box_out, SortScratch z) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    BatchSortSmem &S = *reinterpret_cast<BatchSortSmem *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const BatchCloud d = desc[blockIdx.x];
+    const int off = d.off, n = d.n;
+    const float4 *__restrict__ pa0 = c.pa[0] + off;
+
+    float4 pos[kBatchSortRounds];
+#pragma unroll
+    for (int k = 0; k < kBatchSortRounds; k++) {
+        const int e = k * kBatchSortThreads + tid;
+        pos[k] = (e < n) ? pa0[e] : make_float4(NAN, NAN, 0.0f, 0.0f);
+    }
+    const float4 p0 = pa0[0];
+    const float ox = isfinite(p0.x) ? p0.x : 0.0f, oy = isfinite(p0.y) ? p0.y : 0.0f;
+    {
+        float v[kMomentFields] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, INFINITY, INFINITY, -INFINITY, -INFINITY};
+#pragma unroll
+        for (int k = 0; k < kBatchSortRounds; k++) moments_f32_add(v, pos[k], ox, oy);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            float w[kMomentFields];
+#pragma unroll
+            for (int k = 0; k < kMomentFields; k++) w[k] = __shfl_xor_sync(0xffffffffu, v[k], o);
+            moments_f32_merge(v, w);
+        }
+        if (lane == 0)
+            for (int k = 0; k < kMomentFields; k++) S.wmom[warp][k] = v[k];
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < kBatchSortWarps; w++) moments_f32_merge(v, S.wmom[w]);
+            float lo[2] = {0.0f, 0.0f}, hi[2] = {0.0f, 0.0f};
+            if (v[0] > 0.0f) {
+                const float org[2] = {ox, oy};
+                for (int a = 0; a < 2; a++) {
+                    const float mean = v[1 + a] / v[0];
+                    const float sd = sqrtf(fmaxf(v[3 + a] / v[0] - mean * mean, 0.0f));
+                    lo[a] = fmaxf(v[5 + a], org[a] + mean - 4.0f * sd);
+                    hi[a] = fminf(v[7 + a], org[a] + mean + 4.0f * sd);
+                    if (!(lo[a] <= hi[a])) {
+                        lo[a] = v[5 + a];
+                        hi[a] = v[7 + a];
+                    }
+                }
+            }
+            S.box[0] = lo[0];
+            S.box[1] = lo[1];
+            S.box[2] = fmaxf(hi[0] - lo[0], hi[1] - lo[1]);
+            double *bo = box_out + 8 * blockIdx.x;
+            bo[0] = S.box[0];
+            bo[1] = S.box[1];
+            bo[2] = S.box[2];
+            bo[3] = 0.0;
+            for (int k = 0; k < 4; k++) bo[4 + k] = (v[0] > 0.0f) ? (double)v[5 + k] : 0.0;
+        }
+        __syncthreads();
+    }
+    {
+        const float x0 = S.box[0], y0 = S.box[1], ext = S.box[2];
+        const float scale = (ext > 0.0f && isfinite(ext)) ? 4095.0f / ext : 0.0f;
+#pragma unroll
+        for (int k = 0; k < kBatchSortRounds; k++) {
+            const int li = k * kBatchSortThreads + tid;
+            uint32_t key = 0u;
+            if (li < n) {
+                const float fx = (pos[k].x - x0) * scale, fy = (pos[k].y - y0) * scale;
+                const uint32_t qx = (fx > 0.0f) ? (uint32_t)fminf(fx, 4095.0f) : 0u;  // NaN: 0
+                const uint32_t qy = (fy > 0.0f) ? (uint32_t)fminf(fy, 4095.0f) : 0u;
+                key = spread_bits12(qx) | (spread_bits12(qy) << 1);
+            }
+            S.keys[0][li] = key;
+            S.slot[0][li] = (uint16_t)li;
+        }
+    }
+    __syncthreads();
+
+    const uint32_t lower = (1u << lane) - 1u;
+    int cur = 0;
+    for (int shift = 0; shift < kSortBits; shift += kSortDigitBits) {
+        for (int dg = lane; dg < kSortBuckets; dg += 32) S.wcnt[warp][dg] = 0u;
+        __syncwarp();
+        uint32_t dk[kBatchSortRounds], rk[kBatchSortRounds];
+#pragma unroll
+        for (int k = 0; k < kBatchSortRounds; k++) {
+            const int li = warp * (32 * kBatchSortRounds) + k * 32 + lane;
+            const bool valid = li < n;
+            const uint32_t dg = (S.keys[cur][li] >> shift) & (kSortBuckets - 1);
+            const uint32_t peers = match_digit8(dg, valid);
+            rk[k] = S.wcnt[warp][dg] + __popc(peers & lower);
+            dk[k] = valid ? dg : kSortBuckets;
+            __syncwarp();
+            if (valid && (peers & lower) == 0u) S.wcnt[warp][dg] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        uint32_t tot = 0u, inc = 0u;
+        if (tid < kSortBuckets) {  // per digit: offsets of the warps, block total, scan over digits
+            for (int w = 0; w < kBatchSortWarps; w++) {
+                const uint32_t v = S.wcnt[w][tid];
+                S.wcnt[w][tid] = tot;
+                tot += v;
+            }
+            inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            if (lane == 31) S.part[warp] = inc;
+        }
+        __syncthreads();
+        if (tid < kSortBuckets) {
+            uint32_t wb = 0u;
+            for (int w = 0; w < warp; w++) wb += S.part[w];
+            S.dbase[tid] = wb + inc - tot;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kBatchSortRounds; k++) {
+            if (dk[k] < (uint32_t)kSortBuckets) {
+                const int li = warp * (32 * kBatchSortRounds) + k * 32 + lane;
+                const uint32_t p = S.dbase[dk[k]] + S.wcnt[warp][dk[k]] + rk[k];
+                if (p >= (uint32_t)n) {  // cannot happen for a consistent count; never store out of range
+                    atomicOr(c.err, kErrSortPermutation);
+                    continue;
+                }
+                S.keys[cur ^ 1][p] = S.keys[cur][li];
+                S.slot[cur ^ 1][p] = S.slot[cur][li];
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+
+    // gather the cloud's state in the new order (all loads before the stores)
+    int src[kBatchSortRounds];
+#pragma unroll
+    for (int k = 0; k < kBatchSortRounds; k++) {
+        const int li = k * kBatchSortThreads + tid;
+        int o = (li < n) ? (int)S.slot[cur][li] : 0;
+        if (li < n && o >= n) {
+            atomicOr(c.err, kErrSortPermutation);
+            o = li;
+        }
+        src[k] = off + o;
+    }
+    const double *__restrict__ in[6] = {c.x, c.y, c.vx, c.vy, c.q, c.m};
+    double val[6][kBatchSortRounds];
+    int ov[kBatchSortRounds];
+#pragma unroll
+    for (int k = 0; k < kBatchSortRounds; k++) {
+        const bool ok = k * kBatchSortThreads + tid < n;
+#pragma unroll
+        for (int a = 0; a < 6; a++) val[a][k] = ok ? __ldg(in[a] + src[k]) : 0.0;
+        ov[k] = ok ? __ldg(c.orig + src[k]) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kBatchSortRounds; k++) {
+        const int li = k * kBatchSortThreads + tid;
+        if (li < n) {
+#pragma unroll
+            for (int a = 0; a < 6; a++) z.stage[a][off + li] = val[a][k];
+            z.orig_stage[off + li] = ov[k];
+        }
+    }
+}
+
 // For the batch autotuner: every cloud squeezed about its own box centre
 // so that ~30% of its pairs are inside its cutoff (clouds already that dense
 // are copied as they are), written as stage buffer 1 (nothing live there
