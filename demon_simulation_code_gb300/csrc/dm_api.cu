@@ -14,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/demon_gb300.h"
@@ -258,21 +259,44 @@ int ensure_kernel_attrs(dm_ctx *ctx) {
     return DM_OK;
 }
 
+// Launch of a kernel that starts with pdl_wait(): it may be scheduled while
+// the previous kernel in the stream finishes.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                       Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 int variant_groups(const Variant &k) { return k.precision == DM_FP64 ? kG64 : k.nt / 32; }
 
+// attr must hold 2 entries: programmatic serialization (see pdl_wait) and,
+// for cluster variants, the cluster shape.
 cudaLaunchConfig_t make_cfg(dm_ctx *ctx, const Variant &k, int ntiles, int S, cudaLaunchAttribute *attr) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ntiles * S, 1, 1);
     cfg.blockDim = dim3(k.nt, 1, 1);
     cfg.dynamicSmemBytes = k.smem;
     cfg.stream = ctx->stream;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     if (k.cluster) {
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = S;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
+        attr[1].id = cudaLaunchAttributeClusterDimension;
+        attr[1].val.clusterDim.x = S;
+        attr[1].val.clusterDim.y = 1;
+        attr[1].val.clusterDim.z = 1;
+        cfg.numAttrs = 2;
     }
     return cfg;
 }
@@ -292,7 +316,7 @@ int model_split(dm_ctx *ctx, const Variant &k, int n, int n_pad) {
         if (S > 1 && n_pad / S < 64 * variant_groups(k)) break;
         int slots = 0;
         if (k.cluster) {
-            cudaLaunchAttribute attr[1];
+            cudaLaunchAttribute attr[2];
             cudaLaunchConfig_t cfg = make_cfg(ctx, k, ntiles, S, attr);
             if (cudaOccupancyMaxActiveClusters(&slots, k.fn, &cfg) != cudaSuccess) {
                 cudaGetLastError();
@@ -343,12 +367,11 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
     P.split = S;
     P.partial = c->partial;
     const int ntiles = (c->n + k.tile - 1) / k.tile;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     cudaLaunchConfig_t cfg = make_cfg(ctx, k, ntiles, S, attr);
     const int br = (mode == kModeForceOnly) ? c->fo_buf : (stage - 1) & 1;  // buffer read
     if (k.cull && !c->boxes_valid[br]) {  // boxes of the buffer this stage reads
-        group_bounds<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d, br);
-        DM_CUDA(ctx, cudaGetLastError());
+        DM_CUDA(ctx, launch_pdl(group_bounds, dim3((c->n_pad + 255) / 256), dim3(256), 0, ctx->stream, c->d, br));
         ctx->launches++;
         c->boxes_valid[br] = true;
     }
@@ -357,8 +380,7 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
     if (!k.cluster) {
         // stage_finish also writes the group boxes of the buffer the stage writes
         P.box_out = (mode != kModeForceOnly) ? 1 : 0;
-        stage_finish<<<(c->n + 63) / 64, 64, 0, ctx->stream>>>(P);
-        DM_CUDA(ctx, cudaGetLastError());
+        DM_CUDA(ctx, launch_pdl(stage_finish, dim3((c->n + 63) / 64), dim3(64), 0, ctx->stream, P));
         ctx->launches++;
     }
     if (mode != kModeForceOnly) c->boxes_valid[stage & 1] = !k.cluster;
@@ -474,7 +496,7 @@ int tune_precision(dm_cloud *c, int precision) {
                 if (S > 1 && c->n_pad / S < 64 * variant_groups(k)) continue;
                 if (k.cluster) {
                     int nc = 0;
-                    cudaLaunchAttribute attr[1];
+                    cudaLaunchAttribute attr[2];
                     cudaLaunchConfig_t cfg = make_cfg(ctx, k, (c->n + k.tile - 1) / k.tile, S, attr);
                     if (cudaOccupancyMaxActiveClusters(&nc, k.fn, &cfg) != cudaSuccess || nc <= 0) {
                         cudaGetLastError();
@@ -545,8 +567,9 @@ int reorder(dm_cloud *c) {
     if (n <= kSmallSortMax) {  // one cluster launch sorts and gathers; one more commits
         int rc = ensure_kernel_attrs(ctx);
         if (rc) return rc;
-        sort_cluster<<<kSortClusterCtas, kSortClusterThreads, kSortClusterSmem, s>>>(c->d.pa[0], c->d, z);
-        permute_commit_init<<<(c->n_pad + 255) / 256, 256, 0, s>>>(c->d, z);
+        DM_CUDA(ctx, launch_pdl(sort_cluster, dim3(kSortClusterCtas), dim3(kSortClusterThreads), kSortClusterSmem,
+                                s, (const float4 *)c->d.pa[0], c->d, z));
+        DM_CUDA(ctx, launch_pdl(permute_commit_init, dim3((c->n_pad + 255) / 256), dim3(256), 0, s, c->d, z));
         c->boxes_valid[0] = c->boxes_valid[1] = false;
         DM_CUDA(ctx, cudaGetLastError());
         ctx->launches += 2;
@@ -1181,7 +1204,7 @@ int dm_cloud_set_kernel(dm_cloud *c, const char *variant, int split) {
     if (split == 0) split = model_split(ctx, k, c->n, c->n_pad);
     if (k.cluster) {
         int nc = 0;
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         cudaLaunchConfig_t cfg = make_cfg(ctx, k, (c->n + k.tile - 1) / k.tile, split, attr);
         if (cudaOccupancyMaxActiveClusters(&nc, k.fn, &cfg) != cudaSuccess || nc <= 0) {
             cudaGetLastError();
@@ -1464,8 +1487,6 @@ int batch_tune(dm_batch *B) {
         DM_CUDA(ctx, cudaEventCreate(&a));
         DM_CUDA(ctx, cudaEventCreate(&b));
         float best_ms = 1e30f;
-        const char *ev = getenv("DM_TUNE_VERBOSE");  // per-candidate timings on stderr
-        const bool verbose = ev && ev[0] && ev[0] != '0';
         for (int v = 0; v < kNumBatchVariants; v++) {
             B->variant = v;
             float total = 0.0f;

@@ -44,6 +44,7 @@ static __global__ void tune_compress(CloudDev c, double cx, double cy, double la
 // stage buffer b, for the culling pair kernels: one warp per group; padding
 // particles are left out, so an all-padding group gets an empty box.
 static __global__ void group_bounds(CloudDev c, int b) {
+    pdl_wait();
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     const int i = 32 * g + lane;

@@ -543,6 +543,7 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
 template <int NW, int ILP, int TC, bool CL, bool CULL = false>
 __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+    pdl_wait();
     constexpr int TILE = 32 * ILP;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int S = CL ? (int)cg::this_cluster().num_blocks() : P.split;
@@ -584,6 +585,7 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
 // split partial sums in rank order (FP64), then the stage epilogue.  One
 // particle per thread: the FP64 work runs in full warps on every SM.
 static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P.c.n) {
         // each partial (s, c) stands for s - c; the s are summed exactly as
@@ -655,6 +657,7 @@ struct Fp64Smem {
 
 template <int NI, int G, int ILP, int JT>
 __global__ void __launch_bounds__(NI * G, 2) pair_stage_fp64(const StageParams P) {
+    pdl_wait();
     constexpr int NT = NI * G;
     static_assert(NI % 32 == 0 && JT % G == 0, "shape");
     extern __shared__ __align__(128) unsigned char smem_raw[];

@@ -335,6 +335,7 @@ __device__ __forceinline__ void moments_f32_merge(float *v, const float *o) {
 // staging arrays of z (permute_commit_init copies them back).
 static __global__ void __cluster_dims__(kSortClusterCtas, 1, 1) __launch_bounds__(kSortClusterThreads, 1)
     sort_cluster(const float4 *__restrict__ pa0, CloudDev c, SortScratch z) {
+    pdl_wait();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SortClusterSmem &S = *reinterpret_cast<SortClusterSmem *>(smem_raw);
     cg::cluster_group cl = cg::this_cluster();
@@ -569,6 +570,7 @@ static __global__ void permute_commit(CloudDev c, SortScratch z) {
 // permute_commit and init_positions in one launch: copy the gathered arrays
 // back, and write stage buffer 0 from the new positions.
 static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= c.n_pad) return;
     if (s < c.n) {
