@@ -570,7 +570,8 @@ int reorder(dm_cloud *c) {
         DM_CUDA(ctx, launch_pdl(sort_cluster, dim3(kSortClusterCtas), dim3(kSortClusterThreads), kSortClusterSmem,
                                 s, (const float4 *)c->d.pa[0], c->d, z));
         DM_CUDA(ctx, launch_pdl(permute_commit_init, dim3((c->n_pad + 255) / 256), dim3(256), 0, s, c->d, z));
-        c->boxes_valid[0] = c->boxes_valid[1] = false;
+        c->boxes_valid[0] = true;  // written by permute_commit_init
+        c->boxes_valid[1] = false;
         DM_CUDA(ctx, cudaGetLastError());
         ctx->launches += 2;
         c->order_dirty = false;
@@ -1300,8 +1301,8 @@ struct BatchVariant {
 template <int NW, int ILP, int TC, bool CULL>
 cudaError_t launch_batch(dim3 g, dim3 b, size_t smem, cudaStream_t s, const StageParams &P,
                          const BatchCloud *desc, const int2 *items, int nitems, unsigned int *ctr) {
-    batch_stage_fp32c<NW, ILP, TC, CULL><<<g, b, smem, s>>>(P, desc, items, nitems, ctr, exp_consts());
-    return cudaGetLastError();
+    return launch_pdl(batch_stage_fp32c<NW, ILP, TC, CULL>, g, b, smem, s, P, desc, items, nitems, ctr,
+                      exp_consts());
 }
 
 #define DM_BATCH_VARIANT(NW, ILP, TC, CULL, SUFFIX)                                                \
@@ -1382,9 +1383,8 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf =
     const int slot = (mode == kModeForceOnly) ? 0 : stage - 1;
     if (k.cull) {  // group boxes of the buffer this stage reads
         const int br = (mode == kModeForceOnly) ? fo_buf : (stage - 1) & 1;
-        batch_group_bounds<<<(B->ngroups * 32 + 255) / 256, 256, 0, ctx->stream>>>(B->d, B->ddesc, B->dgseg,
-                                                                                    B->ngroups, br);
-        DM_CUDA(ctx, cudaGetLastError());
+        DM_CUDA(ctx, launch_pdl(batch_group_bounds, dim3((B->ngroups * 32 + 255) / 256), dim3(256), 0, ctx->stream,
+                                B->d, (const BatchCloud *)B->ddesc, (const int *)B->dgseg, B->ngroups, br));
         ctx->launches++;
     }
     DM_CUDA(ctx, k.launch(dim3(B->grid[B->variant]), dim3(k.nt), k.smem, ctx->stream, P, B->ddesc,
@@ -1402,10 +1402,11 @@ int batch_reorder(dm_batch *B) {
     if (B->max_n <= kBatchSortMax) {  // one block per cloud sorts and gathers; two more commit
         DM_CUDA(ctx, cudaFuncSetAttribute(batch_sort_clouds, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)kBatchSortSmem));
-        batch_sort_clouds<<<B->nclouds, kBatchSortThreads, kBatchSortSmem, s>>>(B->d, B->ddesc, B->dbox, z);
-        permute_commit<<<grid, 256, 0, s>>>(B->d, z);
-        batch_init_positions<<<(B->total_pad + 255) / 256, 256, 0, s>>>(B->d, B->ddesc, B->dseg);
-        DM_CUDA(ctx, cudaGetLastError());
+        DM_CUDA(ctx, launch_pdl(batch_sort_clouds, dim3(B->nclouds), dim3(kBatchSortThreads), kBatchSortSmem, s,
+                                B->d, (const BatchCloud *)B->ddesc, B->dbox, z));
+        DM_CUDA(ctx, launch_pdl(permute_commit, dim3(grid), dim3(256), 0, s, B->d, z));
+        DM_CUDA(ctx, launch_pdl(batch_init_positions, dim3((B->total_pad + 255) / 256), dim3(256), 0, s, B->d,
+                                (const BatchCloud *)B->ddesc, (const int *)B->dseg));
         ctx->launches += 3;
         B->order_dirty = false;
         return DM_OK;

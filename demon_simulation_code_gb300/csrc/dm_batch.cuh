@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     __shared__ int s_item;
     float4 *s_red = reinterpret_cast<float4 *>(smem_raw) + Fp32cSmem<NW, ILP, TC>::red_offset;
     const int tid = threadIdx.x;
+    pdl_wait();
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
         __syncthreads();
@@ -90,6 +91,7 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
 // group; gseg[w] is group w's cloud; a cloud's last group may be partial).
 static __global__ void batch_group_bounds(CloudDev c, const BatchCloud *__restrict__ desc,
                                           const int *__restrict__ gseg, int ngroups, int b) {
+    pdl_wait();
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= ngroups) return;  // whole warp
@@ -179,6 +181,7 @@ constexpr size_t kBatchSortSmem = sizeof(BatchSortSmem);
 // max x, max y (as batch_boxes writes them; the batch autotuner reads it).
 static __global__ void __launch_bounds__(kBatchSortThreads, 1)
     batch_sort_clouds(CloudDev c, const BatchCloud *__restrict__ desc, double *box_out, SortScratch z) {
+    pdl_wait();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     BatchSortSmem &S = *reinterpret_cast<BatchSortSmem *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -370,6 +373,7 @@ static __global__ void batch_tune_compress(CloudDev c, const BatchCloud *__restr
 // filter bound.
 static __global__ void batch_init_positions(CloudDev c, const BatchCloud *__restrict__ desc,
                                             const int *__restrict__ seg) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < c.n) {
         CloudDev v = c;

@@ -556,6 +556,7 @@ static __global__ void permute_gather(CloudDev c, const int *__restrict__ perm, 
 // ... and copy back (the cloud's array addresses never change, so captured
 // CUDA graphs stay valid)
 static __global__ void permute_commit(CloudDev c, SortScratch z) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= c.n) return;
     c.x[s] = z.stage[0][s];
@@ -568,11 +569,13 @@ static __global__ void permute_commit(CloudDev c, SortScratch z) {
 }
 
 // permute_commit and init_positions in one launch: copy the gathered arrays
-// back, and write stage buffer 0 from the new positions.
+// back, write stage buffer 0 from the new positions and the boxes of its
+// 32-particle groups (each warp is one group; as group_bounds computes them).
 static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= c.n_pad) return;
+    if (s >= c.n_pad) return;  // whole warps: n_pad is a multiple of 64
+    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
     if (s < c.n) {
         const double x = z.stage[0][s], y = z.stage[1][s];
         c.x[s] = x;
@@ -583,6 +586,9 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
         c.m[s] = z.stage[5][s];
         c.orig[s] = z.orig_stage[s];
         write_stage_position(c, 0, s, x, y);
+        const float4 A = c.pa[0][s];
+        x0 = x1 = A.x;
+        y0 = y1 = A.y;
     } else {
         for (int b = 0; b < 2; b++) {
             c.px[b][s] = (double)kPadPosition;
@@ -593,6 +599,14 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
         c.q[s] = 0.0;
         c.m[s] = 1.0;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if ((threadIdx.x & 31) == 0) c.gbox[0][s >> 5] = make_float4(x0, y0, x1, y1);
 }
 
 static __global__ void set_identity(int *orig, int n) {
