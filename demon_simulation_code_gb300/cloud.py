@@ -126,8 +126,17 @@ class DeviceCloud:
         a = [np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, vx, vy)]
         self._chk(self.lib.dm_cloud_upload(self.h, *(ptr(v) for v in a)))
 
-    def download(self):
-        out = [np.empty(self.n) for _ in range(4)]
+    def download(self, out=None):
+        """x, y, vx, vy in the caller's order; `out`: four contiguous float64
+        arrays of length n to fill (e.g. pinned host buffers) instead of new
+        ones."""
+        if out is None:
+            out = [np.empty(self.n) for _ in range(4)]
+        else:
+            out = list(out)
+            if len(out) != 4 or any(not (isinstance(v, np.ndarray) and v.dtype == np.float64 and
+                                         v.flags.c_contiguous and v.size == self.n) for v in out):
+                raise ValueError("download(out=...): four contiguous float64 arrays of length n")
         self._chk(self.lib.dm_cloud_download(self.h, *(ptr(v) for v in out)))
         return tuple(out)
 

@@ -52,6 +52,7 @@ struct dm_ctx {
     size_t prof_used = 0;
     double prof_pairs = 0.0;
     long long prof_launches = 0;
+    int *h_err = nullptr;  // pinned word for the device error flags (read with each download)
 
     int fail(int code, const char *fmt, ...) {
         char buf[512];
@@ -124,10 +125,8 @@ namespace {
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-int check_device_errors(dm_ctx *ctx, dm_cloud *c) {
-    int h = 0;
-    DM_CUDA(ctx, cudaMemcpyAsync(&h, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+// Status for device error flags h already read back (and clears them).
+int device_error_status(dm_ctx *ctx, dm_cloud *c, int h) {
     if (h) {
         DM_CUDA(ctx, cudaMemsetAsync(c->d.err, 0, sizeof(int), ctx->stream));
         if (h & 2) return ctx->fail(DM_ERR_NUMERIC, "zero particle separation in the adaptive time step test");
@@ -136,6 +135,13 @@ int check_device_errors(dm_ctx *ctx, dm_cloud *c) {
         return ctx->fail(DM_ERR_NUMERIC, "non-finite particle position after a stage (error bits 0x%x)", h);
     }
     return DM_OK;
+}
+
+int check_device_errors(dm_ctx *ctx, dm_cloud *c) {
+    int h = 0;
+    DM_CUDA(ctx, cudaMemcpyAsync(&h, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return device_error_status(ctx, c, h);
 }
 
 ExpConsts make_exp_consts() {
@@ -543,19 +549,6 @@ int tune_precision(dm_cloud *c, int precision) {
     return DM_OK;
 }
 
-// Charges and masses back to the caller's order (before orig is reset).
-int gather_to_caller_order(dm_cloud *c) {
-    dm_ctx *ctx = c->ctx;
-    double **st = c->sort.stage;
-    const size_t bytes = (size_t)c->n * sizeof(double);
-    scatter_to_caller<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(
-        c->d.orig, c->n, c->d.q, c->d.m, nullptr, nullptr, st[4], st[5], nullptr, nullptr);
-    DM_CUDA(ctx, cudaGetLastError());
-    DM_CUDA(ctx, cudaMemcpyAsync(c->d.q, st[4], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    DM_CUDA(ctx, cudaMemcpyAsync(c->d.m, st[5], bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    return DM_OK;
-}
-
 // Puts the cloud in Morton order (dm_sort.cuh); graph-capturable.
 int reorder(dm_cloud *c) {
     dm_ctx *ctx = c->ctx;
@@ -720,6 +713,7 @@ int dm_ctx_destroy(dm_ctx *ctx) {
         cudaEventDestroy(p.second);
     }
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->h_err) cudaFreeHost(ctx->h_err);
     delete ctx;
     return DM_OK;
 }
@@ -929,19 +923,19 @@ int dm_cloud_upload(dm_cloud *c, const double *x, const double *y, const double 
     if (!x || !y || !vx || !vy) return ctx->fail(DM_ERR_ARG, "dm_cloud_upload: NULL array");
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t bytes = (size_t)c->n * sizeof(double);
-    DM_CUDA(ctx, cudaMemcpyAsync(c->d.x, x, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    DM_CUDA(ctx, cudaMemcpyAsync(c->d.y, y, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    DM_CUDA(ctx, cudaMemcpyAsync(c->d.vx, vx, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    DM_CUDA(ctx, cudaMemcpyAsync(c->d.vy, vy, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    // charges and masses stay; bring them back to the caller's order too
-    int rc = gather_to_caller_order(c);
-    if (rc) return rc;
-    set_identity<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->d.orig, c->n);
-    init_positions<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d);
-    c->boxes_valid[0] = c->boxes_valid[1] = false;
+    // caller order -> staging -> the cloud's current internal order (charges,
+    // masses and the order stay; stage buffer 0 and its boxes are rewritten)
+    double **st = c->sort.stage;
+    DM_CUDA(ctx, cudaMemcpyAsync(st[0], x, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(st[1], y, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(st[2], vx, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    DM_CUDA(ctx, cudaMemcpyAsync(st[3], vy, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    upload_internal_order<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d, c->sort);
+    c->boxes_valid[0] = true;
+    c->boxes_valid[1] = false;
     DM_CUDA(ctx, cudaGetLastError());
-    ctx->launches += 3;
-    c->order_dirty = true;
+    ctx->launches += 1;
+    c->order_dirty = true;  // the uploaded positions may be far from the old order
     return DM_OK;
 }
 
@@ -959,8 +953,11 @@ int dm_cloud_download(dm_cloud *c, double *x, double *y, double *vx, double *vy)
     if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, st[1], bytes, cudaMemcpyDeviceToHost, ctx->stream));
     if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, st[2], bytes, cudaMemcpyDeviceToHost, ctx->stream));
     if (vy) DM_CUDA(ctx, cudaMemcpyAsync(vy, st[3], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    // the error flags come back with the state: one synchronisation
+    if (!ctx->h_err) DM_CUDA(ctx, cudaMallocHost((void **)&ctx->h_err, sizeof(int)));
+    DM_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return check_device_errors(ctx, c);
+    return device_error_status(ctx, c, *ctx->h_err);
 }
 
 int dm_cloud_set_charge_mass(dm_cloud *c, const double *q, const double *m) {

@@ -609,6 +609,36 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
     if ((threadIdx.x & 31) == 0) c.gbox[0][s >> 5] = make_float4(x0, y0, x1, y1);
 }
 
+// An upload in the caller's order (staging arrays 0..3: x, y, vx, vy) put
+// straight into the cloud's current internal order, with stage buffer 0 and
+// the boxes of its 32-particle groups: charges, masses and the order itself
+// stay where they are (the next re-sort starts from them).
+static __global__ void upload_internal_order(CloudDev c, SortScratch z) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= c.n_pad) return;  // whole warps: n_pad is a multiple of 64
+    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+    if (s < c.n) {
+        const int o = c.orig[s];
+        const double x = z.stage[0][o], y = z.stage[1][o];
+        c.x[s] = x;
+        c.y[s] = y;
+        c.vx[s] = z.stage[2][o];
+        c.vy[s] = z.stage[3][o];
+        write_stage_position(c, 0, s, x, y);
+        const float4 A = c.pa[0][s];
+        x0 = x1 = A.x;
+        y0 = y1 = A.y;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, off));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, off));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, off));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, off));
+    }
+    if ((threadIdx.x & 31) == 0) c.gbox[0][s >> 5] = make_float4(x0, y0, x1, y1);
+}
+
 static __global__ void set_identity(int *orig, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < n) orig[s] = s;

@@ -182,7 +182,9 @@ int dm_cloud_upload(dm_cloud *cloud, const double *x, const double *y,
                     const double *vx, const double *vy);
 
 /* Device -> host state.  The reference's driver reads Cloud::x.. before
- * Cloud::writeTimeStep (driver.cpp:448-449, Cloud.cpp:258-271). */
+ * Cloud::writeTimeStep (driver.cpp:448-449, Cloud.cpp:258-271).  One stream
+ * synchronisation: the device error flags come back with the state.  Host
+ * buffers in page-locked memory (cudaMallocHost) are copied by DMA. */
 int dm_cloud_download(dm_cloud *cloud, double *x, double *y, double *vx,
                       double *vy);
 
