@@ -253,10 +253,14 @@ __device__ __forceinline__ void split2(double x, float &hi, float &lo) {
 // margin, evaluated in FP32 on the hi parts.  The margin 2^-17 (|p_i| + rc)^2
 // is ~10x the worst FP32 rounding of that expanded form plus the hi/lo split
 // error for any pair within rc of i, so no pair the reference keeps is
-// filtered out.  Rounded up.
+// filtered out.  Rounded up.  |p_i| + rc is formed from FP32 square roots
+// with every operation rounded up (an upper bound, so the margin only grows):
+// two FP64 square roots per particle per stage cost more than the rest of
+// this function at GB300's FP64 rate.
 __device__ __forceinline__ float filter_threshold(float xh, float yh, double rc2) {
     const double a2 = (double)xh * xh + (double)yh * yh;
-    const double pr = sqrt(a2) + sqrt(rc2);
+    const float pf = __fadd_ru(__fsqrt_ru(__double2float_ru(a2)), __fsqrt_ru(__double2float_ru(rc2)));
+    const double pr = (double)pf;
     return __double2float_ru(rc2 - a2 + 7.62939453125e-6 * pr * pr);
 }
 
