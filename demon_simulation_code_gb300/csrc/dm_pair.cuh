@@ -342,6 +342,41 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         for (int k = 0; k < ILP; k++) hits[k] = 0u;
     };
 
+    // Chunk c of the staged tile against the i slots in `full` (bit k: slot
+    // k), every lane evaluating the same 4 j; pair terms summed plainly and
+    // added to the slot's compensated sums.  The slot is a runtime value, so
+    // the precise path appears once here, as in flush_hits.
+    auto direct_chunk = [&](int c, uint32_t full) {
+#pragma unroll 1
+        for (int k = 0; k < ILP; k++) {
+            if (!((full >> k) & 1u)) continue;
+            float xh = -0.5f * mx2[0].x, yh = -0.5f * my2[0].x;
+#pragma unroll
+            for (int t = 1; t < ILP; t++) {
+                xh = (k == t) ? -0.5f * mx2[t].x : xh;
+                yh = (k == t) ? -0.5f * my2[t].x : yh;
+            }
+            const float4 c4 = s_cold[k * 32 + lane];
+            PairCtx ic;
+            ic.xl = c4.x;
+            ic.yl = c4.y;
+            ic.qc = c4.z;
+            ic.ii = __float_as_int(c4.w);
+            float px = 0.0f, py = 0.0f;
+#pragma unroll 1
+            for (int u = 0; u < 4; u++) {
+                const int jj = 4 * c + u;
+                const float4 Bj = s_pb[jj];
+                precise_pair(P, b, xh, yh, ic, make_float4(s_xf[jj], s_yf[jj], 0.0f, Bj.z), Bj,
+                             __float_as_int(Bj.w), px, py);
+            }
+            float4 acc = my_acc[k * 32 + lane];
+            kahan_add(acc.x, acc.z, px);
+            kahan_add(acc.y, acc.w, py);
+            my_acc[k * 32 + lane] = acc;
+        }
+    };
+
     // Sweeps the `count` chunks (4 consecutive j) of this CTA's list through
     // shared-memory tiles; chunk_of(q) is the cloud chunk index of entry q.
     // Within a tile, chunk c goes to warp c % NW.
@@ -430,14 +465,25 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
                            __float_as_uint(d23[k].y);
                 }
                 if (__any_sync(0xffffffffu, (int)sgn < 0)) {
-                    // record this lane's hits: the sign bits of the 4 j
+                    // slots where every lane passed all 4 j: evaluate the chunk
+                    // now, all lanes on the same j (no hit bits, no per-lane
+                    // j lookup); the other slots record this lane's hits, the
+                    // sign bits of the 4 j
+                    uint32_t full = 0u;
+#pragma unroll
+                    for (int k = 0; k < ILP; k++) {
+                        const uint32_t all4 = __float_as_uint(d01[k].x) & __float_as_uint(d01[k].y) &
+                                              __float_as_uint(d23[k].x) & __float_as_uint(d23[k].y);
+                        full |= (__all_sync(0xffffffffu, (int)all4 < 0) ? 1u : 0u) << k;
+                    }
+                    if (full) direct_chunk(c, full);
 #pragma unroll
                     for (int k = 0; k < ILP; k++) {
                         const uint32_t bits = (__float_as_uint(d01[k].x) >> 31) |
                                               ((__float_as_uint(d01[k].y) >> 30) & 2u) |
                                               ((__float_as_uint(d23[k].x) >> 29) & 4u) |
                                               ((__float_as_uint(d23[k].y) >> 28) & 8u);
-                        hits[k] |= bits << (4 * nb);
+                        hits[k] |= ((full >> k) & 1u) ? 0u : bits << (4 * nb);
                     }
                     any_hit = true;
                 }
