@@ -586,8 +586,17 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
 // through distributed shared memory and run the stage epilogue in the same
 // launch.  CL = false: plain blocks; each writes its partial sums to global
 // memory and stage_finish (below) completes the stage.
+// Occupancy: with two i slots per lane the kernel fits 64 registers without
+// spills, so 32 warps per SM are resident (more latency hidden in the sparse
+// phases, where a block is short and bound by dependent loads and barriers);
+// four slots need more registers and stay at 24 warps.
+template <int NW, int ILP>
+constexpr int fp32c_min_blocks() {
+    return (ILP <= 2 ? 32 : 24) / NW > 0 ? (ILP <= 2 ? 32 : 24) / NW : 1;
+}
+
 template <int NW, int ILP, int TC, bool CL, bool CULL = false>
-__global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
+__global__ void __launch_bounds__(NW * 32, fp32c_min_blocks<NW, ILP>())
     pair_stage_fp32c(const StageParams P, const ExpConsts E) {
     pdl_wait();
     constexpr int TILE = 32 * ILP;
