@@ -97,7 +97,7 @@ struct dm_cloud {
     int partial_cap = 0;
     SortScratch sort{};
     int sort_blocks = 0;
-    int reorder_interval = 4;   // steps between Morton re-sorts (0 = never); 1 for n <= kSmallSortMax
+    int reorder_interval = 1;   // steps between Morton re-sorts (0 = never)
     bool order_dirty = true;    // re-sort before the next step
     unsigned long long host_steps = 0;  // RK4 steps enqueued so far
     long long graph_launches = 0;       // kernels in one replay of the step graph
@@ -820,10 +820,11 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->ctx = ctx;
     c->n = n;
     c->n_pad = (n + 63) & ~63;
-    // the one-block sort costs less than the pair sweeps it saves every step
-    // (a confined cloud's particles cross many cutoffs per step while it
-    // collapses, and a stale order inflates every group box)
-    c->reorder_interval = (n <= kSmallSortMax) ? 1 : 4;
+    // a re-sort costs less than the pair sweeps it saves every step (a confined
+    // cloud's particles cross many cutoffs per step while it collapses, close
+    // pairs of a random cloud are thrown out, and a stale order inflates
+    // every group box)
+    c->reorder_interval = 1;
     c->coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);
     c->d.coulomb = c->coulomb;
     c->d.rc2 = (10.0 / 2e4) * (10.0 / 2e4);  // default kappa until set_forces

@@ -259,9 +259,9 @@ int dm_cloud_set_kernel(dm_cloud *cloud, const char *variant, int split);
  * wakes the precise arithmetic for few j; the order is internal (every
  * array crossing this ABI is in the caller's order).  The cloud is re-sorted
  * every `steps` RK4 steps (0 = only after an upload; otherwise a power of
- * two <= 16).  Default: every step for clouds of up to 16384 particles
- * (sorted by one thread block in one launch), every 4 steps above that.
- * No reference counterpart. */
+ * two <= 16).  Default: every step (clouds of up to 16384 particles are
+ * sorted by one thread-block cluster in one launch).  No reference
+ * counterpart. */
 int dm_cloud_set_reorder_interval(dm_cloud *cloud, int steps);
 
 /* Ordered pairs the culling kernel variants actually swept so far (32-
