@@ -40,7 +40,8 @@ FLOPS_PER_PAIR = 23  # algorithmic FP32 flops per ordered pair
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=10000,
+                    help="timed RK4 steps (default: the configuration's full 10000-step run)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="disk16k", choices=sorted(W.WORKLOADS))
@@ -111,10 +112,16 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the sampler is running (nvidia-smi
+            # takes a fraction of a second to print its first line)
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.skip = len(self.lines)  # samples taken before the timed region
         except OSError:
             self.proc = None
         return self
@@ -134,7 +141,7 @@ class ClockSampler:
 
     def summary(self):
         sm, smax, reasons = [], [], set()
-        for ln in self.lines:
+        for ln in self.lines[getattr(self, "skip", 0):]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) != len(self.FIELDS):
                 continue
