@@ -107,6 +107,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.skip = 0
 
     def __enter__(self):
         try:
@@ -132,6 +133,13 @@ class ClockSampler:
 
     def __exit__(self, *exc):
         if self.proc:
+            self.n_inside = len(self.lines) - self.skip  # samples taken during the timed region
+            if self.n_inside == 0:
+                # a region shorter than the sampling interval holds no sample:
+                # wait for the first one after it, so the region is bracketed
+                t0 = time.time()
+                while len(self.lines) <= self.skip and time.time() - t0 < 1.0 and self.proc.poll() is None:
+                    time.sleep(0.01)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -141,7 +149,15 @@ class ClockSampler:
 
     def summary(self):
         sm, smax, reasons = [], [], set()
-        for ln in self.lines[getattr(self, "skip", 0):]:
+        skip = getattr(self, "skip", 0)
+        n_inside = getattr(self, "n_inside", len(self.lines) - skip)
+        lines = self.lines[skip:skip + n_inside]
+        bracket = False
+        if n_inside == 0 and skip > 0:
+            # no sample inside the region: the last one before it and the first after
+            lines = self.lines[skip - 1:skip + 1]
+            bracket = True
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) != len(self.FIELDS):
                 continue
@@ -155,8 +171,11 @@ class ClockSampler:
                     reasons.add(name)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
-                "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+               "reasons": sorted(reasons), "samples": len(sm)}
+        if bracket:
+            out["bracketing"] = "timed region shorter than the 50 ms sampling interval"
+        return out
 
 
 def cpu_threads():
