@@ -32,6 +32,7 @@ struct AdjCloud {
     double rc2;
     float rc2_lo, rc2_hi;  // FP32 certain-in / certain-out bounds on r^2
     float kappa_f, kappa2_f;
+    float kl2e_hi, kl2e_lo;  // kappa*log2(e) as a float pair (SFU exponential)
 };
 
 constexpr int kAdjThreads = 128;
@@ -95,45 +96,60 @@ __device__ __forceinline__ void adj_tile_fp64(const AdjCloud &d, const AdjJ *sj,
 
 // FP32-compensated pair loop over one shared-memory j tile: positions as
 // float pairs (hi, lo) so the differences keep ~2^-24 relative accuracy,
-// pair terms in FP32, Kahan sums; pairs within 4e-6 of the cutoff in r^2 are
-// decided by the reference's FP64 test on the FP64 positions.
+// pair terms in FP32, summed plainly over groups of four j and each group
+// added to Kahan sums; pairs within 4e-6 of the cutoff in r^2 are decided by
+// the reference's FP64 test on the FP64 positions.  e^{-kappa r} on the SFU
+// with the rounding residue of kappa r restored (exp_neg_kr), 1/(1 + kappa r)
+// from the fast reciprocal: a few ulp per pair term, far below the rounding
+// of the FP32 pair sums themselves.
 template <int MODE>
 __device__ __forceinline__ void adj_tile_fp32c(const AdjCloud &d, const ExpConsts &E, const float4 *sp,
                                                const float4 *sa, int cnt, int jbase, int li, float xh, float yh,
                                                float xl, float yl, float qci, float axi, float ayi,
                                                const double *__restrict__ x, const double *__restrict__ y,
                                                double xi, double yi, float (&s)[4], float (&c)[4]) {
-    for (int e = 0; e < cnt; e++) {
-        const float4 P = sp[e];
-        const float dx = (xh - P.x) + (xl - P.z);
-        const float dy = (yh - P.y) + (yl - P.w);
-        const float r2 = fmaf(dx, dx, dy * dy);
-        if (!(r2 < d.rc2_hi)) continue;
-        if (jbase + e == li) continue;
-        if (!(r2 < d.rc2_lo)) {
-            const int j = d.off + jbase + e;
-            double r, a;
-            if (!ref_in_cutoff(__dsub_rn(xi, x[j]), __dsub_rn(yi, y[j]), d.kappa, r, a)) continue;
+    constexpr int NS = MODE == 0 ? 2 : 4;
+    for (int e0 = 0; e0 < cnt; e0 += 4) {
+        float t[NS];
+#pragma unroll
+        for (int k = 0; k < NS; k++) t[k] = 0.0f;
+        const int e1 = min(cnt, e0 + 4);
+        for (int e = e0; e < e1; e++) {
+            const float4 P = sp[e];
+            const float dx = (xh - P.x) + (xl - P.z);
+            const float dy = (yh - P.y) + (yl - P.w);
+            const float r2 = fmaf(dx, dx, dy * dy);
+            if (!(r2 < d.rc2_hi)) continue;
+            if (jbase + e == li) continue;
+            if (!(r2 < d.rc2_lo)) {
+                const int j = d.off + jbase + e;
+                double r, a;
+                if (!ref_in_cutoff(__dsub_rn(xi, x[j]), __dsub_rn(yi, y[j]), d.kappa, r, a)) continue;
+            }
+            float w = rsqrtf(r2);  // 1/r, one Newton step
+            w = fmaf(0.5f * fmaf(-(r2 * w), w, 1.0f), w, w);
+            const float r = r2 * w;
+            const float kr = d.kappa_f * r;
+            const float ex = exp_neg_kr(r, d.kl2e_hi, d.kl2e_lo);
+            const float4 A = sa[e];  // (q_j, a_j.x, a_j.y, -)
+            const float qq = qci * A.x;
+            const float g = (qq * (1.0f + kr)) * ex * ((w * w) * w);
+            if constexpr (MODE == 0) {
+                t[0] = fmaf(g, dx, t[0]);
+                t[1] = fmaf(g, dy, t[1]);
+            } else {
+                const float h = -g * fmaf(d.kappa2_f, __fdividef(1.0f, 1.0f + kr), 3.0f * (w * w));
+                const float bx = axi - A.y, by = ayi - A.z;
+                const float dd = fmaf(dx, bx, dy * by);
+                const float hd = h * dd;
+                t[0] += fmaf(hd, dx, g * bx);
+                t[1] += fmaf(hd, dy, g * by);
+                t[2] = fmaf(g, dd, t[2]);
+                t[NS - 1] = fmaf(-(qq * d.kappa_f) * ex * w, fmaf(axi, dx, ayi * dy), t[NS - 1]);
+            }
         }
-        float w = rsqrtf(r2);  // 1/r, one Newton step
-        w = fmaf(0.5f * fmaf(-(r2 * w), w, 1.0f), w, w);
-        const float kr = d.kappa_f * (r2 * w);
-        const float ex = exp_neg(kr, E);
-        const float4 A = sa[e];  // (q_j, a_j.x, a_j.y, -)
-        const float qq = qci * A.x;
-        const float g = (qq * (1.0f + kr)) * ex * ((w * w) * w);
-        if (MODE == 0) {
-            kahan_add(s[0], c[0], g * dx);
-            kahan_add(s[1], c[1], g * dy);
-        } else {
-            const float h = -g * fmaf(d.kappa2_f, __frcp_rn(1.0f + kr), 3.0f * (w * w));
-            const float bx = axi - A.y, by = ayi - A.z;
-            const float hd = h * fmaf(dx, bx, dy * by);
-            kahan_add(s[0], c[0], fmaf(hd, dx, g * bx));
-            kahan_add(s[1], c[1], fmaf(hd, dy, g * by));
-            kahan_add(s[2], c[2], g * fmaf(dx, bx, dy * by));
-            kahan_add(s[3], c[3], (-(qq * d.kappa_f) * ex * w) * fmaf(axi, dx, ayi * dy));
-        }
+#pragma unroll
+        for (int k = 0; k < NS; k++) kahan_add(s[k], c[k], t[k]);
     }
 }
 

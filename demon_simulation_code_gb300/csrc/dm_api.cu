@@ -1878,6 +1878,7 @@ void adj_fill(dm_adjoint *A, const dm_force_params *params) {
         d.rc2_hi = (float)(d.rc2 * (1.0 + 4e-6));
         d.kappa_f = (float)d.kappa;
         d.kappa2_f = (float)(d.kappa * d.kappa);
+        kappa_log2e(d.kappa, d.kl2e_hi, d.kl2e_lo);
     }
 }
 
