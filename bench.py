@@ -34,7 +34,10 @@ from demon_simulation_code_gb300 import workloads as W  # noqa: E402
 
 METRIC = "pair-interactions/s/GPU: FP32-compensated vs FP64 at <=1e-6 rel force err"
 UNIT = "pair-interactions/s"
-FLOPS_PER_PAIR = 23  # algorithmic FP32 flops per ordered pair
+# algorithmic FP32 flops per ordered pair: dx, dy 2; r^2 3; rsqrt 1; r 1;
+# kappa r 1; exp 2; 1 + kappa r 1; r^-3 2; q_j (1 + kappa r) e 2; x C q_i 1;
+# fx, fy 4; cutoff compare/select 2 (2 of them on the SFU: rsqrt, ex2)
+FLOPS_PER_PAIR = 23
 
 
 def parse():

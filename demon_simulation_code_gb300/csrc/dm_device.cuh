@@ -267,12 +267,12 @@ __device__ __forceinline__ float filter_threshold(float xh, float yh, double rc2
 // Programmatic dependent launch: a kernel launched with the programmatic-
 // serialization attribute may be scheduled while its predecessor in the
 // stream is still running.  pdl_wait() blocks until the predecessor grid has
-// completed and its writes are visible, so every kernel calls it before its
-// first global memory access; pdl_trigger() lets the next kernel be
-// scheduled now (it still waits for this grid to complete).  Both are no-ops
-// for a kernel launched without the attribute.
+// completed and its writes are visible, so every such kernel calls it before
+// its first global memory access (a no-op for a kernel launched without the
+// attribute).  No kernel here triggers its dependents early: the next
+// kernel's blocks would then occupy SMs that a multi-wave pair launch still
+// needs.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, int i,
                                                      double xs, double ys) {
