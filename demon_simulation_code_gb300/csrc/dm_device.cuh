@@ -274,6 +274,10 @@ __device__ __forceinline__ float filter_threshold(float xh, float yh, double rc2
 // needs.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Starts bringing a global-memory line into L1 (no data returned, no fault on
+// the address being read later by this thread).
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, int i,
                                                      double xs, double ys) {
     c.px[b][i] = xs;

@@ -643,6 +643,34 @@ static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P.c.n) {
+        // One warp per 32 particles is little parallelism for the chain of
+        // dependent loads below (the split partials, then the epilogue's
+        // state): the epilogue's operands are prefetched into L1 first, so
+        // their round trip overlaps the partials'.
+        {
+            const CloudDev &c = P.c;
+            const int b = (P.mode == kModeForceOnly) ? P.fo_buf : (P.stage - 1) & 1;
+            const bool first = P.mode == kModeForceOnly || P.stage == 1;
+            prefetch_l1(c.px[b] + i);
+            prefetch_l1(c.py[b] + i);
+            prefetch_l1((first ? c.vx : c.vxc) + i);
+            prefetch_l1((first ? c.vy : c.vyc) + i);
+            prefetch_l1(c.q + i);
+            prefetch_l1(c.m + i);
+            prefetch_l1(c.orig + i);
+            if (P.mode != kModeForceOnly) {
+                prefetch_l1(c.x + i);
+                prefetch_l1(c.y + i);
+                if (!first) {
+                    prefetch_l1(c.vx + i);
+                    prefetch_l1(c.vy + i);
+                }
+                if (P.stage >= 3)
+                    for (int k = 0; k < 4; k++) prefetch_l1(c.a23[k] + i);
+                if (P.stage == 4)
+                    for (int k = 0; k < 4; k++) prefetch_l1(c.a1[k] + i);
+            }
+        }
         // each partial (s, c) stands for s - c; the s are summed exactly as
         // an unevaluated float pair (TwoSum), the small c plainly, in rank
         // order, and FP64 is used once: FP64 runs at ~1/64 of the FP32 rate
@@ -652,6 +680,18 @@ static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
         const float4 *p = P.partial + i;
         const size_t stride = (size_t)P.c.n_pad;
         int r = 0;
+        for (; r + 16 <= P.split; r += 16) {  // 16 loads in flight, summed in rank order
+            float4 v[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) v[u] = p[(size_t)(r + u) * stride];
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                sx.add(v[u].x);
+                sy.add(v[u].y);
+                cx += v[u].z;
+                cy += v[u].w;
+            }
+        }
         for (; r + 8 <= P.split; r += 8) {  // 8 loads in flight, summed in rank order
             float4 v[8];
 #pragma unroll
