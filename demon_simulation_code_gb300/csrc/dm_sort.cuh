@@ -278,10 +278,11 @@ static __global__ void __launch_bounds__(kSortThreads) radix_scatter(
 // position.  The multi-kernel path above needs fifteen dependent launches
 // (~0.1 ms at n = 16384); a single block was no better (one SM's issue rate).
 //
-// Element order: block r, warp w, round k, lane l is element r*P +
-// w*32*kSortClusterRounds + k*32 + l.  Digits are ranked in that order (lanes with equal digits found
-// by match_digit8) and bases are laid out digit-major over (digit, block,
-// warp), so the sort is stable and depends only on the positions.  The key
+// Element order: block r, warp w, round k, lane l is element
+// r*P + w*32*kSortClusterRounds + k*32 + l.  Digits are ranked in that order
+// (lanes with equal digits found by match_digit8) and bases are laid out
+// digit-major over (digit, block, warp), so the sort is stable and depends
+// only on the positions.  The key
 // box and keys are FP32 functions of the positions' hi parts: GB300's FP64
 // rate (~2 FMA per clock per SM) would dominate a pass over 16384 doubles,
 // and any order is correct (the permutation moves every array together).
