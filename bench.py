@@ -8,6 +8,17 @@ workload's cloud.  Metric: pair-interactions/s = 4 * N(N-1) * steps / time
     python bench.py [--steps K] [--warmup W] [--workload disk16k]
                     [--precision fp32c] [--impl gb300|reference]
 
+The window: W warm-up steps from the seeded state, then every figure starts
+from the state reached (s0) and covers the same steps: `value` (K steps of
+the tuned kernel), the FP64 kernel and the fastest unculled FP32C kernel
+(the first K64 <= K of those steps, K64 bounded by --fp64-budget), `e2e`
+(the K steps again through the C ABI with host buffers), the force error at
+the window's last and densest states, the FP32C-vs-FP64 trajectory
+divergence at the window's output steps, and the CPU legs (the oracle
+stepping from states of the window, all cores and one core).  The
+`--impl reference` arm times the oracle over steps W .. W+K-1 of its own
+FP64 trajectory.
+
 Multi-GPU (torchrun, one rank per GPU): every rank integrates its own
 replica of the workload (independent clouds, no collective on the data path,
 weak scaling); the time is the max over ranks.
@@ -49,9 +60,18 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="disk16k", choices=sorted(W.WORKLOADS))
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
-    ap.add_argument("--fp64-steps", type=int, default=10)
-    ap.add_argument("--e2e-steps", type=int, default=100)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=0,
+                    help="most FP64 steps of the window to time (0 = all K, within --fp64-budget)")
+    ap.add_argument("--fp64-budget", type=float, default=40.0,
+                    help="seconds of FP64 steps; the FP64 figures cover the first K64 steps of the window")
+    ap.add_argument("--no-unculled", dest="unculled", action="store_false",
+                    help="skip the unculled FP32C kernel on the FP64 steps")
+    ap.add_argument("--cpu-states", type=int, default=5,
+                    help="states of the window (evenly spaced) the CPU legs step from")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds for the all-cores CPU leg")
+    ap.add_argument("--cpu-budget-1core", type=float, default=30.0, help="seconds for the 1-core CPU leg")
+    ap.add_argument("--ref-max-steps", type=int, default=40,
+                    help="--impl reference: most steps of the window timed on the CPU")
     ap.add_argument("--batch-steps", type=int, default=32)
     ap.add_argument("--adjoint-grads", type=int, default=2,
                     help="timed loss+gradient evaluations of the 64-cloud trajectory fit (0 = skip)")
@@ -188,20 +208,45 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_rk4_rate(w, nsteps, nthreads):
-    """The oracle (restatement of the reference's algorithm, OpenMP, per-block
-    locks like the reference) on `nsteps` RK4 steps of the first cloud."""
+def _oracle():
     import oracle
 
     oracle.build()
-    o = oracle.Oracle()
+    return oracle, oracle.Oracle()
+
+
+def oracle_pair_params(oracle, c):
+    """The shielded-Coulomb force alone (for force-error figures)."""
+    return oracle.make_params(**{**c.params(), "flags": W.SHIELDED_COULOMB})
+
+
+def cpu_sample_rate(w, states, nthreads, budget_s):
+    """The oracle (restatement of the reference's algorithm, OpenMP with
+    per-block locks like ShieldedCoulombForce.cpp) on sampled states of the
+    timed window: one RK4 step from each state (one force evaluation where an
+    RK4 step is above 5e9 pair interactions), in order until `budget_s` is
+    spent (at least one).  Rate = pair interactions / summed time."""
+    oracle, o = _oracle()
     c = w.clouds[0]
     p = oracle.make_params(**c.params())
-    t0 = time.perf_counter()
-    o.rk4_fixed(c.x, c.y, c.vx, c.vy, c.q, c.m, p, w.dt, nsteps, 0, nthreads)
-    el = time.perf_counter() - t0
-    pairs = 4.0 * c.n * (c.n - 1) * nsteps
-    return pairs / el, el
+    n = c.n
+    per_step = 4.0 * n * (n - 1)
+    by_eval = per_step > 5e9
+    done, total = [], 0.0
+    for k, st, ctr, t in states:
+        x, y, vx, vy = st
+        t0 = time.perf_counter()
+        if by_eval:
+            o.forces(x, y, vx, vy, c.q, c.m, p, ctr, 1, nthreads, t)
+        else:
+            o.rk4_fixed(x, y, vx, vy, c.q, c.m, p, w.dt, 1, ctr, nthreads, t)
+        total += time.perf_counter() - t0
+        done.append(int(k))
+        if total >= budget_s:
+            break
+    pairs = (n * (n - 1) if by_eval else per_step) * len(done)
+    unit = "force evaluation" if by_eval else "RK4 step"
+    return pairs / total, total, done, unit
 
 
 def traffic_from_profiles(kernel: str, workload: str):
@@ -218,31 +263,55 @@ def traffic_from_profiles(kernel: str, workload: str):
     return None
 
 
+def ref_window(args):
+    """Steps [first, first + steps) of the reference arm: the GPU arm's
+    warm-up and step count, the count capped so that the CPU run stays within
+    a few minutes."""
+    return max(args.warmup, 3), max(1, min(args.steps, args.ref_max_steps))
+
+
 def run_reference(args, world, rank):
     """The reference's CPU algorithm (oracle port: the reference sources need
-    x86 SSE4.2 and do not build on the Arm host) on this host's cores."""
+    x86 SSE4.2 and do not build on the Arm host) on this host's cores, over
+    the same window of steps as the GPU arm."""
     if rank != 0:
         return 0
     w = workload(args.workload)
+    c = w.clouds[0]
     threads = cpu_threads()
-    nst = max(1, min(args.steps, 10))
-    if args.warmup > 0:
-        cpu_rk4_rate(w, 1, threads)
-    rate, el = cpu_rk4_rate(w, nst, threads)
+    first, nst = ref_window(args)
+    oracle, o = _oracle()
+    p = oracle.make_params(**c.params())
+    # untimed: the reference's own (FP64) trajectory up to the window
+    x, y, vx, vy = o.rk4_fixed(c.x, c.y, c.vx, c.vy, c.q, c.m, p, w.dt, first, 0, threads, 0.0)
+    t0 = time.perf_counter()
+    o.rk4_fixed(x, y, vx, vy, c.q, c.m, p, w.dt, nst, first, threads, first * w.dt)
+    el = time.perf_counter() - t0
+    rate = 4.0 * c.n * (c.n - 1) * nst / el
     out = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": nst, "warmup": min(args.warmup, 1), "ms_per_step": el / nst * 1e3,
+        "steps": nst, "warmup": first, "ms_per_step": el / nst * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generator, demon_simulation_code_gb300/workloads.py)",
         "config": config_of(w, args, {"precision": "fp64 (CPU)"}),
+        "window": {"first_step": first, "steps": nst,
+                   "state": f"the oracle's own FP64 trajectory from the seeded initial state "
+                            f"(steps 0..{first - 1} untimed)"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{nst} RK4 steps of {w.name} (oracle/demon_oracle.c, OpenMP "
-                                   f"per-block locks as in ShieldedCoulombForce.cpp), "
-                                   f"{threads} threads, {el:.2f} s"},
+                         "sample": f"RK4 steps {first}..{first + nst - 1} of {w.name} "
+                                   f"(oracle/demon_oracle.c, OpenMP per-block locks as in "
+                                   f"ShieldedCoulombForce.cpp), {threads} threads, {el:.2f} s"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
     return 0
+
+
+def rel_err(a, b, ax, ay):
+    """||(a - ax, b - ay)||_2 / ||(ax, ay)||_2 and max_i |dF_i| / max_i |F_i|."""
+    d2 = (a - ax) ** 2 + (b - ay) ** 2
+    r2 = ax ** 2 + ay ** 2
+    return float(np.sqrt(d2.sum() / r2.sum())), float(np.sqrt(d2.max() / r2.max()))
 
 
 def run_gb300(args, world, rank, local):
@@ -251,19 +320,22 @@ def run_gb300(args, world, rank, local):
     if not torch.cuda.is_available():
         raise SystemExit("bench.py: no CUDA device")
     torch.cuda.set_device(local)
-    from demon_simulation_code_gb300 import Context, DeviceCloud
+    from demon_simulation_code_gb300 import Context, DeviceCloud, _lib
 
     w = workload(args.workload)
     c0 = w.clouds[0]
     n = c0.n
+    K = args.steps
     pairs_step = 4.0 * n * (n - 1)
+    prec = args.precision
     # a dedicated (non-default) stream shared by torch events and the library
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = Context(local)
     ctx.set_stream(stream.cuda_stream)
-    cloud = DeviceCloud.from_cloud(ctx, c0)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    radius = float(np.sqrt(np.max(c0.x ** 2 + c0.y ** 2)))  # scale of the trajectory errors
+    pin = (args.kernel, args.split) if args.kernel else None
 
     def barrier():
         if world > 1:
@@ -271,100 +343,192 @@ def run_gb300(args, world, rank, local):
 
             dist.barrier()
 
-    step_ms = []
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        import torch.distributed as dist
 
-    def timed_steps(prec, k):
-        evs = []
-        for _ in range(k):
+        t = torch.tensor([v], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def new_cloud(state, t, ctr, p=None, variant=None, forces=None):
+        """A cloud at `state` (caller order), force time t, RNG step ctr.
+        Every cloud of the window is made the same way, so they run the same
+        internal order and the same arithmetic from the same state."""
+        cl = DeviceCloud.from_cloud(ctx, c0)
+        if forces is not None:
+            cl.set_forces(forces)
+        if variant:
+            cl.set_kernel(*variant)
+        cl.upload(*state)
+        cl.set_time(t)
+        cl.set_step_counter(ctr)
+        cl.autotune(p or prec)  # the context's cached choice; sizes the split buffers before any timing
+        torch.cuda.synchronize()
+        return cl
+
+    def timed(cl, p, k, budget_s=None, keep=(), states=None):
+        """Up to k steps of cl, each timed alone with CUDA events on the
+        launching stream after a 256 MiB L2 flush; with budget_s, stops once
+        the steps so far took that long.  States at the step indices in
+        `keep` go into `states`.  Returns the per-step ms."""
+        ms, evs = [], []
+        t_start = time.perf_counter()
+        for i in range(k):
+            if states is not None and i in keep:
+                states[i] = cl.download()
             flush.fill_(1.0)
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            cloud.step(1, w.dt, prec)
+            cl.step(1, w.dt, p)
             b.record(stream)
             evs.append((a, b))
+            if budget_s is not None and i % 8 == 7:
+                torch.cuda.synchronize()
+                if time.perf_counter() - t_start > budget_s:
+                    break
         torch.cuda.synchronize()
         ms = [a.elapsed_time(b) for a, b in evs]
-        step_ms[:] = ms
-        return sum(ms) / 1e3
+        if states is not None:
+            states[len(ms)] = cl.download()
+        return ms
 
-    if args.kernel:
-        cloud.set_kernel(args.kernel, args.split)
-    tuned = cloud.autotune(args.precision)  # autotuner: variant x split on this cloud
-    # warm-up (untimed)
-    cloud.step(max(args.warmup, 3), w.dt, args.precision)
-    torch.cuda.synchronize()
+    # -- the window: autotuning and W warm-up steps from the seeded state,
+    #    then every number below starts from the state reached (s0)
+    warm = DeviceCloud.from_cloud(ctx, c0)
+    if pin:
+        warm.set_kernel(*pin)
+    tuned = warm.autotune(prec)  # autotuner: variant x split on this cloud
+    W_steps = max(args.warmup, 3)
+    warm.step(W_steps, w.dt, prec)
+    s0 = warm.download()
+    t0 = warm.get_time()
+    ctr0 = warm.get_step_counter()
+    warm.close()
 
-    # timed region: K steps, pair kernels bracketed by events inside the library
+    # -- value: K steps of the tuned kernel from s0
+    A = new_cloud(s0, t0, ctr0, variant=pin)
     ctx.profile(True)
     barrier()
     torch.cuda.synchronize()
     l0 = ctx.launch_count()
-    ev0 = cloud.evaluated_pairs()
+    ev0 = A.evaluated_pairs()
     with ClockSampler(local) as clk:
-        elapsed = timed_steps(args.precision, args.steps)
+        ms32 = timed(A, prec, K)
     launches_timed = ctx.launch_count() - l0
-    # ordered pairs the culling kernel swept (0: no culling variant ran, every pair was swept)
-    swept = cloud.evaluated_pairs() - ev0
-    pair_ms, launches, pairs_prof = ctx.profile_read()
-    main_step_ms = list(step_ms)
+    swept = A.evaluated_pairs() - ev0  # 0: no culling variant ran, every pair was swept
+    pair_ms, launches, _ = ctx.profile_read()
     ctx.profile(False)
-    t_max = elapsed
-    if world > 1:
-        import torch.distributed as dist
+    end_state = A.download()
+    A.close()
+    elapsed = sum(ms32) / 1e3
+    t_max = max_over_ranks(elapsed)
+    value = pairs_step * K * world / t_max
 
-        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = pairs_step * args.steps * world / t_max
+    # -- the same K steps again, untimed, keeping states: per-step swept pairs,
+    #    the densest step's input state, the output states, the CPU sample
+    out_every = 100 if K >= 200 else max(1, K // 4)
+    out_steps = set(range(out_every, K, out_every))
+    cpu_idx = sorted({int(round(v)) for v in np.linspace(0, K - 1, min(K, args.cpu_states))})
+    B = new_cloud(s0, t0, ctr0, variant=pin)
+    keep32, swept_steps = {}, []
+    dense_k, dense_state, dense_sw = 0, s0, -1
+    prev = B.evaluated_pairs()
+    for k in range(K):
+        st = B.download()
+        if k in out_steps or k in cpu_idx:
+            keep32[k] = st
+        B.step(1, w.dt, prec)
+        e = B.evaluated_pairs()
+        swept_steps.append(e - prev)
+        if e - prev > dense_sw:
+            dense_k, dense_state, dense_sw = k, st, e - prev
+        prev = e
+    keep32[K] = B.download()
+    replay_identical = all(np.array_equal(a, b) for a, b in zip(keep32[K], end_state))
+    B.close()
 
-    # FP64 kernel on the same workload (the 5x comparison)
-    fp64_value = None
-    if args.precision == "fp32c" and args.fp64_steps > 0:
-        c64 = DeviceCloud.from_cloud(ctx, c0)
-        c64.step(1, w.dt, "fp64")
-        torch.cuda.synchronize()
-        cloud_saved = cloud
-        cloud = c64
-        e64 = timed_steps("fp64", args.fp64_steps)
-        cloud = cloud_saved
-        fp64_value = pairs_step * args.fp64_steps / e64
-        c64.close()
+    # -- FP64 kernel from s0 over the first K64 steps of the window (all K
+    #    unless that exceeds the time budget), states at the output steps
+    states64 = {}
+    C = new_cloud(s0, t0, ctr0, p="fp64")
+    ms64 = timed(C, "fp64", min(K, args.fp64_steps or K), budget_s=args.fp64_budget, keep=out_steps,
+                 states=states64)
+    C.close()
+    K64 = len(ms64)
+    fp64_value = pairs_step * K64 / (sum(ms64) / 1e3)
+    same32 = pairs_step * K64 / (sum(ms32[:K64]) / 1e3)
 
-    # end to end through the public API with host buffers: pinned H2D of the
-    # state, one RK4 step, D2H of the state, every step
-    pin = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(4)]
-    hx = [p.numpy() for p in pin]
-    st = cloud.download()
-    for dst, src in zip(hx, st):
+    # -- the fastest unculled FP32C kernel over the same K64 steps (culling
+    #    and precision separated)
+    unculled = None
+    if prec == "fp32c" and args.unculled:
+        cands = [v for v in _lib.kernel_variants() if v.startswith("fp32c<") and "cull" not in v]
+        best = None
+        for v in cands:
+            for sp in (0, 4, 8, 16, 32):
+                try:
+                    T = new_cloud(s0, t0, ctr0, variant=(v, sp))
+                except _lib.DemonError:
+                    continue
+                ms = sum(timed(T, prec, 2))
+                T.close()
+                if best is None or ms < best[0]:
+                    best = (ms, v, sp)
+        U = new_cloud(s0, t0, ctr0, variant=best[1:])
+        msu = timed(U, prec, K64)
+        U.close()
+        uval = pairs_step * K64 / (sum(msu) / 1e3)
+        unculled = {"variant": best[1], "split": best[2], "steps": K64, "value": uval,
+                    "over_fp64": uval / fp64_value,
+                    "culled_over_unculled": same32 / uval}
+
+    # -- end to end through the public API with host buffers: pinned H2D of
+    #    the state, one RK4 step, D2H of the state, every step, from s0
+    pinned = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(4)]
+    hx = [p.numpy() for p in pinned]
+    for dst, src in zip(hx, s0):
         dst[:] = src
-    e2e_cloud = DeviceCloud.from_cloud(ctx, c0)
-    e2e_cloud.upload(*hx)
-    e2e_cloud.step(1, w.dt, args.precision)
-    torch.cuda.synchronize()
+    E = new_cloud(s0, t0, ctr0, variant=pin)
     barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        e2e_cloud.upload(*hx)
-        e2e_cloud.step(1, w.dt, args.precision)
-        e2e_cloud.download(out=hx)  # back into the same pinned buffers
     torch.cuda.synchronize()
-    e2e_el = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
+    t_e = time.perf_counter()
+    for _ in range(K):
+        E.upload(*hx)
+        E.step(1, w.dt, prec)
+        E.download(out=hx)  # back into the same pinned buffers
+    torch.cuda.synchronize()
+    e2e_el = max_over_ranks(time.perf_counter() - t_e)
+    E.close()
+    e2e_value = pairs_step * K * world / e2e_el
+    e2e_same = all(np.array_equal(a, b) for a, b in zip(hx, end_state))
 
-        t = torch.tensor([e2e_el], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_el = float(t.item())
-    e2e_value = pairs_step * args.e2e_steps * world / e2e_el if args.e2e_steps > 0 else None
-
-    # roofline of the dominant kernel (fused pair + stage, FP32 pipe bound)
-    peak = ctx.probe_peak("fp32")
-    avg_launch_s = pair_ms / 1e3 / max(launches, 1)
-    achieved = FLOPS_PER_PAIR * n * (n - 1) / avg_launch_s / 1e12
-    kname = "pair_stage_fp32c" if args.precision == "fp32c" else "pair_stage_fp64"
-    swept_frac = swept / (pairs_step * args.steps) if swept > 0 else 1.0
-    traffic = traffic_from_profiles(kname + ("_cull" if "cull" in tuned[0] else ""), w.name)
+    # -- force error of the timed kernel at the window's last and densest
+    #    states (shielded-Coulomb force alone), FP32C vs the FP64 kernel
+    coul = {**c0.params(), "flags": W.SHIELDED_COULOMB}
+    parity = {"forces": "shielded-Coulomb pair force alone", "R_m": radius}
+    force_states = {"end": (K, keep32[K]), "dense": (dense_k, dense_state)}
+    gpu_forces = {}
+    for tag, (k, st) in force_states.items():
+        F = new_cloud(st, t0, ctr0 + k, variant=pin, forces=coul)
+        f32 = F.eval_forces(prec)
+        f64 = F.eval_forces("fp64")
+        F.close()
+        gpu_forces[tag] = (st, f32, f64)
+        e2, emax = rel_err(*f32, *f64)
+        parity[f"e_F_{prec}_vs_fp64_{tag}"] = e2
+        parity[f"maxrel_F_{prec}_vs_fp64_{tag}"] = emax
+    parity["dense_step"] = dense_k
+    parity["dense_swept_fraction"] = dense_sw / pairs_step if dense_sw > 0 else None
+    # trajectory divergence FP32C vs FP64 from the same s0 at each output
+    traj = []
+    for k in sorted(set(states64) & set(keep32)):
+        a, b = keep32[k], states64[k]
+        d = np.sqrt((a[0] - b[0]) ** 2 + (a[1] - b[1]) ** 2) / radius
+        traj.append({"step": k, "rms_over_R": float(np.sqrt(np.mean(d ** 2))), "max_over_R": float(d.max())})
+    parity["trajectory_fp32c_vs_fp64"] = traj
 
     # batched workload (256 clouds of uneven N, one persistent launch per stage)
     batch = None
@@ -383,19 +547,13 @@ def run_gb300(args, world, rank, local):
         b = torch.cuda.Event(enable_timing=True)
         barrier()
         torch.cuda.synchronize()
-        ev0 = bt.evaluated_pairs()
+        bev0 = bt.evaluated_pairs()
         a.record(stream)
         bt.step(args.batch_steps, wb.dt)
         b.record(stream)
         torch.cuda.synchronize()
-        el = a.elapsed_time(b) / 1e3
-        bswept = bt.evaluated_pairs() - ev0
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([el], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(a.elapsed_time(b) / 1e3)
+        bswept = bt.evaluated_pairs() - bev0
         name, nitems, grid = bt.info()
         batch = {"workload": wb.name, "value": 4.0 * wb.pairs_per_eval * args.batch_steps / el,
                  "unit": UNIT, "steps": args.batch_steps, "ms_per_step": el / args.batch_steps * 1e3,
@@ -419,18 +577,18 @@ def run_gb300(args, world, rank, local):
         fit = TrajectoryFit(wa, precision="fp32c")
         fit.loss_and_grad()  # warm-up
         torch.cuda.synchronize()
-        l0 = fit.K.ctx.launch_count()
+        al0 = fit.K.ctx.launch_count()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
-        t0 = time.perf_counter()
+        t_a = time.perf_counter()
         a.record(stream)
         for _ in range(args.adjoint_grads):
             L, _ = fit.loss_and_grad()
         b.record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+        wall = time.perf_counter() - t_a
         el = a.elapsed_time(b) / 1e3
-        sweeps = (fit.K.ctx.launch_count() - l0) / args.adjoint_grads  # force + VJP launches per gradient
+        sweeps = (fit.K.ctx.launch_count() - al0) / args.adjoint_grads  # force + VJP launches per gradient
         adjoint = {"workload": wa.name, "clouds": len(fit.ns), "n": fit.ns[0], "steps": fit.steps,
                    "checkpoint_every": fit.every, "precision": "fp32c",
                    "seconds_per_gradient": el / args.adjoint_grads,
@@ -440,30 +598,61 @@ def run_gb300(args, world, rank, local):
                    "loss": float(L.item()), "gradients": "kappa, q, k_c per cloud; initial positions"}
         del fit
 
-    cpu = None
-    if rank == 0 and not args.no_cpu and args.cpu_steps > 0:
+    # CPU legs (rank 0, N = 1 host): the oracle on the window's own states
+    cpu = cpu1 = None
+    if rank == 0 and not args.no_cpu and args.cpu_states > 0:
+        oracle, o = _oracle()
+        pp = oracle_pair_params(oracle, c0)
+        for tag, (st, f32, f64) in gpu_forces.items():
+            rx, ry = o.forces(*st, c0.q, c0.m, pp, 0, 1, cpu_threads(), 0.0)
+            parity[f"e_F_{prec}_vs_oracle_{tag}"] = rel_err(*f32, rx, ry)[0]
+            parity[f"e_F_fp64_vs_oracle_{tag}"] = rel_err(*f64, rx, ry)[0]
+        sample = [(k, keep32[k], ctr0 + k, t0 + k * w.dt) for k in cpu_idx]
         threads = cpu_threads()
-        rate, el = cpu_rk4_rate(w, args.cpu_steps, threads)
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_steps} RK4 steps of {w.name} (oracle/demon_oracle.c, "
-                         f"OpenMP per-block locks as in the reference), {threads} threads, "
-                         f"{el:.2f} s"}
+        for nth, budget in ((threads, args.cpu_budget), (1, args.cpu_budget_1core)):
+            rate, el, done, unit = cpu_sample_rate(w, sample, nth, budget)
+            rec = {"value": rate, "unit": UNIT, "cores": nth, "kind": "port",
+                   "sample": f"one {unit} from each of the window's states at steps {done} "
+                             f"(of {K}, same states as the GPU run; oracle/demon_oracle.c, OpenMP "
+                             f"per-block locks as in the reference), {nth} thread(s), {el:.2f} s"}
+            if nth == threads:
+                cpu = rec
+            else:
+                cpu1 = rec
+
+    # roofline of the dominant kernel (fused pair + stage, FP32 pipe bound)
+    peak = ctx.probe_peak("fp32")
+    avg_launch_s = pair_ms / 1e3 / max(launches, 1)
+    achieved = FLOPS_PER_PAIR * n * (n - 1) / avg_launch_s / 1e12
+    kname = "pair_stage_fp32c" if prec == "fp32c" else "pair_stage_fp64"
+    swept_frac = swept / (pairs_step * K) if swept > 0 else 1.0
+    traffic = traffic_from_profiles(kname + ("_cull" if "cull" in tuned[0] else ""), w.name)
 
     if rank == 0:
         res = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps * 1e3,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W_steps, "ms_per_step": t_max / K * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32" if args.precision == "fp32c" else "f64",
+            "dtype": "f32" if prec == "fp32c" else "f64",
             "data": "synthetic (seeded generator, demon_simulation_code_gb300/workloads.py)",
             "config": config_of(w, args),
+            "window": {"first_step": W_steps, "steps": K,
+                       "state": "every figure below starts from the state after the warm-up steps "
+                                "(same internal order, force time and RNG counter)",
+                       "replay_bit_identical": replay_identical},
             "tuning": {"variant": tuned[0], "split": tuned[1]},
             "fp64_value": fp64_value,
-            "fp32c_over_fp64": (value / world / fp64_value) if fp64_value else None,
+            "fp64_steps": K64,
+            "fp32c_value_same_steps": same32,
+            "fp32c_over_fp64": same32 / fp64_value,
+            "fp32c_unculled": unculled,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * n,
-                    "d2h_bytes_per_step": 4 * 8 * n, "steps": args.e2e_steps},
-            "step_ms_percentiles": {p: float(np.percentile(main_step_ms, q))
+                    "d2h_bytes_per_step": 4 * 8 * n, "steps": K, "same_trajectory": e2e_same},
+            "parity": parity,
+            "step_ms_percentiles": {p: float(np.percentile(ms32, q))
                                     for p, q in (("p10", 10), ("p50", 50), ("p90", 90), ("max", 100))},
+            "swept_fraction_per_step": {p: float(np.percentile(np.array(swept_steps) / pairs_step, q))
+                                        for p, q in (("p10", 10), ("p50", 50), ("p90", 90), ("max", 100))},
             "gpu_launches": launches_timed,
             "roofline": {"bound": "fp32-pipe", "kernel": kname, "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
@@ -480,6 +669,7 @@ def run_gb300(args, world, rank, local):
             "batch": batch,
             "adjoint": adjoint,
             "cpu_baseline": cpu,
+            "cpu_baseline_1core": cpu1,
             "clocks": clk.summary(),
         }
         print(json.dumps(res))

@@ -982,14 +982,12 @@ int dm_cloud_set_charge_mass(dm_cloud *c, const double *q, const double *m) {
 int dm_cloud_set_forces(dm_cloud *c, const dm_force_params *p) {
     if (!c || !p) return DM_ERR_ARG;
     dm_ctx *ctx = c->ctx;
-    if (p->flags & ~kAllForces)
-        return ctx->fail(DM_ERR_UNSUPPORTED, "dm_cloud_set_forces: unknown force flags 0x%llx",
-                         (unsigned long long)(p->flags & ~kAllForces));
-    if ((p->flags & kShieldedCoulomb) && !(p->shielding > 0.0 && std::isfinite(p->shielding)))
-        return ctx->fail(DM_ERR_ARG, "dm_cloud_set_forces: shielding must be positive and finite");
-    if (p->thermal_mode != 0 && p->thermal_mode != 1)
-        return ctx->fail(DM_ERR_ARG, "dm_cloud_set_forces: thermal_mode must be 0 or 1");
-    std::memcpy(&c->f, p, sizeof(ForceParams));
+    ForceParams fp;
+    std::memcpy(&fp, p, sizeof(ForceParams));
+    const char *why = nullptr;
+    if (const int st = check_force_params(fp, &why))
+        return ctx->fail(st, "dm_cloud_set_forces: %s (flags 0x%llx)", why, (unsigned long long)p->flags);
+    c->f = fp;
     c->d.rc2 = (p->shielding > 0.0) ? (10.0 / p->shielding) * (10.0 / p->shielding) : 0.0;
     c->drop_graphs();
     // the stage buffers carry a per-particle filter bound that depends on kappa
@@ -1533,12 +1531,11 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     long long total = 0;
     for (int c = 0; c < nclouds; c++) {
         if (n[c] < 1) return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d has n = %d", c, n[c]);
-        if (params[c].flags & ~kAllForces)
-            return ctx->fail(DM_ERR_UNSUPPORTED, "dm_batch_create: unknown force flags in cloud %d", c);
-        if (params[c].thermal_mode != 0 && params[c].thermal_mode != 1)
-            return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d thermal_mode must be 0 or 1", c);
-        if ((params[c].flags & kShieldedCoulomb) && !(params[c].shielding > 0.0))
-            return ctx->fail(DM_ERR_ARG, "dm_batch_create: cloud %d shielding must be positive", c);
+        ForceParams fp;
+        std::memcpy(&fp, &params[c], sizeof(ForceParams));
+        const char *why = nullptr;
+        if (const int st = check_force_params(fp, &why))
+            return ctx->fail(st, "dm_batch_create: cloud %d: %s", c, why);
         total += n[c];
     }
     if (total > (1LL << 30)) return ctx->fail(DM_ERR_ARG, "dm_batch_create: too many particles");
@@ -1909,8 +1906,11 @@ int dm_adjoint_create(dm_ctx *ctx, int nclouds, const int *n, const dm_force_par
         if (params[c].flags & ~known)
             return ctx->fail(DM_ERR_UNSUPPORTED, "dm_adjoint_create: only confinement, drag and shielded "
                                                  "Coulomb forces are differentiated");
-        if ((params[c].flags & kShieldedCoulomb) && !(params[c].shielding > 0.0))
-            return ctx->fail(DM_ERR_ARG, "dm_adjoint_create: shielding must be positive");
+        ForceParams fp;
+        std::memcpy(&fp, &params[c], sizeof(ForceParams));
+        const char *why = nullptr;
+        if (const int st = check_force_params(fp, &why))
+            return ctx->fail(st, "dm_adjoint_create: cloud %d: %s", c, why);
     }
     DM_CUDA(ctx, cudaSetDevice(ctx->device));
     dm_adjoint *A = new dm_adjoint();

@@ -19,6 +19,7 @@
 //                    cutoff test never selects them.
 #pragma once
 
+#include <cfloat>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -73,6 +74,27 @@ struct CloudDev {
     double coulomb;                // 1/(4 pi eps0)
     int *orig;                     // caller's index of internal slot s (Morton order)
 };
+
+// Host-side check of a force parameter set, shared by every entry point that
+// takes one: DM_OK (0), or a status with *why set to a static message.
+// Flags must be among the fifteen ForceFlag bits (status 6, unsupported);
+// with ShieldedCoulomb on, kappa must be positive and finite (the cutoff is
+// kappa*r < 10) and thermal_mode must be 0 or 1 (status 1, bad argument).
+inline int check_force_params(const ForceParams &p, const char **why) {
+    if (p.flags & ~kAllForces) {
+        *why = "unknown force flags";
+        return 6;
+    }
+    if ((p.flags & kShieldedCoulomb) && !(p.shielding > 0.0 && p.shielding <= DBL_MAX)) {
+        *why = "shielding must be positive and finite";
+        return 1;
+    }
+    if (p.thermal_mode != 0 && p.thermal_mode != 1) {
+        *why = "thermal_mode must be 0 or 1";
+        return 1;
+    }
+    return 0;
+}
 
 enum StageMode : int { kModeStep = 0, kModeForceOnly = 1 };
 

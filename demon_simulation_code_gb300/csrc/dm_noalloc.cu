@@ -19,10 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <cstdio>
 #include <cstring>
-#include <mutex>
-#include <string>
 
 #include "../../include/demon_gb300.h"
 #include "dm_misc.cuh"
@@ -38,12 +35,9 @@ constexpr int kMaxParticles = kDiagThreads * kMaxBlocks;
 // The scratch: one row of 5 partial sums per block.
 static __device__ __align__(256) double g_diag_scratch[kMaxBlocks * 5];
 
-// In host code g_diag_scratch names a host-side stand-in, not device memory;
-// the device address is looked up once per device (with that device current)
-// and cached here.
-constexpr int kMaxDevices = 64;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
-std::mutex g_setup_mutex;
+// In host code g_diag_scratch names a host-side stand-in, not device memory:
+// the device address is looked up on every call, with the calling device
+// current (see scratch_for_current_device).
 
 // Sums the per-block partials into out[0..4] (one block, strided partial
 // sums then a tree): a fixed order for a given block count.
@@ -62,31 +56,16 @@ __global__ void __launch_bounds__(256) diag_finish(const double *partial, int nb
     if (threadIdx.x < 5) out[threadIdx.x] = red[threadIdx.x][0];
 }
 
-// Errors are reported by status code only (no message store is shared with
-// the rest of the library).
-int fail(int code, const std::string &msg) {
-    (void)msg;
-    return code;
-}
-
-// Per-device set-up: runs on the first call on each device, with that
-// device current.  It may load the module, so make that first call before
-// any stream capture.
+// The device address of the scratch on the current device.  Looked up on
+// every call rather than cached: the lookup allocates nothing, and a cached
+// address would dangle after the host application calls cudaDeviceReset
+// (the module is loaded again and the array may move).  The first call on a
+// device may load this library's module there, so make that first call
+// before any stream capture.
 int scratch_for_current_device(double **out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(DM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(DM_ERR_UNSUPPORTED, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_diag_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(DM_ERR_CUDA, std::string("cudaGetSymbolAddress(g_diag_scratch): ") +
-                                         cudaGetErrorString(e));
-        g_scratch_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_scratch_addr[dev];
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_diag_scratch) != cudaSuccess || !p) return DM_ERR_CUDA;
+    *out = static_cast<double *>(p);
     return DM_OK;
 }
 
@@ -97,17 +76,17 @@ extern "C" int dm_diagnostics_noalloc(int n, const double *d_x, const double *d_
                                       const double *d_q, const double *d_m,
                                       const dm_force_params *params, double *d_out,
                                       void *stream) {
-    if (n < 1 || n > kMaxParticles)
-        return fail(DM_ERR_ARG, "dm_diagnostics_noalloc: n = " + std::to_string(n) +
-                                    " outside [1, " + std::to_string(kMaxParticles) +
-                                    "] (the fixed scratch holds " + std::to_string(kMaxBlocks) +
-                                    " blocks of " + std::to_string(kDiagThreads) + ")");
-    if (!d_x || !d_y || !d_vx || !d_vy || !d_q || !d_m || !d_out || !params)
-        return fail(DM_ERR_ARG, "dm_diagnostics_noalloc: NULL pointer");
-    if ((params->flags & DM_SHIELDED_COULOMB_FORCE) && !(params->shielding > 0.0))
-        return fail(DM_ERR_ARG, "dm_diagnostics_noalloc: shielding must be positive");
+    // Errors are reported by status code only (no message store is shared
+    // with the rest of the library, and building one would allocate).
+    if (n < 1 || n > kMaxParticles) return DM_ERR_ARG;  // the scratch holds kMaxBlocks blocks
+    if (!d_x || !d_y || !d_vx || !d_vy || !d_q || !d_m || !d_out || !params) return DM_ERR_ARG;
+    ForceParams f;
+    static_assert(sizeof(ForceParams) == sizeof(dm_force_params), "layout");
+    memcpy(&f, params, sizeof(f));
+    const char *why = nullptr;
+    if (const int st = check_force_params(f, &why)) return st;  // same rules as dm_cloud_set_forces
     double *scratch = nullptr;
-    int rc = scratch_for_current_device(&scratch);
+    const int rc = scratch_for_current_device(&scratch);
     if (rc) return rc;
 
     CloudDev c{};
@@ -119,9 +98,6 @@ extern "C" int dm_diagnostics_noalloc(int n, const double *d_x, const double *d_
     c.vy = const_cast<double *>(d_vy);
     c.q = const_cast<double *>(d_q);
     c.m = const_cast<double *>(d_m);
-    ForceParams f;
-    static_assert(sizeof(ForceParams) == sizeof(dm_force_params), "layout");
-    memcpy(&f, params, sizeof(f));
     const double coulomb = 1.0 / (4.0 * M_PI * 8.8541878E-12);
     const int blocks = (n + kDiagThreads - 1) / kDiagThreads;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -131,7 +107,5 @@ extern "C" int dm_diagnostics_noalloc(int n, const double *d_x, const double *d_
         diag_finish<<<1, 256, 0, s>>>(scratch, blocks, d_out);
         e = cudaGetLastError();
     }
-    if (e != cudaSuccess)
-        return fail(DM_ERR_CUDA, std::string("dm_diagnostics_noalloc launch: ") + cudaGetErrorString(e));
-    return DM_OK;
+    return e == cudaSuccess ? DM_OK : DM_ERR_CUDA;
 }

@@ -36,17 +36,22 @@ def imbalance(ns, parts) -> float:
     return max(w) / (sum(w) / len(w)) if sum(w) else 1.0
 
 
-def gather_per_cloud(values, ids, nclouds: int, group=None):
-    """Per-cloud values computed on each rank (values[k] for cloud ids[k],
-    a float64 array of shape [len(ids), ...]) -> the full [nclouds, ...]
-    array on every rank (all_gather of a zero-padded buffer + sum; each
-    cloud belongs to exactly one rank)."""
+def gather_per_cloud(values, ids, nclouds: int, width: int | None = None, group=None):
+    """Per-cloud values computed on each rank (values[k] for cloud ids[k])
+    -> the full array on every rank: [nclouds] when width is None, else
+    [nclouds, width].  Every rank builds the same zero-filled shape from
+    (nclouds, width), not from its own values, so a rank that owns no cloud
+    (more ranks than clouds) still reduces a buffer of the same size; the
+    buffers are summed with one all_reduce (each cloud belongs to exactly one
+    rank)."""
     import torch
     import torch.distributed as dist
 
-    values = np.asarray(values, dtype=np.float64)
-    full = np.zeros((nclouds,) + values.shape[1:], dtype=np.float64)
-    full[np.asarray(ids, dtype=np.int64)] = values
+    shape = (nclouds,) if width is None else (nclouds, int(width))
+    ids = np.asarray(ids, dtype=np.int64)
+    values = np.asarray(values, dtype=np.float64).reshape((len(ids),) + shape[1:])
+    full = np.zeros(shape, dtype=np.float64)
+    full[ids] = values
     t = torch.from_numpy(full)
     if dist.get_backend(group) == "nccl":
         t = t.cuda()

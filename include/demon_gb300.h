@@ -371,8 +371,11 @@ int dm_adjoint_vjp(dm_adjoint *adj, int precision, const double *x,
  * file-scope device array of 4096 x 5 doubles (160 KiB, held by every GPU
  * that loads this library until the process exits).
  *  - n must be in [1, 524288]; larger n returns DM_ERR_ARG without launching.
- *  - The first call on each device looks up that array's device address with
- *    the device current; make that first call before any stream capture.
+ *  - params are checked as dm_cloud_set_forces checks them.
+ *  - Every call looks up that array's device address on the current device
+ *    (so the address stays right after a cudaDeviceReset); the first call on
+ *    a device may load this library's module there, so make that first call
+ *    before any stream capture.
  *  - All calls share the array: calls that overlap on the GPU race on it and
  *    must be serialised by the caller (e.g. one stream).
  * Errors are reported by the status code only (dm_last_error is not set). */

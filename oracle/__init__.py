@@ -106,8 +106,16 @@ def _ptr(a):
     return a.ctypes.data_as(_dp)
 
 
+def ref_dir() -> str | None:
+    """The reference checkout named by the environment variable
+    DEMON_REF_DIR (None when unset or not a directory)."""
+    d = os.environ.get("DEMON_REF_DIR", "")
+    return d if d and os.path.isdir(d) else None
+
+
 def build(ref: bool = False) -> None:
-    """Compile the restatement (and, if asked and possible, the reference)."""
+    """Compile the restatement (and, if asked, the reference from the
+    checkout named by DEMON_REF_DIR)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)

@@ -3,9 +3,10 @@
 Runs the reference sources compiled by oracle/Makefile (`make ref`,
 serial build, so the summation order is the reference's single-thread
 order) on seeded inputs and records inputs and outputs.  Needs the
-reference checkout (read at build time only) and an x86-64 host.
+reference checkout named by the environment variable DEMON_REF_DIR (read at
+build time only) and an x86-64 host.
 
-    python tests/golden/make_golden.py [fixture names]   # all, or only these
+    DEMON_REF_DIR=<reference checkout> python tests/golden/make_golden.py [fixture names]
 """
 from __future__ import annotations
 

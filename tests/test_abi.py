@@ -80,3 +80,27 @@ def test_workloads_are_seeded():
     ns = [c.n for c in w.clouds]
     assert len(ns) == 256 and min(ns) >= 64 and max(ns) <= 4096
     assert W.disk512().pairs_per_eval == 512 * 511
+
+
+def test_noalloc_rejects_bad_sizes_and_params_before_any_device_call():
+    """dm_diagnostics_noalloc checks its size limit and its force parameters
+    on the host, before it looks up its scratch or launches anything, with
+    the same parameter rules as dm_cloud_set_forces -- so these rejections
+    need no GPU."""
+    import ctypes
+
+    lib = _lib.load(build())
+    fake = 16  # never dereferenced: every case below is rejected on the host
+    ok = dict(flags=W.CONFINEMENT | W.DRAG | W.SHIELDED_COULOMB, shielding=2e4, confine=1e8, gamma=3.0)
+    cases = [
+        (0, ok, _lib.DM_ERR_ARG),
+        (524288 + 1, ok, _lib.DM_ERR_ARG),
+        (64, {**ok, "shielding": float("inf")}, _lib.DM_ERR_ARG),
+        (64, {**ok, "shielding": 0.0}, _lib.DM_ERR_ARG),
+        (64, {**ok, "thermal_mode": 2}, _lib.DM_ERR_ARG),
+        (64, {**ok, "flags": ok["flags"] | (1 << 20)}, 6),  # DM_ERR_UNSUPPORTED
+    ]
+    for n, params, want in cases:
+        p = _lib.force_params(**params)
+        rc = lib.dm_diagnostics_noalloc(n, *([fake] * 6), ctypes.byref(p), fake, None)
+        assert rc == want, (n, params, rc)

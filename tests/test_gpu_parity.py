@@ -292,7 +292,7 @@ def test_reorder_interval_does_not_change_fp64_results_beyond_rounding(gpu_ctx):
 
 # kernel families by precision: FP32C has the shared-memory (fp32c) and the
 # streamed (fp32s) sweeps
-FAMILIES = {"fp64": ("fp64<",), "fp32c": ("fp32c<", "fp32s<")}
+FAMILIES = {"fp64": ("fp64<",), "fp32c": ("fp32c<",)}
 
 
 def _variants(prec):

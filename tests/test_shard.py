@@ -41,7 +41,7 @@ def _free_port():
     return p
 
 
-def _worker(rank, world, port, out_dir):
+def _worker(rank, world, port, out_dir, nclouds=12):
     import torch.distributed as dist
 
     import oracle
@@ -51,7 +51,7 @@ def _worker(rank, world, port, out_dir):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        clouds = W.batch256(nclouds=12, nmin=16, nmax=128).clouds
+        clouds = W.batch256(nclouds=nclouds, nmin=16, nmax=128).clouds
         ids = assign_clouds([c.n for c in clouds], world)[rank]
         o = oracle.Oracle()
         vals = []
@@ -59,7 +59,7 @@ def _worker(rank, world, port, out_dir):
             cl = clouds[c]
             d = o.diagnostics(cl.x, cl.y, cl.vx, cl.vy, cl.q, cl.m, oracle.make_params(**cl.params()))
             vals.append(d)
-        full = gather_per_cloud(np.array(vals).reshape(len(ids), 5), ids, len(clouds))
+        full = gather_per_cloud(np.array(vals).reshape(len(ids), 5), ids, len(clouds), width=5)
         total = sum_scalar(float(sum(v[1] for v in vals)))
         np.save(os.path.join(out_dir, f"r{rank}.npy"), np.concatenate([full.ravel(), [total]]))
     finally:
@@ -80,3 +80,21 @@ def test_gloo_two_ranks_gather_per_cloud_results(tmp_path):
                     for c in clouds])
     assert np.array_equal(r0[:-1].reshape(12, 5), ref)
     assert abs(r0[-1] - ref[:, 1].sum()) <= 1e-12 * abs(ref[:, 1].sum())
+
+
+def test_gloo_more_ranks_than_clouds(tmp_path):
+    """Three ranks, two clouds: the rank that owns no cloud reduces a buffer
+    of the same shape as the others, and all three get the full result."""
+    import torch.multiprocessing as mp
+
+    import oracle
+
+    mp.spawn(_worker, args=(3, _free_port(), str(tmp_path), 2), nprocs=3, join=True)
+    outs = [np.load(tmp_path / f"r{r}.npy") for r in range(3)]
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+    clouds = W.batch256(nclouds=2, nmin=16, nmax=128).clouds
+    assert [len(p) for p in assign_clouds([c.n for c in clouds], 3)].count(0) == 1
+    o = oracle.Oracle()
+    ref = np.array([o.diagnostics(c.x, c.y, c.vx, c.vy, c.q, c.m, oracle.make_params(**c.params()))
+                    for c in clouds])
+    assert np.array_equal(outs[0][:-1].reshape(2, 5), ref)

@@ -47,6 +47,43 @@ def test_noalloc_diagnostics_matches_cloud_diagnostics_twice():
         np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-30)
 
 
+def _call(lib, c0, params, stream):
+    import torch
+
+    dev = [torch.tensor(a, dtype=torch.float64, device="cuda")
+           for a in (c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m)]
+    out = torch.full((5,), float("nan"), dtype=torch.float64, device="cuda")
+    p = _lib.force_params(**params)
+    rc = lib.dm_diagnostics_noalloc(c0.n, *(t.data_ptr() for t in dev), ctypes.byref(p),
+                                    out.data_ptr(), stream)
+    assert rc == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_noalloc_diagnostics_match_the_oracle_including_the_size_limit():
+    """The device reduction itself (per-block partials in the fixed scratch,
+    then one block's strided sums) against the oracle's FP64 diagnostics:
+    a small cloud, then n = 524,288, the most the scratch holds (4096
+    blocks, each of the finishing block's 256 threads summing 16 rows) --
+    with the pair term off so that the large call stays short."""
+    import torch
+
+    import oracle
+
+    lib = _lib.load()
+    o = oracle.Oracle()
+    stream = torch.cuda.current_stream().cuda_stream
+    small = _cloud(2048, 3)
+    big = _cloud(524288, 4)
+    for c0, flags in ((small, None), (big, 3)):
+        params = c0.params() if flags is None else {**c0.params(), "flags": flags}
+        got = _call(lib, c0, params, stream)
+        ref = o.diagnostics(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m, oracle.make_params(**params))
+        scale = np.abs(ref).max()
+        np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-11 * scale)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     import torch
 
