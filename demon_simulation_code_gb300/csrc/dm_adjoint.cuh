@@ -103,7 +103,7 @@ __device__ __forceinline__ void adj_tile_fp64(const AdjCloud &d, const AdjJ *sj,
 // from the fast reciprocal: a few ulp per pair term, far below the rounding
 // of the FP32 pair sums themselves.
 template <int MODE>
-__device__ __forceinline__ void adj_tile_fp32c(const AdjCloud &d, const ExpConsts &E, const float4 *sp,
+__device__ __forceinline__ void adj_tile_fp32c(const AdjCloud &d, const float4 *sp,
                                                const float4 *sa, int cnt, int jbase, int li, float xh, float yh,
                                                float xl, float yl, float qci, float axi, float ayi,
                                                const double *__restrict__ x, const double *__restrict__ y,
@@ -163,8 +163,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(
     const double *__restrict__ vy, const double *__restrict__ q, const double *__restrict__ m,
     const double *__restrict__ ax, const double *__restrict__ ay,  // MODE 1: force adjoint
     double *__restrict__ o0, double *__restrict__ o1, double *__restrict__ o2, double *__restrict__ o3,
-    double *__restrict__ o4, double *__restrict__ o5, double *__restrict__ o6, double coulomb,
-    const ExpConsts E) {
+    double *__restrict__ o4, double *__restrict__ o5, double *__restrict__ o6, double coulomb) {
     // FP64: AdjJ[kAdjTile] + float2[kAdjTile]; FP32C: two float4[kAdjTile]
     constexpr int kSmem = F32C ? 2 * 16 * kAdjTile : (int)(sizeof(AdjJ) + 8) * kAdjTile;
     __shared__ __align__(16) unsigned char smem[kSmem];
@@ -203,7 +202,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(
             }
             __syncthreads();
             if (valid)
-                adj_tile_fp32c<MODE>(d, E, sp, sa, cnt, j0, li, xh, yh, xl, yl, qci, axf, ayf, x, y, xi, yi, fs,
+                adj_tile_fp32c<MODE>(d, sp, sa, cnt, j0, li, xh, yh, xl, yl, qci, axf, ayf, x, y, xi, yi, fs,
                                      fc);
         } else {
             AdjJ *sj = reinterpret_cast<AdjJ *>(smem);

@@ -144,23 +144,17 @@ int check_device_errors(dm_ctx *ctx, dm_cloud *c) {
     return device_error_status(ctx, c, h);
 }
 
-ExpConsts make_exp_consts() {
-    ExpConsts E;
-    const double l2e = 1.4426950408889634;
-    E.l2e_hi = (float)l2e;
-    E.l2e_lo = (float)(l2e - (double)E.l2e_hi);
-    const double ln2 = 0.69314718055994530942;
-    double fact = 1.0, pw = 1.0;
-    for (int k = 0; k < 8; k++) {
-        if (k > 0) { fact *= k; pw *= -ln2; }
-        E.c[k] = (float)(pw / fact);
-    }
-    return E;
-}
-
-const ExpConsts &exp_consts() {
-    static const ExpConsts E = make_exp_consts();
-    return E;
+// The FP32C sweep's threshold for evaluating a filtered chunk directly
+// (StageParams::direct_min): at least this many of a slot's 128 (lane, j)
+// pairs passed the filter.  DM_DIRECT_MIN_HITS overrides it (1..129; 129
+// never evaluates directly).
+int direct_min_hits() {
+    static const int v = [] {
+        const char *e = getenv("DM_DIRECT_MIN_HITS");
+        const int k = e ? atoi(e) : 0;
+        return (k >= 1 && k <= 129) ? k : 48;
+    }();
+    return v;
 }
 
 // kappa*log2(e) as a float pair (hi + lo to ~2^-48 relative).
@@ -191,7 +185,8 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     P.rc2_lo = (float)(P.rc2 * (1.0 - 4e-6));
     P.rc2_hi = (float)(P.rc2 * (1.0 + 4e-6));
     P.kappa_f = (float)kappa;
-    kappa_log2e(kappa, P.kl2e_hi, P.kl2e_lo);
+    P.nkl2e = (float)(-kappa * 1.4426950408889634);
+    P.direct_min = direct_min_hits();
     return P;
 }
 
@@ -212,7 +207,7 @@ struct Variant {
 
 template <int NW, int ILP, int TC, bool CL, bool CULL>
 cudaError_t launch_fp32c(const cudaLaunchConfig_t *cfg, const StageParams &P) {
-    return cudaLaunchKernelEx(cfg, pair_stage_fp32c<NW, ILP, TC, CL, CULL>, P, exp_consts());
+    return cudaLaunchKernelEx(cfg, pair_stage_fp32c<NW, ILP, TC, CL, CULL>, P);
 }
 template <int NI, int G, int ILP, int JT>
 cudaError_t launch_fp64(const cudaLaunchConfig_t *cfg, const StageParams &P) {
@@ -1297,8 +1292,7 @@ struct BatchVariant {
 template <int NW, int ILP, int TC, bool CULL>
 cudaError_t launch_batch(dim3 g, dim3 b, size_t smem, cudaStream_t s, const StageParams &P,
                          const BatchCloud *desc, const int2 *items, int nitems, unsigned int *ctr) {
-    return launch_pdl(batch_stage_fp32c<NW, ILP, TC, CULL>, g, b, smem, s, P, desc, items, nitems, ctr,
-                      exp_consts());
+    return launch_pdl(batch_stage_fp32c<NW, ILP, TC, CULL>, g, b, smem, s, P, desc, items, nitems, ctr);
 }
 
 #define DM_BATCH_VARIANT(NW, ILP, TC, CULL, SUFFIX)                                                \
@@ -1376,6 +1370,7 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf =
     P.coulomb = B->d.coulomb;
     P.fx_out = B->d_fx;
     P.fy_out = B->d_fy;
+    P.direct_min = direct_min_hits();
     const int slot = (mode == kModeForceOnly) ? 0 : stage - 1;
     if (k.cull) {  // group boxes of the buffer this stage reads
         const int br = (mode == kModeForceOnly) ? fo_buf : (stage - 1) & 1;
@@ -1615,7 +1610,7 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
         bc.rc2_lo = (float)(bc.rc2 * (1.0 - 4e-6));
         bc.rc2_hi = (float)(bc.rc2 * (1.0 + 4e-6));
         bc.kappa_f = (float)kappa;
-        kappa_log2e(kappa, bc.kl2e_hi, bc.kl2e_lo);
+        bc.nkl2e = (float)(-kappa * 1.4426950408889634);
         for (int i = 0; i < n[c]; i++) {
             seg[off + i] = c;
             orig[off + i] = off + i;
@@ -1886,12 +1881,10 @@ void adj_launch(dm_adjoint *A, int precision, const double *x, const double *y, 
     cudaStream_t st = A->ctx->stream;
     if (precision == DM_FP32C)
         adjoint_kernel<MODE, true><<<A->nblocks, kAdjThreads, 0, st>>>(
-            A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, o0, o1, o2, o3, o4, o5, o6, A->coulomb,
-            exp_consts());
+            A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, o0, o1, o2, o3, o4, o5, o6, A->coulomb);
     else
         adjoint_kernel<MODE, false><<<A->nblocks, kAdjThreads, 0, st>>>(
-            A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, o0, o1, o2, o3, o4, o5, o6, A->coulomb,
-            exp_consts());
+            A->ddesc, A->dcloud, A->dtile, x, y, vx, vy, q, m, ax, ay, o0, o1, o2, o3, o4, o5, o6, A->coulomb);
 }
 }  // namespace
 

@@ -24,7 +24,7 @@ struct BatchCloud {
     ForceParams f;
     double rc2;
     float rc2_lo, rc2_hi, kappa_f;
-    float kl2e_hi, kl2e_lo;  // kappa*log2(e) as a float pair
+    float nkl2e;    // -kappa*log2(e)
 };
 
 // A StageParams view of one cloud: pointers offset to the cloud's particles.
@@ -48,15 +48,13 @@ __device__ __forceinline__ void batch_view(StageParams &V, const StageParams &P0
     V.rc2_lo = d.rc2_lo;
     V.rc2_hi = d.rc2_hi;
     V.kappa_f = d.kappa_f;
-    V.kl2e_hi = d.kl2e_hi;
-    V.kl2e_lo = d.kl2e_lo;
+    V.nkl2e = d.nkl2e;
 }
 
 template <int NW, int ILP, int TC, bool CULL = false>
 __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     batch_stage_fp32c(const StageParams P0, const BatchCloud *__restrict__ desc,
-                      const int2 *__restrict__ items, int nitems, unsigned int *counter,
-                      const ExpConsts E) {
+                      const int2 *__restrict__ items, int nitems, unsigned int *counter) {
     constexpr int TILE = 32 * ILP;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ StageParams sV;
@@ -73,13 +71,14 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
         if (tid == 0) batch_view(sV, P0, desc[w.x]);
         __syncthreads();
         const int tile = w.y;
-        fp32c_sweep<NW, ILP, TC, CULL>(sV, E, tile, 0, 1, smem_raw);
+        fp32c_sweep<NW, ILP, TC, CULL>(sV, tile, 0, 1, smem_raw);
         if (tid < TILE) {
             const int i = tile * TILE + tid;
             if (i < sV.c.n) {
                 const float4 v = s_red[tid];
-                stage_epilogue(sV, i, (double)v.x - (double)v.z, (double)v.y - (double)v.w,
-                               stage_thermal(sV, i));
+                const double cq = pair_scale(sV, i);
+                stage_epilogue(sV, i, __dmul_rn(cq, (double)v.x - (double)v.z),
+                               __dmul_rn(cq, (double)v.y - (double)v.w), stage_thermal(sV, i));
             }
         }
         __syncthreads();  // before the next item reuses shared memory

@@ -115,7 +115,11 @@ struct StageParams {
     double rc2;           // (10/kappa)^2
     float rc2_lo, rc2_hi; // FP32 certain-in / certain-out bounds on r^2
     float kappa_f;
-    float kl2e_hi, kl2e_lo;  // kappa*log2(e) as a float pair
+    float nkl2e;          // -kappa*log2(e): e^{-kappa r} = 2^{nkl2e r}
+    // FP32C sweep: a filtered chunk whose 4 j pass the filter for at least
+    // this many of the 128 (lane, j) pairs of a slot is evaluated directly
+    // (all lanes, cutoff by a select) instead of through per-lane hit bits
+    int direct_min;
     // j split without clusters: rank r of tile t is block t*split + r and
     // writes its partial sums to partial[r*n_pad + i]; stage_finish sums them
     int split;

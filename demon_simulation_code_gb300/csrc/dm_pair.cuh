@@ -6,19 +6,21 @@
 // stage/combine loops (see dm_device.cuh).
 //
 // Work decomposition (owner computes, no atomics on forces):
-//   * an i-tile of NT*ILP particles belongs to one thread-block CLUSTER of S
-//     CTAs; thread t of every CTA owns particles i = tile*NT*ILP + k*NT + t,
-//     k < ILP, kept in registers;
-//   * CTA rank r of the cluster sweeps the r-th of S contiguous j ranges,
-//     staging JT j particles at a time in shared memory;
-//   * each pair is first filtered with the expanded distance
-//       |p_i|^2 + |p_j|^2 - 2 p_i.p_j < (r_c + margin)^2
-//     (2 FMAs per pair with |p_j|^2 precomputed), and only surviving pairs
-//     run the precise force arithmetic -- the GPU form of the reference's
-//     early exit for kappa*r >= 10 (ShieldedCoulombForce.cpp:178-180);
-//   * the S partial sums of a particle are combined through distributed
-//     shared memory (DSMEM) inside the cluster, in rank order, and the
-//     stage epilogue runs once per particle.
+//   * an i-tile of 32*ILP particles belongs to S CTAs (a thread-block
+//     cluster, or S plain blocks whose partial sums stage_finish adds); lane
+//     l of every warp of those CTAs owns particles i = tile*32*ILP + k*32 + l,
+//     k < ILP (the lane's i "slots"), kept in registers;
+//   * rank r of the S sweeps every S-th chunk of 4 j (or, culling, every
+//     S-th 32-particle j group within reach of the tile), staging them in
+//     shared memory; the CTA's warps deal the staged chunks round-robin;
+//   * pairs of groups that may hold a pair within the cutoff are first
+//     filtered with the expanded distance |p_j|^2 - 2 p_i.p_j against a per-i
+//     bound (two j per packed FMA) -- the GPU form of the reference's early
+//     exit for kappa*r >= 10 (ShieldedCoulombForce.cpp:178-180); groups
+//     entirely within the cutoff skip the filter;
+//   * the pair terms are evaluated two j at a time in packed f32x2
+//     arithmetic (pair2_terms); the per-particle sums are compensated and the
+//     stage epilogue runs once per particle in FP64.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -29,30 +31,6 @@
 
 namespace dm {
 namespace cg = cooperative_groups;
-
-// log2(e) as a float pair, and Taylor coefficients c_k = (-ln 2)^k / k! of
-// 2^-f on |f| <= 1/2 (degree 7: truncation error < 6e-9 relative).
-struct ExpConsts {
-    float l2e_hi, l2e_lo;
-    float c[8];
-};
-
-// e^{-a} for a >= 0 in FP32 with the argument carried as a float pair:
-// t = a*log2(e) = t_hi + t_lo exactly to ~2^-48, n = rint(t_hi),
-// f = (t_hi - n) + t_lo, e^{-a} = 2^-n * poly(f) (Cody-Waite style range
-// reduction; the 2^-n scale is exact).
-__device__ __forceinline__ float exp_neg(float a, const ExpConsts &E) {
-    const float t_hi = a * E.l2e_hi;
-    const float t_lo = fmaf(a, E.l2e_hi, -t_hi) + a * E.l2e_lo;
-    const float n = rintf(t_hi);
-    const float f = (t_hi - n) + t_lo;
-    float p = E.c[7];
-#pragma unroll
-    for (int k = 6; k >= 0; k--) p = fmaf(p, f, E.c[k]);
-    const int e = 127 - (int)n;
-    const float scale = __int_as_float((e > 0 ? e : 0) << 23);
-    return p * scale;
-}
 
 // e^{-kappa r} on the SFU with kappa*log2(e) = k_hi + k_lo given as a float
 // pair: t = k_hi r rounded to FP32 (absolute error up to ~1e-6 at kappa r =
@@ -88,6 +66,82 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
     s = t;
 }
 
+// ---------------------------------------------------------------------------
+// Packed f32x2 arithmetic: one instruction evaluates the same operation for
+// two j against one i (sm_100+ FADD2/FMUL2/FFMA2), halving the issue slots
+// of the pair arithmetic.  Both halves round exactly like the scalar
+// operations.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// One i particle, each value duplicated into both halves of a pair: hi and
+// lo parts of the two-float position (x = xh + xl).
+struct PairI {
+    float2 xh, yh, xl, yl;
+};
+
+// Pair terms of i with two j, the j values negated (nxh = -xh_j, ...):
+//   dx = x_i - x_j as (xh_i - xh_j) + (xl_i - xl_j) (the hi difference is
+//        exact for nearby particles, so dx keeps ~2^-24 of its own size),
+//   r2 = dx^2 + dy^2,
+//   w  = q_j e^{-kappa r} y^2 (y + kappa), y = 1/r,
+// so that the force on i from j is C q_i w (dx, dy) = C q_i q_j (1 + kappa
+// r) e^{-kappa r} / r^3 (dx, dy), the reference's pair force
+// (ShieldedCoulombForce.cpp:144-157), C q_i applied once per particle.
+// 1/r: hardware rsqrt plus one Newton step, which also gives r = r2 y
+// refined; e^{-kappa r} = 2^{-(kappa log2 e) r} on the SFU.  A pair at
+// r2 = 0 gives non-finite w: callers exclude j == i by a select.
+__device__ __forceinline__ void pair2_terms(const PairI &I, float2 nxh, float2 nyh, float2 nxl, float2 nyl,
+                                            float2 q, float2 kap, float2 nkl2e, float2 &dx, float2 &dy,
+                                            float2 &r2, float2 &w) {
+    dx = add2(add2(I.xh, nxh), add2(I.xl, nxl));
+    dy = add2(add2(I.yh, nyh), add2(I.yl, nyl));
+    r2 = fma2(dx, dx, mul2(dy, dy));
+    const float2 y0 = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+    const float2 u = mul2(r2, y0);                       // r, unrefined
+    const float2 h = mul2(fma2(u, y0, dup2(-1.0f)), dup2(-0.5f));  // (1 - r2 y0^2) / 2
+    const float2 y = fma2(h, y0, y0);                    // 1/r after one Newton step
+    const float2 r = fma2(h, u, u);                      // r = r2 y, from the same step
+    const float2 nt = mul2(r, nkl2e);                    // -(kappa log2 e) r
+    const float2 ex = make_float2(ex2_approx(nt.x), ex2_approx(nt.y));
+    w = mul2(mul2(q, ex), mul2(mul2(y, y), add2(y, kap)));
+}
+
+// The scalar form of one pair for the slow path (pairs within 4e-6 of the
+// cutoff in r^2, decided exactly as the reference decides): w as in
+// pair2_terms, 0 for a pair outside the cutoff.  j values negated.
+__device__ __forceinline__ float border_pair(const StageParams &P, int b, const PairI &I, int ii, float nxh,
+                                             float nyh, float nxl, float nyl, float q, int jg, float &dx,
+                                             float &dy) {
+    dx = (I.xh.x + nxh) + (I.xl.x + nxl);
+    dy = (I.yh.x + nyh) + (I.yl.x + nyl);
+    double r, a;
+    if (jg == ii || jg < 0 ||
+        !ref_in_cutoff(P.c.px[b][ii] - P.c.px[b][jg], P.c.py[b][ii] - P.c.py[b][jg], P.f.shielding, r, a))
+        return 0.0f;
+    const float r2 = fmaf(dx, dx, dy * dy);
+    float y = rsqrt_approx(r2);
+    const float u = r2 * y;
+    const float h = -0.5f * fmaf(u, y, -1.0f);
+    y = fmaf(h, y, y);
+    const float rr = fmaf(h, u, u);
+    const float ex = ex2_approx(rr * P.nkl2e);
+    return (q * ex) * ((y * y) * (y + P.kappa_f));
+}
+
 struct PairTuning {
     int nt, ilp, jt, s;
 };
@@ -95,26 +149,27 @@ struct PairTuning {
 // ---------------------------------------------------------------------------
 // FP32-compensated kernel.
 //
-// CTA = G j-groups x NI i-lanes.  Lane t of every group owns the ILP
-// particles i = tile*NI*ILP + k*NI + t; group g sweeps every G-th j of each
-// shared-memory tile, so all G groups reuse one tile.  Hot registers per
-// particle: -2*xh, -2*yh (packed in pairs for the f32x2 FMA), the filter
-// threshold and the Kahan sums; the rest of the particle's data lives in
-// shared memory.
-//
-// Filter hits are not evaluated where they are found.  Per j the warp takes
-// one uniform branch (vote over lanes and slots); when some lane's filter
-// fired, the warp ballots each slot and queues (j, ballot) in shared memory.
-// Every 32 queued entries of a slot (and at the end of a tile) a 32x32
-// bit-matrix transpose gives each lane the set of queued j it hit, and all
-// lanes run the precise path on their own hits together.  Each lane
-// accumulates only into its own sums, so the result is deterministic and no
-// atomics are needed; SIMD utilisation of the precise path goes from ~1/32
-// (sparse) or the hit fraction (dense) to mean/max of the per-lane hit count.
+// A CTA of NW warps shares one i tile of 32*ILP particles (lane l, slot k ->
+// i = tile*32*ILP + k*32 + l).  Each staged j chunk (4 j) goes to one warp;
+// its pairs are classified:
+//   * groups entirely within the cutoff of the tile (box test): evaluated
+//     directly, every lane on the same j from shared-memory broadcasts, two
+//     j per packed instruction, no filter and no cutoff test;
+//   * other groups within reach: the packed filter on all 4 j and every
+//     slot, one warp vote per chunk; where it fired, per slot, the number
+//     of (lane, j) pairs that passed decides (a warp reduction): at least
+//     P.direct_min of the 128 -> the chunk is evaluated directly for that
+//     slot with the cutoff taken by a select; fewer -> each lane records its
+//     own passing j as hit bits (4 per chunk, 8 chunks per 32-bit word) and
+//     later evaluates them two at a time.
+// Each lane accumulates only into its own sums (plain f32x2 sums over a few
+// chunks, then Kahan), so the result is deterministic and needs no atomics.
+// The sums leave out C q_i (applied in FP64 once per particle).
 // ---------------------------------------------------------------------------
 template <int NW, int ILP, int TC>
 struct Fp32cSmem {
-    // j tile: TC 4-j chunks as structure of arrays (x, y, |p|^2) + precise data
+    // j tile: TC 4-j chunks as structure of arrays (-xh, -yh, |p|^2) for the
+    // filter + (-xl, -yl, q, j) per j
     static constexpr size_t tile = (size_t)TC * (3 * sizeof(float4) + 4 * sizeof(float4));
     static constexpr size_t cold = (size_t)ILP * 32 * sizeof(float4);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
@@ -156,107 +211,27 @@ __device__ __forceinline__ bool boxes_inside(const float4 &a, const float4 &b, f
     return fmaf(dx, dx, dy * dy) < 0.999f * rc2_lo;
 }
 
-// 32x32 bit-matrix transpose across a warp: lane r holds row r on entry and
-// column r (bit c = bit r of row c) on exit.
-__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
-#pragma unroll
-    for (int st = 0; st < 5; st++) {
-        const int j = 16 >> st;
-        const uint32_t m = masks[st];
-        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
-        // lanes with bit j clear keep their low half-blocks and take the
-        // partner's; lanes with it set the reverse
-        if (lane & j) x = (x & ~m) | ((y & ~m) >> j);
-        else x = (x & m) | ((y & m) << j);
-    }
-    return x;
-}
-
-// Calls f(std::integral_constant<int, k>) for k = 0 .. K-1 (compile-time k).
-template <int K, typename F>
-__device__ __forceinline__ void static_for(F &&f) {
-    if constexpr (K > 0) {
-        static_for<K - 1>(f);
-        f(std::integral_constant<int, K - 1>{});
-    }
-}
-
-struct PairCtx {
-    float xl, yl, qc;
-    int ii;
-};
-
-// The pair force on i from j (added into px, py; nothing for j == i or a
-// pair outside the cutoff).
-__device__ __forceinline__ void precise_pair(const StageParams &P, int b,
-                                             float xh_i, float yh_i, const PairCtx &ic,
-                                             const float4 &A, const float4 &Bj, int jg, float &px,
-                                             float &py) {
-    if (jg == ic.ii) return;
-    const float dx = (xh_i - A.x) + (ic.xl - Bj.x);
-    const float dy = (yh_i - A.y) + (ic.yl - Bj.y);
-    const float r2 = fmaf(dx, dx, dy * dy);
-    bool in = r2 < P.rc2_hi;
-    if (in && !(r2 < P.rc2_lo)) {
-        // borderline: decide exactly as the reference does
-        double r, a;
-        in = ref_in_cutoff(P.c.px[b][ic.ii] - P.c.px[b][jg], P.c.py[b][ic.ii] - P.c.py[b][jg],
-                           P.f.shielding, r, a);
-    }
-    if (!in) return;
-    // 1/r: hardware rsqrt + one Newton step
-    float y = rsqrtf(r2);
-    const float h = r2 * y;
-    const float ee = fmaf(-h, y, 1.0f);
-    y = fmaf(0.5f * ee, y, y);
-    const float ex = exp_neg_kr(r2 * y, P.kl2e_hi, P.kl2e_lo);
-    // C q_i q_j (1 + kappa r) e^{-kappa r} / r^3 = C q_i q_j e^{-kappa r} y^2 (y + kappa), y = 1/r
-    const float s = ((ic.qc * A.w) * ex) * ((y * y) * (y + P.kappa_f));
-    px = fmaf(s, dx, px);
-    py = fmaf(s, dy, py);
-}
-
-// The pair force on i from j for a pair known to be inside the cutoff (a
-// j group entirely within reach of the i tile, never one of the tile's own
-// groups, so j != i): the precise arithmetic with no cutoff test.
-__device__ __forceinline__ void inside_pair(const StageParams &P, float xh_i, float yh_i, const PairCtx &ic,
-                                            float xj, float yj, const float4 &Bj, float &px, float &py) {
-    const float dx = (xh_i - xj) + (ic.xl - Bj.x);
-    const float dy = (yh_i - yj) + (ic.yl - Bj.y);
-    const float r2 = fmaf(dx, dx, dy * dy);
-    float y = rsqrtf(r2);
-    const float h = r2 * y;
-    const float ee = fmaf(-h, y, 1.0f);
-    y = fmaf(0.5f * ee, y, y);
-    const float ex = exp_neg_kr(r2 * y, P.kl2e_hi, P.kl2e_lo);
-    const float s = ((ic.qc * Bj.z) * ex) * ((y * y) * (y + P.kappa_f));
-    px = fmaf(s, dx, px);
-    py = fmaf(s, dy, py);
-}
-
 // The FP32C sweep of one i tile against rank `rank` of S of the j chunks:
-// i-side setup, filtered j loop with the compaction queue, and the combine
-// of the NW warps' Kahan sums into s_red[TILE] = (sx, sy, cx, cy).  Ends with
-// the block synchronised.  `P` may live in shared memory (batched kernel).
-// Particles are those of P.c (n = P.c.n); j at or beyond n read as padding,
-// so a cloud needs no padding of its own.
+// i-side setup, the classified j loop, and the combine of the NW warps'
+// Kahan sums into s_red[TILE] = (sx, sy, cx, cy) (force / (C q_i) = s - c).
+// Ends with the block synchronised.  `P` may live in shared memory (batched
+// kernel).  Particles are those of P.c (n = P.c.n); j at or beyond n read as
+// padding, so a cloud needs no padding of its own.
 template <int NW, int ILP, int TC, bool CULL = false>
-__device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConsts &E, int tile,
-                                            int rank, int S, unsigned char *smem_raw) {
+__device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int rank, int S,
+                                            unsigned char *smem_raw) {
     constexpr int NT = NW * 32;
     constexpr int TILE = 32 * ILP;  // particles per i tile
     static_assert(ILP <= 4, "the i slots of a lane are selected with unrolled compares");
-    float4 *s_x4 = reinterpret_cast<float4 *>(smem_raw);  // [TC] xh of 4 j
-    float4 *s_y4 = s_x4 + TC;                              // [TC] yh
+    float4 *s_x4 = reinterpret_cast<float4 *>(smem_raw);  // [TC] -xh of 4 j
+    float4 *s_y4 = s_x4 + TC;                              // [TC] -yh
     float4 *s_b4 = s_y4 + TC;                              // [TC] xh^2 + yh^2
-    float4 *s_pb = s_b4 + TC;                              // [4*TC] (xl, yl, q, j)
-    float4 *s_cold = s_pb + 4 * TC;                        // [ILP][32]
+    float4 *s_pj = s_b4 + TC;                              // [4*TC] (-xl, -yl, q, j)
+    float4 *s_cold = s_pj + 4 * TC;                        // [ILP][32] (xl, yl, -, i)
     float4 *s_acc = s_cold + ILP * 32;                     // [NW][ILP][32]
-    float4 *s_red = s_acc + NW * ILP * 32;                                 // [TILE]
-    int *s_glist = reinterpret_cast<int *>(s_red + TILE);                  // [NT] surviving groups
-    int *s_wcount = s_glist + NT;                                          // [NW]
+    float4 *s_red = s_acc + NW * ILP * 32;                 // [TILE]
+    int *s_glist = reinterpret_cast<int *>(s_red + TILE);  // [NT] surviving groups
+    int *s_wcount = s_glist + NT;                          // [NW]
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
@@ -265,11 +240,13 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
     const float4 *__restrict__ pa = P.c.pa[b];
     const float4 *__restrict__ pb = P.c.pb[b];
     float4 *my_acc = s_acc + warp * ILP * 32;
+    const float2 kap = dup2(P.kappa_f), nkl2e = dup2(P.nkl2e);
+    const float rc2_lo = P.rc2_lo, rc2_hi = P.rc2_hi;
 
     // every warp owns the same TILE particles: lane l, slot k -> i = tile*TILE + k*32 + l.
     // i side duplicated into both halves of a packed pair: the packed FMAs
     // evaluate two consecutive j against one i
-    float2 mx2[ILP], my2[ILP], nu2[ILP];
+    float2 px2[ILP], py2[ILP], nu2[ILP];  // 2 xh_i, 2 yh_i, -(filter bound)
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
         const int i = tile * TILE + k * 32 + lane;
@@ -281,20 +258,31 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
             ax = A.x;
             ay = A.y;
             nu = B.z;
-            cold = make_float4(B.x, B.y, B.w, __int_as_float(i));
+            cold = make_float4(B.x, B.y, 0.0f, __int_as_float(i));
         }
-        mx2[k] = make_float2(-2.0f * ax, -2.0f * ax);
-        my2[k] = make_float2(-2.0f * ay, -2.0f * ay);
-        nu2[k] = make_float2(nu, nu);
+        px2[k] = dup2(2.0f * ax);
+        py2[k] = dup2(2.0f * ay);
+        nu2[k] = dup2(nu);
         if (warp == 0) s_cold[k * 32 + lane] = cold;
         my_acc[k * 32 + lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
+    // i side of slot k (runtime k: the slow paths exist once in the code)
+    auto slot_i = [&](int k, int &ii) {
+        float xh = 0.5f * px2[0].x, yh = 0.5f * py2[0].x;
+#pragma unroll
+        for (int t = 1; t < ILP; t++) {
+            xh = (k == t) ? 0.5f * px2[t].x : xh;
+            yh = (k == t) ? 0.5f * py2[t].x : yh;
+        }
+        const float4 c4 = s_cold[k * 32 + lane];
+        ii = __float_as_int(c4.w);
+        return PairI{dup2(xh), dup2(yh), dup2(c4.x), dup2(c4.y)};
+    };
 
     // Filter hits are recorded per lane: bit 4*g + u of hits[k] is the pair
     // (slot k's i, j = 4*(cbase + g*NW) + u of the staged tile), for the
-    // last (up to 8) chunks this warp swept.  The flush runs the precise
-    // path on every lane's own hits, slot by slot (the slot is a runtime
-    // value, so the precise path exists once in the kernel's code).
+    // last (up to 8) chunks this warp swept.  The flush evaluates every
+    // lane's own hits two at a time, slot by slot.
     uint32_t hits[ILP];
 #pragma unroll
     for (int k = 0; k < ILP; k++) hits[k] = 0u;
@@ -304,37 +292,43 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
 #pragma unroll 1
         for (int k = 0; k < ILP; k++) {
             uint32_t m = hits[0];
-            float xh = -0.5f * mx2[0].x, yh = -0.5f * my2[0].x;
 #pragma unroll
-            for (int t = 1; t < ILP; t++) {
-                m = (k == t) ? hits[t] : m;
-                xh = (k == t) ? -0.5f * mx2[t].x : xh;
-                yh = (k == t) ? -0.5f * my2[t].x : yh;
-            }
+            for (int t = 1; t < ILP; t++) m = (k == t) ? hits[t] : m;
             if (!__any_sync(0xffffffffu, m != 0u)) continue;
-            const float4 c4 = s_cold[k * 32 + lane];
-            PairCtx ic;
-            ic.xl = c4.x;
-            ic.yl = c4.y;
-            ic.qc = c4.z;
-            ic.ii = __float_as_int(c4.w);
+            int ii;
+            const PairI I = slot_i(k, ii);
             float4 acc = my_acc[k * 32 + lane];
             const int jbase = 4 * cbase;  // j of bit 0
-            // up to 4 pair terms are summed plainly, each group then added to
-            // the compensated sums (the group's rounding is that of one pair term)
             while (m) {
-                float px = 0.0f, py = 0.0f;
-#pragma unroll 1
-                for (int g = 0; g < 4 && m; g++) {
-                    const int e = __ffs(m) - 1;
-                    m &= m - 1u;
-                    const int jj = jbase + (e >> 2) * (4 * NW) + (e & 3);  // index into the tile's j
-                    const float4 Bj = s_pb[jj];
-                    precise_pair(P, b, xh, yh, ic, make_float4(s_xf[jj], s_yf[jj], 0.0f, Bj.z), Bj,
-                                 __float_as_int(Bj.w), px, py);
+                // two hits per packed evaluation; a missing second one
+                // repeats the first with q = 0 (a finite, zero term)
+                const int e0 = __ffs(m) - 1;
+                m &= m - 1u;
+                const int e1 = m ? __ffs(m) - 1 : e0;
+                const float q1 = m ? 1.0f : 0.0f;
+                m &= m - 1u;
+                const int j0 = jbase + (e0 >> 2) * (4 * NW) + (e0 & 3);  // index into the tile's j
+                const int j1 = jbase + (e1 >> 2) * (4 * NW) + (e1 & 3);
+                const float4 B0 = s_pj[j0], B1 = s_pj[j1];
+                float2 dx, dy, r2, w;
+                pair2_terms(I, make_float2(s_xf[j0], s_xf[j1]), make_float2(s_yf[j0], s_yf[j1]),
+                            make_float2(B0.x, B1.x), make_float2(B0.y, B1.y), make_float2(B0.z, B1.z * q1), kap,
+                            nkl2e, dx, dy, r2, w);
+                const int g0 = __float_as_int(B0.w), g1 = __float_as_int(B1.w);
+                // certainly inside: r2 < rc2_lo; borderline pairs decided exactly
+                w.x = (r2.x < rc2_lo && g0 != ii) ? w.x : 0.0f;
+                w.y = (r2.y < rc2_lo && g1 != ii && q1 != 0.0f) ? w.y : 0.0f;
+                if (!(r2.x < rc2_lo) && r2.x < rc2_hi) {
+                    float bx, by;
+                    w.x = border_pair(P, b, I, ii, s_xf[j0], s_yf[j0], B0.x, B0.y, B0.z, g0, bx, by);
                 }
-                kahan_add(acc.x, acc.z, px);
-                kahan_add(acc.y, acc.w, py);
+                if (q1 != 0.0f && !(r2.y < rc2_lo) && r2.y < rc2_hi) {
+                    float bx, by;
+                    w.y = border_pair(P, b, I, ii, s_xf[j1], s_yf[j1], B1.x, B1.y, B1.z, g1, bx, by);
+                }
+                const float2 fx = mul2(w, dx), fy = mul2(w, dy);
+                kahan_add(acc.x, acc.z, fx.x + fx.y);
+                kahan_add(acc.y, acc.w, fy.x + fy.y);
             }
             my_acc[k * 32 + lane] = acc;
         }
@@ -342,39 +336,48 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         for (int k = 0; k < ILP; k++) hits[k] = 0u;
     };
 
-    // Chunk c of the staged tile against the i slots in `full` (bit k: slot
-    // k), every lane evaluating the same 4 j; pair terms summed plainly and
-    // added to the slot's compensated sums.  The slot is a runtime value, so
-    // the precise path appears once here, as in flush_hits.
-    auto direct_chunk = [&](int c, uint32_t full) {
-#pragma unroll 1
-        for (int k = 0; k < ILP; k++) {
-            if (!((full >> k) & 1u)) continue;
-            float xh = -0.5f * mx2[0].x, yh = -0.5f * my2[0].x;
-#pragma unroll
-            for (int t = 1; t < ILP; t++) {
-                xh = (k == t) ? -0.5f * mx2[t].x : xh;
-                yh = (k == t) ? -0.5f * my2[t].x : yh;
-            }
-            const float4 c4 = s_cold[k * 32 + lane];
-            PairCtx ic;
-            ic.xl = c4.x;
-            ic.yl = c4.y;
-            ic.qc = c4.z;
-            ic.ii = __float_as_int(c4.w);
-            float px = 0.0f, py = 0.0f;
+    // Chunk c of the staged tile against slot k (runtime k), every lane on
+    // the same 4 j, the cutoff taken by a select (pairs within 4e-6 of it in
+    // r^2 decided exactly, j == i excluded); the chunk's terms summed plainly
+    // and added to the slot's compensated sums.
+    auto direct_chunk = [&](int c, int k) {
+        int ii;
+        const PairI I = slot_i(k, ii);
+        const float4 X = s_x4[c], Y = s_y4[c];
+        const float4 B0 = s_pj[4 * c], B1 = s_pj[4 * c + 1], B2 = s_pj[4 * c + 2], B3 = s_pj[4 * c + 3];
+        float2 dx, dy, r2, w, dx2, dy2, r22, w2;
+        pair2_terms(I, make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(B0.x, B1.x),
+                    make_float2(B0.y, B1.y), make_float2(B0.z, B1.z), kap, nkl2e, dx, dy, r2, w);
+        pair2_terms(I, make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(B2.x, B3.x),
+                    make_float2(B2.y, B3.y), make_float2(B2.z, B3.z), kap, nkl2e, dx2, dy2, r22, w2);
+        const int g0 = __float_as_int(B0.w), g1 = __float_as_int(B1.w);
+        const int g2 = __float_as_int(B2.w), g3 = __float_as_int(B3.w);
+        w.x = (r2.x < rc2_lo && g0 != ii) ? w.x : 0.0f;
+        w.y = (r2.y < rc2_lo && g1 != ii) ? w.y : 0.0f;
+        w2.x = (r22.x < rc2_lo && g2 != ii) ? w2.x : 0.0f;
+        w2.y = (r22.y < rc2_lo && g3 != ii) ? w2.y : 0.0f;
+        const bool bd = (!(r2.x < rc2_lo) && r2.x < rc2_hi) || (!(r2.y < rc2_lo) && r2.y < rc2_hi) ||
+                        (!(r22.x < rc2_lo) && r22.x < rc2_hi) || (!(r22.y < rc2_lo) && r22.y < rc2_hi);
+        float2 fx = fma2(w2, dx2, mul2(w, dx));
+        float2 fy = fma2(w2, dy2, mul2(w, dy));
+        if (bd) {  // rare: pairs within 4e-6 of the cutoff in r^2
 #pragma unroll 1
             for (int u = 0; u < 4; u++) {
+                const float rr = (u == 0) ? r2.x : (u == 1) ? r2.y : (u == 2) ? r22.x : r22.y;
+                if (rr < rc2_lo || !(rr < rc2_hi)) continue;
                 const int jj = 4 * c + u;
-                const float4 Bj = s_pb[jj];
-                precise_pair(P, b, xh, yh, ic, make_float4(s_xf[jj], s_yf[jj], 0.0f, Bj.z), Bj,
-                             __float_as_int(Bj.w), px, py);
+                const float4 Bj = s_pj[jj];
+                float bx, by;
+                const float wb = border_pair(P, b, I, ii, s_xf[jj], s_yf[jj], Bj.x, Bj.y, Bj.z,
+                                             __float_as_int(Bj.w), bx, by);
+                fx.x = fmaf(wb, bx, fx.x);
+                fy.x = fmaf(wb, by, fy.x);
             }
-            float4 acc = my_acc[k * 32 + lane];
-            kahan_add(acc.x, acc.z, px);
-            kahan_add(acc.y, acc.w, py);
-            my_acc[k * 32 + lane] = acc;
         }
+        float4 acc = my_acc[k * 32 + lane];
+        kahan_add(acc.x, acc.z, fx.x + fx.y);
+        kahan_add(acc.y, acc.w, fy.x + fy.y);
+        my_acc[k * 32 + lane] = acc;
     };
 
     // Sweeps the `count` chunks (4 consecutive j) of this CTA's list through
@@ -393,15 +396,15 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
                 if (jb + u < n) {
                     const float4 A = pa[jb + u];
                     const float4 B = pb[jb + u];
-                    xs[u] = A.x;
-                    ys[u] = A.y;
+                    xs[u] = -A.x;
+                    ys[u] = -A.y;
                     bs[u] = A.z;
-                    s_pb[4 * e + u] = make_float4(B.x, B.y, A.w, __int_as_float(jb + u));
-                } else {  // padding: never passes the filter
-                    xs[u] = kPadPosition;
-                    ys[u] = kPadPosition;
+                    s_pj[4 * e + u] = make_float4(-B.x, -B.y, A.w, __int_as_float(jb + u));
+                } else {  // padding: never passes the filter; a finite, zero term
+                    xs[u] = -kPadPosition;
+                    ys[u] = -kPadPosition;
                     bs[u] = INFINITY;
-                    s_pb[4 * e + u] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+                    s_pj[4 * e + u] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
                 }
             }
             s_x4[e] = make_float4(xs[0], xs[1], xs[2], xs[3]);
@@ -410,39 +413,52 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
         }
         __syncthreads();
         if constexpr (DENSE) {
-            // every pair of these groups is inside the cutoff: no filter, no
-            // queue; each lane evaluates its own i against the chunk's 4 j,
-            // with its i data and Kahan sums in registers for the whole tile
-            PairCtx ic[ILP];
-            float xhk[ILP], yhk[ILP];
+            // every pair of these groups is inside the cutoff (and j != i):
+            // no filter, no select; each lane evaluates its own i against the
+            // chunk's 4 j, two per packed instruction, its i data and sums in
+            // registers for the whole tile; plain sums over two chunks, then Kahan
+            PairI I[ILP];
             float4 acc[ILP];
+            float2 fx[ILP], fy[ILP];
 #pragma unroll
             for (int k = 0; k < ILP; k++) {
-                const float4 c4 = s_cold[k * 32 + lane];
-                ic[k].xl = c4.x;
-                ic[k].yl = c4.y;
-                ic[k].qc = c4.z;
-                ic[k].ii = __float_as_int(c4.w);
-                xhk[k] = -0.5f * mx2[k].x;
-                yhk[k] = -0.5f * my2[k].x;
+                int ii;
+                I[k] = slot_i(k, ii);
                 acc[k] = my_acc[k * 32 + lane];
+                fx[k] = fy[k] = dup2(0.0f);
             }
+            int ng = 0;
             for (int c = warp; c < tcn; c += NW) {
                 const float4 X = s_x4[c], Y = s_y4[c];
-                const float xs[4] = {X.x, X.y, X.z, X.w};
-                const float ys[4] = {Y.x, Y.y, Y.z, Y.w};
+                const float4 B0 = s_pj[4 * c], B1 = s_pj[4 * c + 1], B2 = s_pj[4 * c + 2], B3 = s_pj[4 * c + 3];
 #pragma unroll
                 for (int k = 0; k < ILP; k++) {
-                    float px = 0.0f, py = 0.0f;
-#pragma unroll 1
-                    for (int u = 0; u < 4; u++)
-                        inside_pair(P, xhk[k], yhk[k], ic[k], xs[u], ys[u], s_pb[4 * c + u], px, py);
-                    kahan_add(acc[k].x, acc[k].z, px);
-                    kahan_add(acc[k].y, acc[k].w, py);
+                    float2 dx, dy, r2, w;
+                    pair2_terms(I[k], make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(B0.x, B1.x),
+                                make_float2(B0.y, B1.y), make_float2(B0.z, B1.z), kap, nkl2e, dx, dy, r2, w);
+                    fx[k] = fma2(w, dx, fx[k]);
+                    fy[k] = fma2(w, dy, fy[k]);
+                    pair2_terms(I[k], make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(B2.x, B3.x),
+                                make_float2(B2.y, B3.y), make_float2(B2.z, B3.z), kap, nkl2e, dx, dy, r2, w);
+                    fx[k] = fma2(w, dx, fx[k]);
+                    fy[k] = fma2(w, dy, fy[k]);
+                }
+                if (++ng == 2) {
+                    ng = 0;
+#pragma unroll
+                    for (int k = 0; k < ILP; k++) {
+                        kahan_add(acc[k].x, acc[k].z, fx[k].x + fx[k].y);
+                        kahan_add(acc[k].y, acc[k].w, fy[k].x + fy[k].y);
+                        fx[k] = fy[k] = dup2(0.0f);
+                    }
                 }
             }
 #pragma unroll
-            for (int k = 0; k < ILP; k++) my_acc[k * 32 + lane] = acc[k];
+            for (int k = 0; k < ILP; k++) {
+                kahan_add(acc[k].x, acc[k].z, fx[k].x + fx[k].y);
+                kahan_add(acc[k].y, acc[k].w, fy[k].x + fy[k].y);
+                my_acc[k * 32 + lane] = acc[k];
+            }
         } else {
         // one flush site: the loop runs one step past the tile's last chunk
         int nb = 0, cbase = warp;  // chunks recorded in hits, chunk of bit group 0
@@ -454,37 +470,33 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
                 const float2 X01 = make_float2(X.x, X.y), X23 = make_float2(X.z, X.w);
                 const float2 Y01 = make_float2(Y.x, Y.y), Y23 = make_float2(Y.z, Y.w);
                 const float2 B01 = make_float2(Bq.x, Bq.y), B23 = make_float2(Bq.z, Bq.w);
-                // d = |p_j|^2 - 2 p_i.p_j - threshold_i: pair (i, j) passes iff d < 0
+                // d = |p_j|^2 - 2 p_i.p_j - bound_i: pair (i, j) passes iff d < 0
                 float2 d01[ILP], d23[ILP];
                 uint32_t sgn = 0u;
 #pragma unroll
                 for (int k = 0; k < ILP; k++) {
-                    d01[k] = __ffma2_rn(mx2[k], X01, __ffma2_rn(my2[k], Y01, __fadd2_rn(B01, nu2[k])));
-                    d23[k] = __ffma2_rn(mx2[k], X23, __ffma2_rn(my2[k], Y23, __fadd2_rn(B23, nu2[k])));
+                    d01[k] = fma2(px2[k], X01, fma2(py2[k], Y01, add2(B01, nu2[k])));
+                    d23[k] = fma2(px2[k], X23, fma2(py2[k], Y23, add2(B23, nu2[k])));
                     sgn |= __float_as_uint(d01[k].x) | __float_as_uint(d01[k].y) | __float_as_uint(d23[k].x) |
                            __float_as_uint(d23[k].y);
                 }
                 if (__any_sync(0xffffffffu, (int)sgn < 0)) {
-                    // slots where every lane passed all 4 j: evaluate the chunk
-                    // now, all lanes on the same j (no hit bits, no per-lane
-                    // j lookup); the other slots record this lane's hits, the
-                    // sign bits of the 4 j
-                    uint32_t full = 0u;
-#pragma unroll
-                    for (int k = 0; k < ILP; k++) {
-                        const uint32_t all4 = __float_as_uint(d01[k].x) & __float_as_uint(d01[k].y) &
-                                              __float_as_uint(d23[k].x) & __float_as_uint(d23[k].y);
-                        full |= (__all_sync(0xffffffffu, (int)all4 < 0) ? 1u : 0u) << k;
-                    }
-                    if (full) direct_chunk(c, full);
+                    // per slot: enough passing (lane, j) pairs -> the whole
+                    // chunk directly; else this lane's hits as bits
+                    uint32_t direct = 0u;
 #pragma unroll
                     for (int k = 0; k < ILP; k++) {
                         const uint32_t bits = (__float_as_uint(d01[k].x) >> 31) |
                                               ((__float_as_uint(d01[k].y) >> 30) & 2u) |
                                               ((__float_as_uint(d23[k].x) >> 29) & 4u) |
                                               ((__float_as_uint(d23[k].y) >> 28) & 8u);
-                        hits[k] |= ((full >> k) & 1u) ? 0u : bits << (4 * nb);
+                        const bool dir = (int)__reduce_add_sync(0xffffffffu, __popc(bits)) >= P.direct_min;
+                        direct |= (dir ? 1u : 0u) << k;
+                        hits[k] |= dir ? 0u : bits << (4 * nb);
                     }
+#pragma unroll 1
+                    for (int k = 0; k < ILP; k++)
+                        if ((direct >> k) & 1u) direct_chunk(c, k);
                     any_hit = true;
                 }
                 nb++;
@@ -582,14 +594,19 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, const ExpConst
     __syncthreads();
 }
 
+// C q_i in FP64: the factor the FP32C sweeps leave out of their sums.
+__device__ __forceinline__ double pair_scale(const StageParams &P, int i) {
+    return __dmul_rn(P.coulomb, P.c.q[i]);
+}
+
 // CL = true: the S ranks of a tile form a thread-block cluster, combine
 // through distributed shared memory and run the stage epilogue in the same
 // launch.  CL = false: plain blocks; each writes its partial sums to global
 // memory and stage_finish (below) completes the stage.
-// Occupancy: with two i slots per lane the kernel fits 64 registers without
-// spills, so 32 warps per SM are resident (more latency hidden in the sparse
-// phases, where a block is short and bound by dependent loads and barriers);
-// four slots need more registers and stay at 24 warps.
+// Occupancy: with two i slots per lane the kernel is bounded to 64
+// registers, so 32 warps per SM are resident (more latency hidden in the
+// sparse phases, where a block is short and bound by dependent loads and
+// barriers); four slots need more registers and stay at 24 warps.
 template <int NW, int ILP>
 constexpr int fp32c_min_blocks() {
     return (ILP <= 2 ? 32 : 24) / NW > 0 ? (ILP <= 2 ? 32 : 24) / NW : 1;
@@ -597,7 +614,7 @@ constexpr int fp32c_min_blocks() {
 
 template <int NW, int ILP, int TC, bool CL, bool CULL = false>
 __global__ void __launch_bounds__(NW * 32, fp32c_min_blocks<NW, ILP>())
-    pair_stage_fp32c(const StageParams P, const ExpConsts E) {
+    pair_stage_fp32c(const StageParams P) {
     pdl_wait();
     constexpr int TILE = 32 * ILP;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -606,7 +623,7 @@ __global__ void __launch_bounds__(NW * 32, fp32c_min_blocks<NW, ILP>())
     const int tile = blockIdx.x / S;
     const int tid = threadIdx.x;
     const int n = P.c.n, n_pad = P.c.n_pad;
-    fp32c_sweep<NW, ILP, TC, CULL>(P, E, tile, rank, S, smem_raw);
+    fp32c_sweep<NW, ILP, TC, CULL>(P, tile, rank, S, smem_raw);
     float4 *s_red = reinterpret_cast<float4 *>(smem_raw) + Fp32cSmem<NW, ILP, TC>::red_offset;
     if constexpr (!CL) {
         for (int e = tid; e < TILE; e += NW * 32)
@@ -628,7 +645,8 @@ __global__ void __launch_bounds__(NW * 32, fp32c_min_blocks<NW, ILP>())
                     fx += (double)v.x - (double)v.z;
                     fy += (double)v.y - (double)v.w;
                 }
-                stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
+                const double cq = pair_scale(P, i);
+                stage_epilogue(P, i, __dmul_rn(cq, fx), __dmul_rn(cq, fy), stage_thermal(P, i));
             }
         }
         stage_step_advance(P);
@@ -711,8 +729,10 @@ static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
             cx += v.z;
             cy += v.w;
         }
-        const double fx = (double)sx.hi + ((double)sx.lo - (double)cx);
-        const double fy = (double)sy.hi + ((double)sy.lo - (double)cy);
+        // the sums leave out C q_i (pair_scale), applied here in FP64
+        const double cq = pair_scale(P, i);
+        const double fx = __dmul_rn(cq, (double)sx.hi + ((double)sx.lo - (double)cx));
+        const double fy = __dmul_rn(cq, (double)sy.hi + ((double)sy.lo - (double)cy));
         stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
     }
     if (P.box_out) {  // a warp is one 32-particle group: its box in the buffer just written
