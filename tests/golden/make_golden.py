@@ -26,6 +26,7 @@ Q = W.Q_DUST
 M = W.M_DUST
 
 OTHER_FORCES = W.OTHER_FORCES
+THERMAL_HEAT = 1e-14  # ThermalForce heatVal of the kick fixture [N]
 # ForceFlag bits of the forces the fixtures exercise one at a time (Force.h:75-91)
 EACH_FORCE = {"gravitational": 8, "driving": 64, "rotational": 128, "tv_drag": 256,
               "magnetic": 1024, "void": 2048, "electric": 4096, "vert_electric": 16384}
@@ -121,14 +122,16 @@ def main():
                                             t0=np.float64(0.1), end=np.float64(0.1 + 5e-4),
                                             flags=np.int64(flags), steps=np.int64(steps), t1=np.float64(t1),
                                             x1=rx, y1=ry, vx1=rvx, vy1=rvy)
-    # 8. the two other thermal forces' kicks from the reference itself (its
-    # RandomNumbers is clock-seeded, so only their distribution is pinned)
+    # 8. the three thermal forces' kicks from the reference itself (its
+    # RandomNumbers is clock-seeded, so only their distribution is pinned):
+    # ThermalForce (heatVal THERMAL_HEAT, ThermalForce.cpp:118-122),
+    # ThermalForceLocalized and TimeVaryingThermalForce
     x, y, vx, vy = disk(4096, 2e-2, 50)
     q = np.full(4096, Q)
     m = np.full(4096, M)
-    d = dict(x=x, y=y)
-    for name, flags, tt in [("localized", 32, 0.0), ("tv", 512, 0.5)]:
-        p = oracle.make_params(flags=flags, **OTHER_FORCES)
+    d = dict(x=x, y=y, thermal_heat=np.float64(THERMAL_HEAT))
+    for name, flags, tt in [("thermal", 16, 0.0), ("localized", 32, 0.0), ("tv", 512, 0.5)]:
+        p = oracle.make_params(flags=flags, heat=THERMAL_HEAT, **OTHER_FORCES)
         d[name + "_fx"], d[name + "_fy"] = ref.forces(x, y, vx, vy, q, m, p, t=tt, thermal=True)
         d[name + "_t"] = np.float64(tt)
     out["thermal_other_ref"] = d

@@ -246,22 +246,26 @@ def _kick_stats(fx, fy, scale):
     return u, np.arctan2(fy, fx)
 
 
-@pytest.mark.parametrize("kind", ["localized", "tv"])
-def test_other_thermal_kicks_match_reference_distribution(oracle_lib, kind):
-    """ThermalForceLocalized / TimeVaryingThermalForce: the reference's kicks
+@pytest.mark.parametrize("kind", ["thermal", "localized", "tv"])
+def test_thermal_kicks_match_reference_distribution(oracle_lib, kind):
+    """ThermalForce (heatVal*U*(cos t, sin t), ThermalForce.cpp:118-122),
+    ThermalForceLocalized and TimeVaryingThermalForce: the reference's kicks
     (clock-seeded) and the oracle's counter-based kicks have the same scale
     per region / time and the same magnitude and angle distributions."""
     from scipy import stats
 
     g = load("thermal_other_ref")
     n = len(g["x"])
-    flags = 32 if kind == "localized" else 512
+    flags = {"thermal": 16, "localized": 32, "tv": 512}[kind]
     t = float(g[kind + "_t"])
-    p = oracle.make_params(flags=flags, thermal_mode=0, seed=11, **OTHER_FORCES)
+    heat = float(g["thermal_heat"])
+    p = oracle.make_params(flags=flags, heat=heat, thermal_mode=0, seed=11, **OTHER_FORCES)
     zeros = np.zeros(n)
     fx, fy = oracle_lib.forces(g["x"], g["y"], zeros, zeros, np.full(n, W.Q_DUST), np.full(n, W.M_DUST),
                                p, step=3, stage=2, t=t)
-    if kind == "localized":
+    if kind == "thermal":
+        scale = np.full(n, heat)
+    elif kind == "localized":
         inside = np.hypot(g["x"], g["y"]) < OTHER_FORCES["heat_radius"]
         scale = np.where(inside, OTHER_FORCES["heat_in"], OTHER_FORCES["heat_out"])
     else:
