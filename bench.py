@@ -571,13 +571,17 @@ def run_gb300(args, world, rank, local):
     # adjoint backward (FP32C pair arithmetic; FP64 targets built untimed)
     adjoint = None
     if args.adjoint_grads > 0:
-        from demon_simulation_code_gb300.fit import TrajectoryFit
+        from demon_simulation_code_gb300.fit import ShardedTrajectoryFit, TrajectoryFit
 
         wa = W.adjoint64_smooth()
-        fit = TrajectoryFit(wa, precision="fp32c")
+        # N > 1: whole clouds per rank, per-cloud gradients met in all-reduces
+        fit = (ShardedTrajectoryFit(wa, precision="fp32c") if world > 1
+               else TrajectoryFit(wa, precision="fp32c"))
+        local = fit.local if world > 1 else fit
         fit.loss_and_grad()  # warm-up
         torch.cuda.synchronize()
-        al0 = fit.K.ctx.launch_count()
+        barrier()
+        al0 = local.K.ctx.launch_count()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         t_a = time.perf_counter()
@@ -586,17 +590,18 @@ def run_gb300(args, world, rank, local):
             L, _ = fit.loss_and_grad()
         b.record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t_a
-        el = a.elapsed_time(b) / 1e3
-        sweeps = (fit.K.ctx.launch_count() - al0) / args.adjoint_grads  # force + VJP launches per gradient
-        adjoint = {"workload": wa.name, "clouds": len(fit.ns), "n": fit.ns[0], "steps": fit.steps,
-                   "checkpoint_every": fit.every, "precision": "fp32c",
+        wall = max_over_ranks(time.perf_counter() - t_a)
+        el = max_over_ranks(a.elapsed_time(b) / 1e3)
+        sweeps = (local.K.ctx.launch_count() - al0) / args.adjoint_grads  # force + VJP launches per gradient
+        adjoint = {"workload": wa.name, "clouds": len(wa.clouds), "n": wa.clouds[0].n, "steps": local.steps,
+                   "checkpoint_every": local.every, "precision": "fp32c",
                    "seconds_per_gradient": el / args.adjoint_grads,
                    "wall_seconds_per_gradient": wall / args.adjoint_grads,
                    "pair_sweeps_per_gradient": sweeps,
-                   "value": sweeps * fit.pairs_per_eval * args.adjoint_grads / el, "unit": UNIT,
-                   "loss": float(L.item()), "gradients": "kappa, q, k_c per cloud; initial positions"}
-        del fit
+                   "value": sweeps * sum(c.n * (c.n - 1) for c in wa.clouds) * args.adjoint_grads / el,
+                   "unit": UNIT, "loss": float(L), "ranks": world,
+                   "gradients": "kappa, q, k_c per cloud; initial positions"}
+        del fit, local
 
     # CPU legs (rank 0, N = 1 host): the oracle on the window's own states
     cpu = cpu1 = None

@@ -21,11 +21,27 @@ import torch
 from .adjoint import AdjointKernels, rollout
 
 
+def start_factors(nclouds: int, perturb: float, seed: int) -> np.ndarray:
+    """[nclouds, 3] seeded factors of (kappa, q, k_c) for the fit's start:
+    row c is cloud c's, so the first k clouds of a workload start where they
+    would in a k-cloud workload, and a shard of clouds starts where those
+    clouds do in the whole workload."""
+    rng = np.random.default_rng(seed)
+    return 1.0 + rng.uniform(-perturb, perturb, (nclouds, 3))
+
+
 class TrajectoryFit:
+    """The fit over `workload`'s clouds, or over the clouds `cloud_ids` of it
+    (a shard: start factors as in the whole workload, losses divided by
+    `norm` particles, by default this fit's own particle count)."""
+
     def __init__(self, workload, perturb: float | None = None, seed: int = 4, device=None,
-                 precision: str = "fp64"):
-        clouds = workload.clouds
+                 precision: str = "fp64", cloud_ids=None, norm: int | None = None):
+        ids = list(range(len(workload.clouds))) if cloud_ids is None else [int(i) for i in cloud_ids]
+        clouds = [workload.clouds[i] for i in ids]
+        self.cloud_ids = ids
         self.ns = [c.n for c in clouds]
+        self.norm = sum(self.ns) if norm is None else int(norm)
         self.dt = float(workload.dt)
         self.steps = int(workload.steps)
         self.every = int(workload.extra.get("checkpoint_every", 20))
@@ -55,8 +71,7 @@ class TrajectoryFit:
         self.K64 = K64
         # row c = cloud c's factors for (kappa, q, k_c): the first k clouds of
         # a workload start where they would in a k-cloud workload
-        rng = np.random.default_rng(seed)
-        f = torch.tensor(1.0 + rng.uniform(-perturb, perturb, (len(self.ns), 3)), dtype=torch.float64,
+        f = torch.tensor(start_factors(len(workload.clouds), perturb, seed)[ids], dtype=torch.float64,
                          device=dev)
         self.start = {k: self.true[k] * f[:, col] for col, k in enumerate(("kappa", "q", "kc"))}
 
@@ -76,7 +91,7 @@ class TrajectoryFit:
         """[nclouds] tensor of L_c (their sum is the loss)."""
         xT, yT, _, _ = self._rollout(self.x0 if x0 is None else x0, kappa, q, kc, K)
         e = (xT - self.xt) ** 2 + (yT - self.yt) ** 2
-        return self.K.per_cloud(e) / self.total
+        return self.K.per_cloud(e) / self.norm
 
     def loss(self, kappa, q, kc, x0=None):
         return self.per_cloud_loss(kappa, q, kc, x0).sum()
@@ -118,3 +133,49 @@ class TrajectoryFit:
         Lu = self.per_cloud_loss(**{**p, name: base + h}, K=K)
         Ld = self.per_cloud_loss(**{**p, name: base - h}, K=K)
         return (Lu - Ld) / (2 * h)
+
+
+class ShardedTrajectoryFit:
+    """The trajectory fit over the ranks of a torch.distributed group: whole
+    clouds per rank (shard.assign_clouds, balanced by N^2), each rank
+    differentiates its own clouds, and the results meet in one all-reduce
+    each -- the loss (a sum over clouds), the per-cloud (kappa, q, k_c)
+    gradients and the initial-position gradient (a segment per cloud).  No
+    data-path exchange: clouds never interact.  Every rank returns the full
+    results.
+
+    make_local(ids, norm) builds the fit of a shard (default: TrajectoryFit
+    on this rank's GPU); a rank that owns no cloud builds none."""
+
+    def __init__(self, workload, group=None, make_local=None, **kw):
+        import torch.distributed as dist
+
+        from .shard import assign_clouds
+
+        self.group = group
+        self.world = dist.get_world_size(group)
+        self.rank = dist.get_rank(group)
+        self.ns_all = [c.n for c in workload.clouds]
+        self.ids = assign_clouds(self.ns_all, self.world)[self.rank]
+        norm = sum(self.ns_all)
+        if make_local is None:
+            def make_local(ids, norm):
+                return TrajectoryFit(workload, cloud_ids=ids, norm=norm, **kw)
+        self.local = make_local(self.ids, norm) if self.ids else None
+
+    def loss_and_grad(self):
+        """(loss, {"kappa", "q", "kc": [nclouds], "x0": [N_total]}) as numpy,
+        identical on every rank."""
+        from .shard import gather_per_cloud, gather_segments, sum_scalar
+
+        if self.local is not None:
+            L, g = self.local.loss_and_grad()
+            L = float(L)
+            g = {k: np.asarray(v.detach().cpu().numpy() if hasattr(v, "detach") else v, dtype=np.float64)
+                 for k, v in g.items()}
+        else:
+            L, g = 0.0, {k: np.zeros(0) for k in ("kappa", "q", "kc", "x0")}
+        n = len(self.ns_all)
+        out = {k: gather_per_cloud(g[k], self.ids, n, group=self.group) for k in ("kappa", "q", "kc")}
+        out["x0"] = gather_segments(g["x0"], self.ids, self.ns_all, group=self.group)
+        return sum_scalar(L, group=self.group), out

@@ -59,6 +59,31 @@ def gather_per_cloud(values, ids, nclouds: int, width: int | None = None, group=
     return t.cpu().numpy()
 
 
+def gather_segments(values, ids, ns, group=None):
+    """Per-particle values of each rank's clouds (the concatenation of cloud
+    ids[0]'s ns[ids[0]] values, then ids[1]'s, ...) -> the [sum(ns)] array of
+    every cloud in cloud order, on every rank (one all_reduce of a buffer of
+    that size; each cloud belongs to exactly one rank)."""
+    import torch
+    import torch.distributed as dist
+
+    offs = np.concatenate([[0], np.cumsum(np.asarray(ns, dtype=np.int64))])
+    full = np.zeros(int(offs[-1]), dtype=np.float64)
+    values = np.asarray(values, dtype=np.float64).ravel()
+    k = 0
+    for c in ids:
+        m = int(ns[c])
+        full[offs[c]:offs[c] + m] = values[k:k + m]
+        k += m
+    if k != len(values):
+        raise ValueError("values do not match the clouds' sizes")
+    t = torch.from_numpy(full)
+    if dist.get_backend(group) == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return t.cpu().numpy()
+
+
 def sum_scalar(value: float, group=None) -> float:
     """Sum of one float over the ranks (e.g. the trajectory-fit loss)."""
     import torch

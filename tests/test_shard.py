@@ -98,3 +98,61 @@ def test_gloo_more_ranks_than_clouds(tmp_path):
     ref = np.array([o.diagnostics(c.x, c.y, c.vx, c.vy, c.q, c.m, oracle.make_params(**c.params()))
                     for c in clouds])
     assert np.array_equal(outs[0][:-1].reshape(2, 5), ref)
+
+
+class _CpuFit:
+    """A CPU stand-in for the device part of a shard's trajectory fit (same
+    interface as fit.TrajectoryFit.loss_and_grad): deterministic per-cloud
+    values computed from the clouds, so the sharded result can be checked
+    exactly against one process."""
+
+    def __init__(self, workload, ids, norm):
+        self.clouds = [workload.clouds[i] for i in ids]
+        self.ids = list(ids)
+        self.norm = norm
+
+    def loss_and_grad(self):
+        L = sum(float(np.sum(c.x ** 2 + c.y ** 2)) for c in self.clouds) / self.norm
+        g = {"kappa": np.array([float(np.sum(c.x)) * c.shielding for c in self.clouds]),
+             "q": np.array([float(c.n) + i for c, i in zip(self.clouds, self.ids)]),
+             "kc": np.array([c.confine for c in self.clouds]),
+             "x0": np.concatenate([2.0 * c.x / self.norm for c in self.clouds])}
+        return L, g
+
+
+def _fit_worker(rank, world, port, out_dir, nclouds):
+    import torch.distributed as dist
+
+    from demon_simulation_code_gb300.fit import ShardedTrajectoryFit
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        w = W.batch256(nclouds=nclouds, nmin=16, nmax=128)
+        fit = ShardedTrajectoryFit(w, make_local=lambda ids, norm: _CpuFit(w, ids, norm))
+        L, g = fit.loss_and_grad()
+        np.save(os.path.join(out_dir, f"fit{rank}.npy"),
+                np.concatenate([[L], g["kappa"], g["q"], g["kc"], g["x0"]]))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world,nclouds", [(2, 12), (3, 2)])
+def test_gloo_sharded_trajectory_fit_equals_one_process(tmp_path, world, nclouds):
+    """The trajectory fit's sharding logic end to end on CPU ranks (gloo):
+    clouds dealt by assign_clouds, the shard fits built with the whole
+    workload's particle count, the loss summed and the per-cloud and
+    per-particle gradients gathered -- equal to one process over all clouds,
+    also with a rank that owns no cloud."""
+    import torch.multiprocessing as mp
+
+    mp.spawn(_fit_worker, args=(world, _free_port(), str(tmp_path), nclouds), nprocs=world, join=True)
+    outs = [np.load(tmp_path / f"fit{r}.npy") for r in range(world)]
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+    w = W.batch256(nclouds=nclouds, nmin=16, nmax=128)
+    norm = sum(c.n for c in w.clouds)
+    L, g = _CpuFit(w, range(nclouds), norm).loss_and_grad()
+    ref = np.concatenate([[L], g["kappa"], g["q"], g["kc"], g["x0"]])
+    assert abs(outs[0][0] - ref[0]) <= 1e-14 * abs(ref[0])
+    assert np.array_equal(outs[0][1:], ref[1:])
