@@ -829,7 +829,8 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->sort_blocks = (n + kSortPerBlock - 1) / kSortPerBlock;
     const size_t nh = align256((size_t)kSortBuckets * c->sort_blocks * sizeof(uint32_t));
     const size_t ngb = align256((size_t)(c->n_pad / 32) * sizeof(float4));
-    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ngb * 2 + ni * 6 + nh + 1024 + 512 +
+    const size_t ngm = align256((size_t)(c->n_pad / 32) * sizeof(uint32_t));
+    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ngb * 2 + ngm * 2 + ni * 6 + nh + 1024 + 512 +
                          align256(sizeof(double) * kMomentBlocks * kMomentFields);
     cudaError_t e = cudaMalloc(&c->block, total);
     if (e != cudaSuccess) {
@@ -851,6 +852,7 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->d_fy = takeD();
     for (int b = 0; b < 2; b++) { c->d.pa[b] = takeF4(); c->d.pb[b] = takeF4(); }
     for (int b = 0; b < 2; b++) { c->d.gbox[b] = (float4 *)p; p += ngb; }
+    for (int b = 0; b < 2; b++) { c->d.gmask[b] = (uint32_t *)p; p += ngm; }
     c->d.eval_pairs = (unsigned long long *)p; p += 256;
     c->d.step_ctr = (unsigned long long *)p; p += 256;
     c->d.time = (double *)(c->d.step_ctr + 4);  // same 256-byte slot, bytes 32-47
@@ -867,6 +869,7 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     for (int k = 0; k < 6; k++) c->sort.stage[k] = takeD();
     c->sort.hist = (uint32_t *)p; p += nh;
     c->sort.box = (double *)p; p += 256;
+    c->d.keybox = c->sort.box;
     c->sort.moments = (double *)p; p += align256(sizeof(double) * kMomentBlocks * kMomentFields);
     cudaStream_t s = ctx->stream;
     const size_t bytes = (size_t)n * sizeof(double);
@@ -1375,7 +1378,8 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf =
     if (k.cull) {  // group boxes of the buffer this stage reads
         const int br = (mode == kModeForceOnly) ? fo_buf : (stage - 1) & 1;
         DM_CUDA(ctx, launch_pdl(batch_group_bounds, dim3((B->ngroups * 32 + 255) / 256), dim3(256), 0, ctx->stream,
-                                B->d, (const BatchCloud *)B->ddesc, (const int *)B->dgseg, B->ngroups, br));
+                                B->d, (const BatchCloud *)B->ddesc, (const int *)B->dgseg, B->ngroups, br,
+                                (const double *)B->dbox));
         ctx->launches++;
     }
     DM_CUDA(ctx, k.launch(dim3(B->grid[B->variant]), dim3(k.nt), k.smem, ctx->stream, P, B->ddesc,
@@ -1622,6 +1626,9 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     for (int b = 0; b < 2 && e == cudaSuccess; b++) {
         e = cudaMalloc((void **)&d.gbox[b], (size_t)B->ngroups * sizeof(float4));
         if (e == cudaSuccess) B->extra.push_back(d.gbox[b]);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&d.gmask[b], (size_t)B->ngroups * sizeof(uint32_t));
+        if (e == cudaSuccess) B->extra.push_back(d.gmask[b]);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d.gmask[b], 0, (size_t)B->ngroups * sizeof(uint32_t), s);
     }
     if (e == cudaSuccess) e = cudaMalloc((void **)&B->dgseg, gseg.size() * sizeof(int));
     if (e == cudaSuccess) B->extra.push_back(B->dgseg);

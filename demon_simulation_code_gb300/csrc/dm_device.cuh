@@ -65,7 +65,10 @@ struct CloudDev {
     double *a23[4];
     double *px[2], *py[2];
     float4 *pa[2], *pb[2];
-    float4 *gbox[2];               // [n_pad/32] FP32 box (x0, y0, x1, y1) of each 32-particle group
+    float4 *gbox[2];               // [n_pad/32] FP32 box (x0, y0, x1, y1) of each 32-particle group's
+                                   // members, its outliers left out (write_group_box)
+    uint32_t *gmask[2];            // [n_pad/32] each group's outlier members (bit = lane)
+    const double *keybox;          // the cloud's Morton key box (x0, y0, extent) of the last re-sort
     unsigned long long *eval_pairs;  // ordered pairs the culling kernels swept (cumulative)
     unsigned long long *step_ctr;  // [2], see stage_step_index()
     double *time;                  // [2] force time slots, see stage_time()
@@ -315,6 +318,91 @@ __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, i
     c.pa[b][i] = make_float4(xh, yh, fmaf(yh, yh, xh * xh), __double2float_rn(q));
     c.pb[b][i] = make_float4(xl, yl, -filter_threshold(xh, yh, c.rc2),
                              __double2float_rn(c.coulomb * q));
+}
+
+// ---------------------------------------------------------------------------
+// Group boxes for the culling kernels, outliers kept out of them.
+//
+// A 32-particle group is consecutive in Morton order, so its members are
+// normally close together.  But a particle can be thrown far from the cloud
+// within one RK4 substep (a close pair at a large dt), and one such member
+// stretches its group's box -- and its tile's -- across the cloud: every
+// tile then sweeps that group, and that tile every group.  So when a group's
+// box is wider than the fat threshold, the members farther than half the
+// threshold from the group's median (per axis) are its outliers: the box
+// covers the other members only, and the outliers are flagged in the group's
+// 32-bit mask, for the culling test to check their positions one by one.
+// Non-finite positions are outliers too.  Any split into box and outliers
+// is correct (the culling test covers both); the threshold only decides how
+// much work is done.
+// ---------------------------------------------------------------------------
+
+// Fat threshold of a cloud of n particles whose key box has the given
+// extent: 16 cutoff radii, or 8x the width of a group at the key box's mean
+// density, whichever is larger.
+__device__ __forceinline__ float group_fat_threshold(double rc2, double extent, int n) {
+    const float by_rc = 16.0f * sqrtf((float)rc2);
+    const float by_density = 8.0f * (float)extent * sqrtf(32.0f / (float)max(n, 1));
+    return (by_density > by_rc && isfinite(by_density)) ? by_density : by_rc;
+}
+__device__ __forceinline__ float group_fat_threshold(const CloudDev &c) {
+    return group_fat_threshold(c.rc2, c.keybox ? c.keybox[2] : 0.0, c.n);
+}
+
+// Median of the first k values of the warp (the other lanes pass +inf):
+// bitonic sort across the lanes, then element (k-1)/2.
+__device__ __forceinline__ float warp_median(float v, int k) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int w = 2; w <= 32; w <<= 1) {
+#pragma unroll
+        for (int j = w >> 1; j > 0; j >>= 1) {
+            const float o = __shfl_xor_sync(0xffffffffu, v, j);
+            const bool up = (lane & w) == 0, low = (lane & j) == 0;
+            v = (low == up) ? fminf(v, o) : fmaxf(v, o);
+        }
+    }
+    return __shfl_sync(0xffffffffu, v, (k - 1) >> 1);
+}
+
+__device__ __forceinline__ void warp_box(float &x0, float &y0, float &x1, float &y1) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+}
+
+// Box and outlier mask of group g: every lane of the warp calls it, (x, y)
+// its member's FP32 position (hi parts), valid = the lane holds a member.
+// A group with no member in its box gets the empty box (+inf, +inf, -inf,
+// -inf).
+__device__ __forceinline__ void write_group_box(float4 *gbox, uint32_t *gmask, int g, float thr, float x,
+                                                float y, bool valid) {
+    const bool fin = valid && isfinite(x) && isfinite(y);
+    float x0 = fin ? x : INFINITY, y0 = fin ? y : INFINITY, x1 = fin ? x : -INFINITY, y1 = fin ? y : -INFINITY;
+    warp_box(x0, y0, x1, y1);
+    uint32_t mask = __ballot_sync(0xffffffffu, valid && !fin);
+    if (fmaxf(x1 - x0, y1 - y0) > thr) {  // warp-uniform: every lane holds the reduced box
+        const int nf = __popc(__ballot_sync(0xffffffffu, fin));
+        const float mx = warp_median(fin ? x : INFINITY, nf);
+        const float my = warp_median(fin ? y : INFINITY, nf);
+        const float h = 0.5f * thr;
+        const bool out = fin && (fabsf(x - mx) > h || fabsf(y - my) > h);
+        mask |= __ballot_sync(0xffffffffu, out);
+        const bool core = fin && !out;
+        x0 = core ? x : INFINITY;
+        y0 = core ? y : INFINITY;
+        x1 = core ? x : -INFINITY;
+        y1 = core ? y : -INFINITY;
+        warp_box(x0, y0, x1, y1);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        gbox[g] = make_float4(x0, y0, x1, y1);
+        gmask[g] = mask;
+    }
 }
 
 // Reference cutoff decision for one pair, bit for bit:
