@@ -592,12 +592,15 @@ def run_gb300(args, world, rank, local):
         torch.cuda.synchronize()
         wall = max_over_ranks(time.perf_counter() - t_a)
         el = max_over_ranks(a.elapsed_time(b) / 1e3)
-        sweeps = (local.K.ctx.launch_count() - al0) / args.adjoint_grads  # force + VJP launches per gradient
+        kernels = (local.K.ctx.launch_count() - al0) / args.adjoint_grads
+        # pair sweeps per gradient: 4 force sweeps per step forward, 4 per
+        # recomputed step and 4 VJP sweeps per step backward
+        sweeps = 12 * local.steps
         adjoint = {"workload": wa.name, "clouds": len(wa.clouds), "n": wa.clouds[0].n, "steps": local.steps,
                    "checkpoint_every": local.every, "precision": "fp32c",
                    "seconds_per_gradient": el / args.adjoint_grads,
                    "wall_seconds_per_gradient": wall / args.adjoint_grads,
-                   "pair_sweeps_per_gradient": sweeps,
+                   "pair_sweeps_per_gradient": sweeps, "kernels_per_gradient": kernels,
                    "value": sweeps * sum(c.n * (c.n - 1) for c in wa.clouds) * args.adjoint_grads / el,
                    "unit": UNIT, "loss": float(L), "ranks": world,
                    "gradients": "kappa, q, k_c per cloud; initial positions"}

@@ -151,6 +151,9 @@ SIGNATURES = {
     "dm_adjoint_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForceParams)]),
     "dm_adjoint_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 10),
     "dm_adjoint_vjp": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 15),
+    "dm_adjoint_rk4_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double] + [ctypes.c_void_p] * 7),
+    "dm_adjoint_rk4_step_vjp": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+                                + [ctypes.c_void_p] * 10),
     "dm_diagnostics_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.POINTER(ForceParams),

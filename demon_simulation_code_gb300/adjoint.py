@@ -1,12 +1,16 @@
 """Differentiable RK4 rollout: a hand-written discrete adjoint behind
 ``torch.autograd.Function``.
 
-The O(N^2) work -- forces and their vector-Jacobian product -- runs in the
-CUDA kernels of libdemon_gb300.so (FP64, or FP32 pair terms with Kahan sums) (``dm_adjoint_forces`` /
-``dm_adjoint_vjp`` on the tensors' device memory); the O(N) RK4 stage
-bookkeeping is FP64 tensor arithmetic on the same stream.  The forward pass
-keeps the state every ``checkpoint_every`` steps; the backward pass
-recomputes each segment from its checkpoint and walks it in reverse.
+All O(N^2) work and the RK4 bookkeeping run in the CUDA kernels of
+libdemon_gb300.so on the tensors' device memory: one fused launch per RK4
+stage forward (pair force, per-particle forces and stage algebra,
+``dm_adjoint_rk4_step``) and one per stage backward (force VJP and the
+adjoint recurrences, ``dm_adjoint_rk4_step_vjp``), FP64 or FP32 pair terms
+with Kahan sums.  The forward pass keeps the state every
+``checkpoint_every`` steps; the backward pass recomputes each segment from
+its checkpoint, keeping the four stage inputs of every step of the segment,
+and walks the segment in reverse from them -- four force sweeps and four
+VJP sweeps per step on the way back, four force sweeps forward.
 
 RK4 step (the reference's Runge_Kutta4.cpp:23-137, written for s = (x, y,
 vx, vy) and f(s) = (vx, vy, Fx/m, Fy/m)):
@@ -112,62 +116,21 @@ class AdjointKernels:
     def per_cloud(self, v):
         return torch.zeros(self.nclouds, dtype=v.dtype, device=v.device).index_add_(0, self.seg, v)
 
+    def rk4_step(self, s, q, m, dt, stages=None):
+        """One fused RK4 step of the state s = (x, y, vx, vy), in place;
+        stages: None or a [16, total] FP64 tensor that receives the four
+        stage inputs."""
+        self._bind_stream()
+        check(self.lib.dm_adjoint_rk4_step(self.h, self.precision, float(dt), *(_p(t) for t in s), _p(q), _p(m),
+                                           _p(stages) if stages is not None else None), self.ctx.h)
 
-def _f(K, s, q, m):
-    x, y, vx, vy = s
-    fx, fy = K.forces(x, y, vx, vy, q, m)
-    return (vx, vy, fx / m, fy / m)
-
-
-def _axpy(s, k, a):
-    return tuple(si + a * ki for si, ki in zip(s, k))
-
-
-def rk4_step(K, s, q, m, dt, stages=False):
-    k1 = tuple(dt * v for v in _f(K, s, q, m))
-    s2 = _axpy(s, k1, 0.5)
-    k2 = tuple(dt * v for v in _f(K, s2, q, m))
-    s3 = _axpy(s, k2, 0.5)
-    k3 = tuple(dt * v for v in _f(K, s3, q, m))
-    s4 = _axpy(s, k3, 1.0)
-    k4 = tuple(dt * v for v in _f(K, s4, q, m))
-    out = tuple(si + (a + ((b + c) * 2.0 + d)) / 6.0 for si, a, b, c, d in zip(s, k1, k2, k3, k4))
-    return (out, (s, s2, s3, s4)) if stages else out
-
-
-def _vjp_f(K, s, q, m, w):
-    """J(s)^T w and the parameter gradients for f(s) = (vx, vy, F/m)."""
-    x, y, vx, vy = s
-    ax, ay = w[2] / m, w[3] / m
-    gx, gy, gvx, gvy, gq, gk, gc = K.vjp(x, y, vx, vy, q, m, ax.contiguous(), ay.contiguous())
-    return (gx, gy, w[0] + gvx, w[1] + gvy), gq, gk, gc
-
-
-def rk4_step_vjp(K, s, q, m, dt, lam):
-    _, (s1, s2, s3, s4) = rk4_step(K, s, q, m, dt, stages=True)
-    gq = torch.zeros_like(q)
-    gk = torch.zeros_like(q)
-    gc = torch.zeros_like(q)
-    sixth = [v / 6.0 for v in lam]
-    third = [v / 3.0 for v in lam]
-
-    def stage(si, dk):
-        mu, a, b, c = _vjp_f(K, si, q, m, [dt * v for v in dk])
-        return mu, a, b, c
-
-    mu4, a, b, c = stage(s4, sixth)
-    gq += a; gk += b; gc += c
-    dk3 = [t + u for t, u in zip(third, mu4)]
-    mu3, a, b, c = stage(s3, dk3)
-    gq += a; gk += b; gc += c
-    dk2 = [t + 0.5 * u for t, u in zip(third, mu3)]
-    mu2, a, b, c = stage(s2, dk2)
-    gq += a; gk += b; gc += c
-    dk1 = [t + 0.5 * u for t, u in zip(sixth, mu2)]
-    mu1, a, b, c = stage(s1, dk1)
-    gq += a; gk += b; gc += c
-    lam_prev = tuple(l + u1 + u2 + u3 + u4 for l, u1, u2, u3, u4 in zip(lam, mu1, mu2, mu3, mu4))
-    return lam_prev, gq, gk, gc
+    def rk4_step_vjp(self, stages, q, m, dt, lam, gq, gk, gc):
+        """The adjoint of one step from its stage inputs: lam (4 tensors)
+        from dL/d(output) to dL/d(input) in place; the parameter gradients
+        per particle added to gq, gk (kappa), gc (k_c)."""
+        self._bind_stream()
+        check(self.lib.dm_adjoint_rk4_step_vjp(self.h, self.precision, float(dt), _p(stages), _p(q), _p(m),
+                                               *(_p(t) for t in lam), _p(gq), _p(gk), _p(gc)), self.ctx.h)
 
 
 class Rollout(torch.autograd.Function):
@@ -182,16 +145,16 @@ class Rollout(torch.autograd.Function):
         K, m, dt, nsteps, every = meta["kernels"], meta["m"], meta["dt"], meta["steps"], meta["every"]
         K.set_params(kappa.detach().cpu().numpy(), kc.detach().cpu().numpy())
         q = qc.detach()[K.seg].contiguous()
-        s = tuple(t.detach().contiguous() for t in (x0, y0, vx0, vy0))
+        s = tuple(t.detach().clone().contiguous() for t in (x0, y0, vx0, vy0))
         ckpts = []
         for t in range(nsteps):
             if t % every == 0:
-                ckpts.append(s)
-            s = rk4_step(K, s, q, m, dt)
+                ckpts.append(tuple(v.clone() for v in s))
+            K.rk4_step(s, q, m, dt)
         ctx.meta = meta
         ctx.ckpts = ckpts
         ctx.save_for_backward(kappa, qc, kc)
-        return tuple(v.clone() for v in s)
+        return s
 
     @staticmethod
     def backward(ctx, gx, gy, gvx, gvy):
@@ -201,21 +164,19 @@ class Rollout(torch.autograd.Function):
         K.set_params(kappa.detach().cpu().numpy(), kc.detach().cpu().numpy())
         q = qc.detach()[K.seg].contiguous()
         ref = ctx.ckpts[0][0]
-        lam = tuple(g.contiguous() if g is not None else torch.zeros_like(ref) for g in (gx, gy, gvx, gvy))
+        lam = tuple(g.clone().contiguous() if g is not None else torch.zeros_like(ref) for g in (gx, gy, gvx, gvy))
         gq = torch.zeros_like(q)
         gk = torch.zeros_like(q)
         gc = torch.zeros_like(q)
+        store = torch.empty((min(every, nsteps), 16, ref.numel()), dtype=torch.float64, device=ref.device)
         for ci in range(len(ctx.ckpts) - 1, -1, -1):
             t0 = ci * every
             t1 = min(nsteps, t0 + every)
-            states = [ctx.ckpts[ci]]
-            for _ in range(t0, t1 - 1):  # recompute the segment
-                states.append(rk4_step(K, states[-1], q, m, dt))
-            for s in reversed(states):
-                lam, a, b, c = rk4_step_vjp(K, s, q, m, dt, lam)
-                gq += a
-                gk += b
-                gc += c
+            s = tuple(v.clone() for v in ctx.ckpts[ci])
+            for t in range(t0, t1):  # recompute the segment, keeping every stage input
+                K.rk4_step(s, q, m, dt, stages=store[t - t0])
+            for t in range(t1 - 1, t0 - 1, -1):
+                K.rk4_step_vjp(store[t - t0], q, m, dt, lam, gq, gk, gc)
         return (lam[0], lam[1], lam[2], lam[3], K.per_cloud(gk), K.per_cloud(gq), K.per_cloud(gc), None)
 
 

@@ -33,6 +33,7 @@ struct AdjCloud {
     float rc2_lo, rc2_hi;  // FP32 certain-in / certain-out bounds on r^2
     float kappa_f, kappa2_f;
     float kl2e_hi, kl2e_lo;  // kappa*log2(e) as a float pair (SFU exponential)
+    float nkl2e;             // -kappa*log2(e): e^{-kappa r} = 2^{nkl2e r} (packed pair terms)
 };
 
 constexpr int kAdjThreads = 128;
@@ -269,6 +270,358 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(
         o4[i] = gq;          // dL/dq_i
         o5[i] = S.v[3];      // dL/dkappa contribution of particle i
         o6[i] = gkc;         // dL/dk_c contribution of particle i
+    }
+}
+
+
+// ===========================================================================
+// Fused RK4 step and its adjoint for the differentiable rollout.
+//
+// One launch per RK4 stage.  Forward (adj_step_forces): the pair force at
+// the stage's input state, the per-particle forces, and the stage algebra
+// of the rollout's RK4 step in FP64 (for s = (x, y, vx, vy) and f(s) =
+// (vx, vy, Fx/m, Fy/m)):
+//     k_s = dt f(s_s),  s_2 = S + k_1/2, s_3 = S + k_2/2, s_4 = S + k_3,
+//     S' = S + (k_1 + ((k_2 + k_3) 2 + k_4)) / 6,
+// with the operations in that order (each rounded, nothing contracted).
+// Backward (adj_step_vjp, stages 4, 3, 2, 1): given lam = dL/dS', the stage
+// weights dk_4 = lam/6, dk_3 = lam/3 + mu_4, dk_2 = lam/3 + mu_3/2,
+// dk_1 = lam/6 + mu_2/2 with mu_s = J(s_s)^T (dt dk_s), and finally
+// dL/dS = lam + mu_1 + mu_2 + mu_3 + mu_4; the parameter gradients
+// (dt dk_s)^T df/dtheta are added into per-particle accumulators.  J^T w
+// for f is (the force VJP of a = w_v / m) for positions, w_p - gamma w_v
+// for velocities.
+//
+// FP32C pair terms: one i per thread, j staged in shared memory as negated
+// two-float positions (plus charge and, backward, the j's force adjoint), two
+// j per packed f32x2 evaluation (pair2_terms), the cutoff by a select (pairs
+// within 4e-6 of it in r^2 decided by the reference's FP64 test on the FP64
+// positions), plain sums over four j, then Kahan; C q_i applied in FP64 per
+// particle.  FP64: adj_tile_fp64.
+// ===========================================================================
+
+constexpr int kAsJ = 256;  // j staged per tile (a multiple of 4)
+
+struct AdjStepIO {
+    const double *x, *y, *vx, *vy;  // the stage's input state s_s
+    double *sx, *sy, *svx, *svy;    // the step's base state S (stage 4 writes S' over it)
+    double *k1[4], *k23[4];         // k_1 and k_2 + k_3
+    double *nx, *ny, *nvx, *nvy;    // the next stage's input (stages 1-3)
+    const double *q, *m;
+    double dt;
+    int stage;
+};
+
+struct AdjVjpIO {
+    const double *x, *y, *vx, *vy;  // the stage's input state s_s
+    const double *dk[4];            // dk_s (stage 4: lam, divided by 6 here)
+    double *dkn[4];                 // dk_{s-1} (stages 4-2)
+    double *lam[4];                 // dL/dS' in, dL/dS out (stage 1)
+    double *mu[3][4];               // mu_4, mu_3, mu_2
+    double *gq, *gkappa, *gkc;      // per-particle parameter gradients (added to)
+    const double *q, *m;
+    double dt;
+    int stage;
+};
+
+// dk_s of particle k, component c.
+__device__ __forceinline__ double adj_dk(const AdjVjpIO &V, int c, int k) {
+    return V.stage == 4 ? __ddiv_rn(V.lam[c][k], 6.0) : V.dk[c][k];
+}
+
+// One pair term in FP32 for the slow path (pairs within 4e-6 of the cutoff
+// in r^2): 0 outside the cutoff (the reference's FP64 test decides).
+__device__ __forceinline__ bool adj_border_in(const AdjCloud &d, const double *x, const double *y, int i, int j) {
+    double r, a;
+    return ref_in_cutoff(__dsub_rn(x[i], x[j]), __dsub_rn(y[i], y[j]), d.kappa, r, a);
+}
+
+// FP32C pair sums of particle li of cloud d over the cloud's j, staged kAsJ
+// at a time.  MODE 0: out[0..1] = sum_j w_ij (dx, dy) (times C q_i: the pair
+// force).  MODE 1 (a_i, a_j the force adjoints): out[0..1] = sum w b + h d
+// (d . b), out[2] = sum w (d . b), out[3] = sum q_j e y (a_i . d)
+// (times C q_i: the position VJP, F_ij . (a_i - a_j) and, times -kappa,
+// dg/dkappa), with b = a_i - a_j.  Every thread of the block calls it.
+template <int MODE>
+__device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, bool valid, const double *x,
+                                                    const double *y, const double *q, const float *ajx,
+                                                    const float *ajy, float aix, float aiy, float (&out)[4]) {
+    __shared__ float s_nxh[kAsJ], s_nyh[kAsJ], s_nxl[kAsJ], s_nyl[kAsJ], s_q[kAsJ];
+    __shared__ float s_ax[MODE == 1 ? kAsJ : 1], s_ay[MODE == 1 ? kAsJ : 1];
+    constexpr int NS = MODE == 0 ? 2 : 4;
+    float sum[NS], cmp[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) sum[k] = cmp[k] = 0.0f;
+    const int i = d.off + (valid ? li : 0);
+    float xh = 0.0f, yh = 0.0f, xl = 0.0f, yl = 0.0f;
+    if (valid) split2(x[i], xh, xl), split2(y[i], yh, yl);
+    const PairI I{dup2(xh), dup2(yh), dup2(xl), dup2(yl)};
+    const float2 kap = dup2(d.kappa_f), nkl2e = dup2(d.nkl2e);
+    const float2 nk2 = dup2(-d.kappa2_f), m3 = dup2(-3.0f);
+    const float2 ax2 = dup2(aix), ay2 = dup2(aiy);
+    for (int j0 = 0; j0 < d.n; j0 += kAsJ) {
+        const int cnt = min(kAsJ, d.n - j0);
+        const int cnt4 = (cnt + 3) & ~3;
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt4; e += blockDim.x) {
+            if (e < cnt) {
+                const int j = d.off + j0 + e;
+                float h, l;
+                split2(x[j], h, l);
+                s_nxh[e] = -h;
+                s_nxl[e] = -l;
+                split2(y[j], h, l);
+                s_nyh[e] = -h;
+                s_nyl[e] = -l;
+                s_q[e] = (float)q[j];
+                if (MODE == 1) {
+                    s_ax[e] = ajx[j];
+                    s_ay[e] = ajy[j];
+                }
+            } else {  // padding: far away, no charge (a finite, zero term)
+                s_nxh[e] = s_nyh[e] = -kPadPosition;
+                s_nxl[e] = s_nyl[e] = 0.0f;
+                s_q[e] = 0.0f;
+                if (MODE == 1) s_ax[e] = s_ay[e] = 0.0f;
+            }
+        }
+        __syncthreads();
+        if (!valid) continue;
+        for (int e = 0; e < cnt4; e += 4) {
+            float2 part[NS];
+#pragma unroll
+            for (int k = 0; k < NS; k++) part[k] = dup2(0.0f);
+#pragma unroll
+            for (int h = 0; h < 4; h += 2) {
+                const int e0 = e + h;
+                float2 dx, dy, r2, yy, ex;
+                const float2 qj = make_float2(s_q[e0], s_q[e0 + 1]);
+                pair2_core(I, make_float2(s_nxh[e0], s_nxh[e0 + 1]), make_float2(s_nyh[e0], s_nyh[e0 + 1]),
+                           make_float2(s_nxl[e0], s_nxl[e0 + 1]), make_float2(s_nyl[e0], s_nyl[e0 + 1]), nkl2e,
+                           dx, dy, r2, yy, ex);
+                const int ja = j0 + e0, jb = ja + 1;
+                bool ina = r2.x < d.rc2_lo && ja != li, inb = r2.y < d.rc2_lo && jb != li;
+                if (!(r2.x < d.rc2_lo) && r2.x < d.rc2_hi && ja < d.n && ja != li)
+                    ina = adj_border_in(d, x, y, i, d.off + ja);
+                if (!(r2.y < d.rc2_lo) && r2.y < d.rc2_hi && jb < d.n && jb != li)
+                    inb = adj_border_in(d, x, y, i, d.off + jb);
+                // q_j e^{-kappa r} and 1/r, both 0 outside the cutoff and for j == i
+                // (where r = 0 made them non-finite), so every term below is 0 there
+                float2 qe = mul2(qj, ex);
+                qe.x = ina ? qe.x : 0.0f;
+                qe.y = inb ? qe.y : 0.0f;
+                yy.x = ina ? yy.x : 0.0f;
+                yy.y = inb ? yy.y : 0.0f;
+                const float2 y2 = mul2(yy, yy);
+                const float2 t = add2(yy, kap);
+                const float2 ww = mul2(qe, mul2(y2, t));  // g / (C q_i)
+                if (MODE == 0) {
+                    part[0] = fma2(ww, dx, part[0]);
+                    part[1] = fma2(ww, dy, part[1]);
+                } else {
+                    // h / (C q_i) = -q_j e y^3 (kappa^2 + 3 y (y + kappa))
+                    const float2 hv = mul2(mul2(qe, mul2(y2, yy)), fma2(mul2(yy, m3), t, nk2));
+                    const float2 bx = add2(ax2, make_float2(-s_ax[e0], -s_ax[e0 + 1]));
+                    const float2 by = add2(ay2, make_float2(-s_ay[e0], -s_ay[e0 + 1]));
+                    const float2 dd = fma2(dx, bx, mul2(dy, by));
+                    const float2 aid = fma2(ax2, dx, mul2(ay2, dy));
+                    const float2 hdd = mul2(hv, dd);
+                    part[0] = fma2(ww, bx, fma2(hdd, dx, part[0]));
+                    part[1] = fma2(ww, by, fma2(hdd, dy, part[1]));
+                    part[2] = fma2(ww, dd, part[2]);
+                    part[3] = fma2(mul2(qe, yy), aid, part[3]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NS; k++) kahan_add(sum[k], cmp[k], part[k].x + part[k].y);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = (k < NS) ? sum[k] - cmp[k] : 0.0f;
+}
+
+// The pair sums of particle i in FP64 (adj_tile_fp64), the same outputs as
+// adj_pair_sums_fp32c multiplied out (C q_i included).
+template <int MODE>
+__device__ __forceinline__ void adj_pair_sums_fp64(const AdjCloud &d, int li, bool valid, const double *x,
+                                                   const double *y, const double *q, const double *ajx,
+                                                   const double *ajy, double axi, double ayi, double coulomb,
+                                                   double (&out)[4]) {
+    __shared__ AdjJ sj[kAdjTile];
+    __shared__ float2 sf[kAdjTile];
+    __shared__ unsigned int s_amax;
+    AdjSums S{};
+    const int i = d.off + (valid ? li : 0);
+    const double xi = x[i], yi = y[i], qi = q[i];
+    const float xfi = (float)xi, yfi = (float)yi;
+    const float ai = fmaxf(fabsf(xfi), fabsf(yfi));
+    const double rc = sqrt(d.rc2);
+    for (int j0 = 0; j0 < d.n; j0 += kAdjTile) {
+        const int cnt = min(kAdjTile, d.n - j0);
+        __syncthreads();
+        if (threadIdx.x == 0) s_amax = 0u;
+        __syncthreads();
+        float am = 0.0f;
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+            const int j = d.off + j0 + e;
+            AdjJ v;
+            v.x = x[j];
+            v.y = y[j];
+            v.q = q[j];
+            v.ax = (MODE == 1) ? ajx[j] : 0.0;
+            v.ay = (MODE == 1) ? ajy[j] : 0.0;
+            sj[e] = v;
+            const float2 f = make_float2((float)v.x, (float)v.y);
+            sf[e] = f;
+            am = fmaxf(am, fmaxf(fabsf(f.x), fabsf(f.y)));
+        }
+        for (int o = 16; o > 0; o >>= 1) am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
+        if ((threadIdx.x & 31) == 0) atomicMax(&s_amax, __float_as_uint(am));  // non-negative: int order
+        __syncthreads();
+        if (valid)
+            adj_tile_fp64<MODE>(d, sj, sf, cnt, j0, li, xi, yi, qi, axi, ayi, xfi, yfi,
+                                adj_candidate_bound(rc, ai, __uint_as_float(s_amax)), coulomb, S);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = S.v[k];
+}
+
+// Forward stage of the fused RK4 step (one thread per particle).
+template <bool F32C>
+__global__ void __launch_bounds__(kAdjThreads) adj_step_forces(const AdjCloud *__restrict__ desc,
+                                                               const int *__restrict__ cloud_of_block,
+                                                               const int *__restrict__ tile_of_block,
+                                                               const AdjStepIO io, double coulomb) {
+    const AdjCloud d = desc[cloud_of_block[blockIdx.x]];
+    const int li = tile_of_block[blockIdx.x] * kAdjThreads + threadIdx.x;
+    const bool valid = li < d.n;
+    const int i = d.off + (valid ? li : 0);
+    double px = 0.0, py = 0.0;
+    if (d.flags & kShieldedCoulomb) {
+        if (F32C) {
+            float o[4];
+            adj_pair_sums_fp32c<0>(d, li, valid, io.x, io.y, io.q, nullptr, nullptr, 0.0f, 0.0f, o);
+            const double cq = __dmul_rn(coulomb, io.q[i]);
+            px = __dmul_rn(cq, (double)o[0]);
+            py = __dmul_rn(cq, (double)o[1]);
+        } else {
+            double o[4];
+            adj_pair_sums_fp64<0>(d, li, valid, io.x, io.y, io.q, nullptr, nullptr, 0.0, 0.0, coulomb, o);
+            px = o[0];
+            py = o[1];
+        }
+    }
+    if (!valid) return;
+    const double xi = io.x[i], yi = io.y[i], vxi = io.vx[i], vyi = io.vy[i], qi = io.q[i], mi = io.m[i];
+    double fx = 0.0, fy = 0.0;
+    if (d.flags & kConfinement) { fx += qi * d.confine * xi; fy += qi * d.confine * yi; }
+    if (d.flags & kDrag) { fx += -d.gamma * mi * vxi; fy += -d.gamma * mi * vyi; }
+    if (d.flags & kRectConfinement) { fx += qi * d.confine_x * xi; fy += qi * d.confine_y * yi; }
+    fx += px;
+    fy += py;
+    const double dt = io.dt;
+    const double k[4] = {__dmul_rn(dt, vxi), __dmul_rn(dt, vyi), __dmul_rn(dt, __ddiv_rn(fx, mi)),
+                         __dmul_rn(dt, __ddiv_rn(fy, mi))};
+    double *const S[4] = {io.sx, io.sy, io.svx, io.svy};
+    double *const N[4] = {io.nx, io.ny, io.nvx, io.nvy};
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const double base = S[c][i];
+        if (io.stage == 1) {
+            io.k1[c][i] = k[c];
+            N[c][i] = __dadd_rn(base, __dmul_rn(0.5, k[c]));
+        } else if (io.stage == 2) {
+            io.k23[c][i] = k[c];
+            N[c][i] = __dadd_rn(base, __dmul_rn(0.5, k[c]));
+        } else if (io.stage == 3) {
+            io.k23[c][i] = __dadd_rn(io.k23[c][i], k[c]);
+            N[c][i] = __dadd_rn(base, k[c]);
+        } else {
+            const double inc = __ddiv_rn(__dadd_rn(io.k1[c][i], __dadd_rn(__dmul_rn(io.k23[c][i], 2.0), k[c])), 6.0);
+            S[c][i] = __dadd_rn(base, inc);
+        }
+    }
+}
+
+// The force adjoint a = dt dk_v / m of every particle for a VJP stage.
+__global__ void adj_force_adjoint(const AdjVjpIO V, int n, float *axf, float *ayf, double *axd, double *ayd) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double ax = __ddiv_rn(__dmul_rn(V.dt, adj_dk(V, 2, k)), V.m[k]);
+    const double ay = __ddiv_rn(__dmul_rn(V.dt, adj_dk(V, 3, k)), V.m[k]);
+    axd[k] = ax;
+    ayd[k] = ay;
+    axf[k] = (float)ax;
+    ayf[k] = (float)ay;
+}
+
+// Backward stage (one thread per particle); a = dt dk_v / m of every
+// particle precomputed by adj_force_adjoint (axd/ayd, FP32 copies axf/ayf).
+template <bool F32C>
+__global__ void __launch_bounds__(kAdjThreads) adj_step_vjp(const AdjCloud *__restrict__ desc,
+                                                            const int *__restrict__ cloud_of_block,
+                                                            const int *__restrict__ tile_of_block, const AdjVjpIO V,
+                                                            const float *__restrict__ axf, const float *__restrict__ ayf,
+                                                            const double *__restrict__ axd,
+                                                            const double *__restrict__ ayd, double coulomb) {
+    const AdjCloud d = desc[cloud_of_block[blockIdx.x]];
+    const int li = tile_of_block[blockIdx.x] * kAdjThreads + threadIdx.x;
+    const bool valid = li < d.n;
+    const int i = d.off + (valid ? li : 0);
+    const double axi = axd[i], ayi = ayd[i];
+    double S[4] = {0.0, 0.0, 0.0, 0.0};
+    if (d.flags & kShieldedCoulomb) {
+        if (F32C) {
+            float o[4];
+            adj_pair_sums_fp32c<1>(d, li, valid, V.x, V.y, V.q, axf, ayf, (float)axi, (float)ayi, o);
+            const double cq = __dmul_rn(coulomb, V.q[i]);
+            S[0] = __dmul_rn(cq, (double)o[0]);
+            S[1] = __dmul_rn(cq, (double)o[1]);
+            S[2] = __dmul_rn(cq, (double)o[2]);
+            S[3] = __dmul_rn(__dmul_rn(-d.kappa, cq), (double)o[3]);
+        } else {
+            adj_pair_sums_fp64<1>(d, li, valid, V.x, V.y, V.q, axd, ayd, axi, ayi, coulomb, S);
+        }
+    }
+    if (!valid) return;
+    const double xi = V.x[i], yi = V.y[i], qi = V.q[i], mi = V.m[i];
+    double gx = S[0], gy = S[1], gq = (qi != 0.0) ? S[2] / qi : 0.0, gkc = 0.0;
+    if (d.flags & kConfinement) {
+        gx += qi * d.confine * axi;
+        gy += qi * d.confine * ayi;
+        gq += d.confine * (xi * axi + yi * ayi);
+        gkc = qi * (xi * axi + yi * ayi);
+    }
+    if (d.flags & kRectConfinement) {
+        gx += qi * d.confine_x * axi;
+        gy += qi * d.confine_y * ayi;
+        gq += d.confine_x * xi * axi + d.confine_y * yi * ayi;
+    }
+    const double gv = (d.flags & kDrag) ? -d.gamma * mi : 0.0;
+    const double dt = V.dt;
+    // mu = J^T (dt dk): positions through the forces, velocities through
+    // f_pos = v and the drag
+    const double mu[4] = {gx, gy, __dadd_rn(__dmul_rn(dt, adj_dk(V, 0, i)), gv * axi),
+                          __dadd_rn(__dmul_rn(dt, adj_dk(V, 1, i)), gv * ayi)};
+    V.gq[i] += gq;
+    V.gkappa[i] += S[3];
+    V.gkc[i] += gkc;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const double l = V.lam[c][i];
+        if (V.stage == 4) {
+            V.mu[0][c][i] = mu[c];
+            V.dkn[c][i] = __dadd_rn(__ddiv_rn(l, 3.0), mu[c]);
+        } else if (V.stage == 3) {
+            V.mu[1][c][i] = mu[c];
+            V.dkn[c][i] = __dadd_rn(__ddiv_rn(l, 3.0), __dmul_rn(0.5, mu[c]));
+        } else if (V.stage == 2) {
+            V.mu[2][c][i] = mu[c];
+            V.dkn[c][i] = __dadd_rn(__ddiv_rn(l, 6.0), __dmul_rn(0.5, mu[c]));
+        } else {
+            V.lam[c][i] = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(l, mu[c]), V.mu[2][c][i]), V.mu[1][c][i]),
+                                    V.mu[0][c][i]);
+        }
     }
 }
 

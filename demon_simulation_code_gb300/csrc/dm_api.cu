@@ -1855,10 +1855,15 @@ struct dm_adjoint {
     AdjCloud *ddesc = nullptr;
     int *dcloud = nullptr, *dtile = nullptr;
     double coulomb = 0.0;
+    // fused RK4 step and adjoint: one block of total-length arrays
+    void *work = nullptr;
+    double *k1[4], *k23[4], *pbuf[2][4], *dk[2][4], *mu[3][4], *axd, *ayd;
+    float *axf, *ayf;
     ~dm_adjoint() {
         if (ddesc) cudaFree(ddesc);
         if (dcloud) cudaFree(dcloud);
         if (dtile) cudaFree(dtile);
+        if (work) cudaFree(work);
     }
 };
 
@@ -1878,6 +1883,7 @@ void adj_fill(dm_adjoint *A, const dm_force_params *params) {
         d.kappa_f = (float)d.kappa;
         d.kappa2_f = (float)(d.kappa * d.kappa);
         kappa_log2e(d.kappa, d.kl2e_hi, d.kl2e_lo);
+        d.nkl2e = (float)(-d.kappa * 1.4426950408889634);
     }
 }
 
@@ -1938,6 +1944,27 @@ int dm_adjoint_create(dm_ctx *ctx, int nclouds, const int *n, const dm_force_par
     if (e == cudaSuccess) e = cudaMemcpy(A->ddesc, A->hdesc.data(), nclouds * sizeof(AdjCloud), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(A->dcloud, bc.data(), bc.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(A->dtile, bt.data(), bt.size() * sizeof(int), cudaMemcpyHostToDevice);
+    // scratch of the fused RK4 step and its adjoint: 38 arrays of total doubles, 2 of floats
+    const size_t nd = align256((size_t)A->total * sizeof(double));
+    const size_t nf = align256((size_t)A->total * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&A->work, 38 * nd + 2 * nf);
+    if (e == cudaSuccess) {
+        char *p = (char *)A->work;
+        auto take = [&]() { double *r = (double *)p; p += nd; return r; };
+        for (int c = 0; c < 4; c++) A->k1[c] = take();
+        for (int c = 0; c < 4; c++) A->k23[c] = take();
+        for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 4; c++) A->pbuf[b][c] = take();
+        for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 4; c++) A->dk[b][c] = take();
+        for (int b = 0; b < 3; b++)
+            for (int c = 0; c < 4; c++) A->mu[b][c] = take();
+        A->axd = take();
+        A->ayd = take();
+        A->axf = (float *)p;
+        p += nf;
+        A->ayf = (float *)p;
+    }
     if (e != cudaSuccess) {
         delete A;
         return ctx->fail(DM_ERR_CUDA, "dm_adjoint_create: %s", cudaGetErrorString(e));
@@ -1977,6 +2004,96 @@ int dm_adjoint_forces(dm_adjoint *A, int precision, const double *x, const doubl
                   nullptr);
     DM_CUDA(ctx, cudaGetLastError());
     ctx->launches++;
+    return DM_OK;
+}
+
+int dm_adjoint_rk4_step(dm_adjoint *A, int precision, double dt, double *x, double *y, double *vx, double *vy,
+                        const double *q, const double *m, double *stages) {
+    if (!A || !x || !y || !vx || !vy || !q || !m) return A ? A->ctx->fail(DM_ERR_ARG, "NULL pointer") : DM_ERR_ARG;
+    dm_ctx *ctx = A->ctx;
+    if (precision != DM_FP64 && precision != DM_FP32C)
+        return ctx->fail(DM_ERR_ARG, "dm_adjoint_rk4_step: unknown precision %d", precision);
+    if (!std::isfinite(dt)) return ctx->fail(DM_ERR_ARG, "dm_adjoint_rk4_step: dt must be finite");
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t n = (size_t)A->total;
+    double *base[4] = {x, y, vx, vy};
+    if (stages)
+        for (int c = 0; c < 4; c++)
+            DM_CUDA(ctx, cudaMemcpyAsync(stages + c * n, base[c], n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                         ctx->stream));
+    for (int st = 1; st <= 4; st++) {
+        AdjStepIO io{};
+        double *in[4], *nx[4];
+        for (int c = 0; c < 4; c++) {
+            in[c] = (st == 1) ? base[c] : stages ? stages + (4 * (st - 1) + c) * n : A->pbuf[st & 1][c];
+            nx[c] = (st == 4) ? nullptr : stages ? stages + (4 * st + c) * n : A->pbuf[(st + 1) & 1][c];
+            io.k1[c] = A->k1[c];
+            io.k23[c] = A->k23[c];
+        }
+        io.x = in[0]; io.y = in[1]; io.vx = in[2]; io.vy = in[3];
+        io.sx = x; io.sy = y; io.svx = vx; io.svy = vy;
+        io.nx = nx[0]; io.ny = nx[1]; io.nvx = nx[2]; io.nvy = nx[3];
+        io.q = q;
+        io.m = m;
+        io.dt = dt;
+        io.stage = st;
+        if (precision == DM_FP32C)
+            adj_step_forces<true><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(A->ddesc, A->dcloud, A->dtile, io,
+                                                                              A->coulomb);
+        else
+            adj_step_forces<false><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(A->ddesc, A->dcloud, A->dtile, io,
+                                                                               A->coulomb);
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches++;
+    }
+    return DM_OK;
+}
+
+int dm_adjoint_rk4_step_vjp(dm_adjoint *A, int precision, double dt, const double *stages, const double *q,
+                            const double *m, double *lx, double *ly, double *lvx, double *lvy, double *gq,
+                            double *gkappa, double *gkc) {
+    if (!A || !stages || !q || !m || !lx || !ly || !lvx || !lvy || !gq || !gkappa || !gkc)
+        return A ? A->ctx->fail(DM_ERR_ARG, "NULL pointer") : DM_ERR_ARG;
+    dm_ctx *ctx = A->ctx;
+    if (precision != DM_FP64 && precision != DM_FP32C)
+        return ctx->fail(DM_ERR_ARG, "dm_adjoint_rk4_step_vjp: unknown precision %d", precision);
+    if (!std::isfinite(dt)) return ctx->fail(DM_ERR_ARG, "dm_adjoint_rk4_step_vjp: dt must be finite");
+    DM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t n = (size_t)A->total;
+    for (int st = 4; st >= 1; st--) {
+        AdjVjpIO V{};
+        V.x = stages + (4 * (st - 1) + 0) * n;
+        V.y = stages + (4 * (st - 1) + 1) * n;
+        V.vx = stages + (4 * (st - 1) + 2) * n;
+        V.vy = stages + (4 * (st - 1) + 3) * n;
+        // dk_3 in dk[0], dk_2 in dk[1], dk_1 in dk[0]; dk_4 = lam / 6
+        const int rd = (st == 3 || st == 1) ? 0 : 1, wr = (st == 4 || st == 2) ? 0 : 1;
+        double *lam[4] = {lx, ly, lvx, lvy};
+        for (int c = 0; c < 4; c++) {
+            V.dk[c] = A->dk[rd][c];
+            V.dkn[c] = A->dk[wr][c];
+            V.lam[c] = lam[c];
+            for (int b = 0; b < 3; b++) V.mu[b][c] = A->mu[b][c];
+        }
+        V.gq = gq;
+        V.gkappa = gkappa;
+        V.gkc = gkc;
+        V.q = q;
+        V.m = m;
+        V.dt = dt;
+        V.stage = st;
+        adj_force_adjoint<<<(A->total + 255) / 256, 256, 0, ctx->stream>>>(V, A->total, A->axf, A->ayf, A->axd,
+                                                                         A->ayd);
+        DM_CUDA(ctx, cudaGetLastError());
+        if (precision == DM_FP32C)
+            adj_step_vjp<true><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(A->ddesc, A->dcloud, A->dtile, V, A->axf,
+                                                                           A->ayf, A->axd, A->ayd, A->coulomb);
+        else
+            adj_step_vjp<false><<<A->nblocks, kAdjThreads, 0, ctx->stream>>>(A->ddesc, A->dcloud, A->dtile, V, A->axf,
+                                                                            A->ayf, A->axd, A->ayd, A->coulomb);
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches += 2;
+    }
     return DM_OK;
 }
 

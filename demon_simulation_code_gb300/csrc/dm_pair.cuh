@@ -93,30 +93,37 @@ struct PairI {
     float2 xh, yh, xl, yl;
 };
 
-// Pair terms of i with two j, the j values negated (nxh = -xh_j, ...):
+// The geometry of i with two j, the j values negated (nxh = -xh_j, ...):
 //   dx = x_i - x_j as (xh_i - xh_j) + (xl_i - xl_j) (the hi difference is
 //        exact for nearby particles, so dx keeps ~2^-24 of its own size),
-//   r2 = dx^2 + dy^2,
-//   w  = q_j e^{-kappa r} y^2 (y + kappa), y = 1/r,
-// so that the force on i from j is C q_i w (dx, dy) = C q_i q_j (1 + kappa
-// r) e^{-kappa r} / r^3 (dx, dy), the reference's pair force
-// (ShieldedCoulombForce.cpp:144-157), C q_i applied once per particle.
+//   r2 = dx^2 + dy^2, y = 1/r, ex = e^{-kappa r}.
 // 1/r: hardware rsqrt plus one Newton step, which also gives r = r2 y
-// refined; e^{-kappa r} = 2^{-(kappa log2 e) r} on the SFU.  A pair at
-// r2 = 0 gives non-finite w: callers exclude j == i by a select.
-__device__ __forceinline__ void pair2_terms(const PairI &I, float2 nxh, float2 nyh, float2 nxl, float2 nyl,
-                                            float2 q, float2 kap, float2 nkl2e, float2 &dx, float2 &dy,
-                                            float2 &r2, float2 &w) {
+// refined; e^{-kappa r} = 2^{-(kappa log2 e) r} on the SFU.
+__device__ __forceinline__ void pair2_core(const PairI &I, float2 nxh, float2 nyh, float2 nxl, float2 nyl,
+                                           float2 nkl2e, float2 &dx, float2 &dy, float2 &r2, float2 &y,
+                                           float2 &ex) {
     dx = add2(add2(I.xh, nxh), add2(I.xl, nxl));
     dy = add2(add2(I.yh, nyh), add2(I.yl, nyl));
     r2 = fma2(dx, dx, mul2(dy, dy));
     const float2 y0 = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-    const float2 u = mul2(r2, y0);                       // r, unrefined
+    const float2 u = mul2(r2, y0);                                  // r, unrefined
     const float2 h = mul2(fma2(u, y0, dup2(-1.0f)), dup2(-0.5f));  // (1 - r2 y0^2) / 2
-    const float2 y = fma2(h, y0, y0);                    // 1/r after one Newton step
-    const float2 r = fma2(h, u, u);                      // r = r2 y, from the same step
-    const float2 nt = mul2(r, nkl2e);                    // -(kappa log2 e) r
-    const float2 ex = make_float2(ex2_approx(nt.x), ex2_approx(nt.y));
+    y = fma2(h, y0, y0);                                            // 1/r after one Newton step
+    const float2 r = fma2(h, u, u);                                 // r = r2 y, from the same step
+    const float2 nt = mul2(r, nkl2e);                               // -(kappa log2 e) r
+    ex = make_float2(ex2_approx(nt.x), ex2_approx(nt.y));
+}
+
+// Pair terms of i with two j (pair2_core), w = q_j e^{-kappa r} y^2 (y +
+// kappa), so that the force on i from j is C q_i w (dx, dy) = C q_i q_j (1 +
+// kappa r) e^{-kappa r} / r^3 (dx, dy), the reference's pair force
+// (ShieldedCoulombForce.cpp:144-157), C q_i applied once per particle.  A
+// pair at r2 = 0 gives non-finite w: callers exclude j == i by a select.
+__device__ __forceinline__ void pair2_terms(const PairI &I, float2 nxh, float2 nyh, float2 nxl, float2 nyl,
+                                            float2 q, float2 kap, float2 nkl2e, float2 &dx, float2 &dy,
+                                            float2 &r2, float2 &w) {
+    float2 y, ex;
+    pair2_core(I, nxh, nyh, nxl, nyl, nkl2e, dx, dy, r2, y, ex);
     w = mul2(mul2(q, ex), mul2(mul2(y, y), add2(y, kap)));
 }
 

@@ -356,6 +356,29 @@ int dm_adjoint_vjp(dm_adjoint *adj, int precision, const double *x,
                    const double *ay, double *gx, double *gy, double *gvx,
                    double *gvy, double *gq, double *gkappa, double *gkc);
 
+/* One RK4 step of the rollout, fused: four launches, each the pair force at
+ * the stage's input state plus the per-particle forces and the stage
+ * algebra k_s = dt f(s_s), s_2 = S + k_1/2, s_3 = S + k_2/2, s_4 = S + k_3,
+ * S' = S + (k_1 + ((k_2 + k_3) 2 + k_4)) / 6 with f(s) = (vx, vy, F/m) --
+ * the reference's Runge_Kutta4::moveParticles written for the state s
+ * (Runge_Kutta4.cpp:23-137).  x, y, vx, vy (device arrays of the
+ * concatenated clouds) are advanced in place.  stages: NULL, or a device
+ * array of 16 * total doubles that receives the four stage inputs (stage s
+ * at offset 4 (s-1) total: x, y, vx, vy), for dm_adjoint_rk4_step_vjp. */
+int dm_adjoint_rk4_step(dm_adjoint *adj, int precision, double dt, double *x,
+                        double *y, double *vx, double *vy, const double *q,
+                        const double *m, double *stages);
+/* The adjoint of one such step from its stage inputs: (lx, ly, lvx, lvy) =
+ * dL/d(output state) on entry, dL/d(input state) on return; the step's
+ * contributions to dL/dq_i, and per particle to dL/dkappa and dL/dk_c of its
+ * cloud, are ADDED to gq, gkappa, gkc.  Four launches (stages 4..1), each
+ * the force VJP at the stage's input and the per-particle adjoint
+ * recurrences of RK4.  No reference counterpart. */
+int dm_adjoint_rk4_step_vjp(dm_adjoint *adj, int precision, double dt,
+                            const double *stages, const double *q, const double *m,
+                            double *lx, double *ly, double *lvx, double *lvy,
+                            double *gq, double *gkappa, double *gkc);
+
 /* ---- allocation-free diagnostics ------------------------------------- */
 
 /* No counterpart in the reference.  dm_cloud_diagnostics' computation for
