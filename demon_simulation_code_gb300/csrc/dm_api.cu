@@ -869,7 +869,6 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     for (int k = 0; k < 6; k++) c->sort.stage[k] = takeD();
     c->sort.hist = (uint32_t *)p; p += nh;
     c->sort.box = (double *)p; p += 256;
-    c->d.keybox = c->sort.box;
     c->sort.moments = (double *)p; p += align256(sizeof(double) * kMomentBlocks * kMomentFields);
     cudaStream_t s = ctx->stream;
     const size_t bytes = (size_t)n * sizeof(double);
@@ -1378,8 +1377,7 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf =
     if (k.cull) {  // group boxes of the buffer this stage reads
         const int br = (mode == kModeForceOnly) ? fo_buf : (stage - 1) & 1;
         DM_CUDA(ctx, launch_pdl(batch_group_bounds, dim3((B->ngroups * 32 + 255) / 256), dim3(256), 0, ctx->stream,
-                                B->d, (const BatchCloud *)B->ddesc, (const int *)B->dgseg, B->ngroups, br,
-                                (const double *)B->dbox));
+                                B->d, (const BatchCloud *)B->ddesc, (const int *)B->dgseg, B->ngroups, br));
         ctx->launches++;
     }
     DM_CUDA(ctx, k.launch(dim3(B->grid[B->variant]), dim3(k.nt), k.smem, ctx->stream, P, B->ddesc,

@@ -89,11 +89,9 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
 
 // Box and outlier mask of every cloud's 32-particle groups in stage buffer
 // b (write_group_box; one warp per group; gseg[w] is group w's cloud; a
-// cloud's last group may be partial).  box: the clouds' key boxes
-// (batch_boxes; zero before the first sort).
+// cloud's last group may be partial).
 static __global__ void batch_group_bounds(CloudDev c, const BatchCloud *__restrict__ desc,
-                                          const int *__restrict__ gseg, int ngroups, int b,
-                                          const double *__restrict__ box) {
+                                          const int *__restrict__ gseg, int ngroups, int b) {
     pdl_wait();
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -107,7 +105,7 @@ static __global__ void batch_group_bounds(CloudDev c, const BatchCloud *__restri
         x = A.x;
         y = A.y;
     }
-    write_group_box(c.gbox[b], c.gmask[b], w, group_fat_threshold(d.rc2, box[8 * cl + 2], d.n), x, y, li < d.n);
+    write_group_box(c.gbox[b], c.gmask[b], w, sqrtf((float)d.rc2), x, y, li < d.n);
 }
 
 // --- per-cloud Morton order ------------------------------------------------

@@ -68,7 +68,6 @@ struct CloudDev {
     float4 *gbox[2];               // [n_pad/32] FP32 box (x0, y0, x1, y1) of each 32-particle group's
                                    // members, its outliers left out (write_group_box)
     uint32_t *gmask[2];            // [n_pad/32] each group's outlier members (bit = lane)
-    const double *keybox;          // the cloud's Morton key box (x0, y0, extent) of the last re-sort
     unsigned long long *eval_pairs;  // ordered pairs the culling kernels swept (cumulative)
     unsigned long long *step_ctr;  // [2], see stage_step_index()
     double *time;                  // [2] force time slots, see stage_time()
@@ -328,30 +327,19 @@ __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, i
 // within one RK4 substep (a close pair at a large dt), and one such member
 // stretches its group's box -- and its tile's -- across the cloud: every
 // tile then sweeps that group, and that tile every group.  So when a group's
-// box is wider than the fat threshold, the members farther than half the
-// threshold from the group's median (per axis) are its outliers: the box
-// covers the other members only, and the outliers are flagged in the group's
-// 32-bit mask, for the culling test to check their positions one by one.
+// box is wider than 16 cutoff radii, its members farther from the group's
+// median than max(8 cutoff radii, 3 interquartile ranges) on either axis are
+// its outliers (quartiles over the group's members): the box covers the
+// other members only, and the outliers are flagged in the group's 32-bit
+// mask, for the culling test to check their positions one by one.
 // Non-finite positions are outliers too.  Any split into box and outliers
-// is correct (the culling test covers both); the threshold only decides how
-// much work is done.
+// is correct (the culling test covers both); the rule only decides how much
+// work is done.
 // ---------------------------------------------------------------------------
 
-// Fat threshold of a cloud of n particles whose key box has the given
-// extent: 16 cutoff radii, or 8x the width of a group at the key box's mean
-// density, whichever is larger.
-__device__ __forceinline__ float group_fat_threshold(double rc2, double extent, int n) {
-    const float by_rc = 16.0f * sqrtf((float)rc2);
-    const float by_density = 8.0f * (float)extent * sqrtf(32.0f / (float)max(n, 1));
-    return (by_density > by_rc && isfinite(by_density)) ? by_density : by_rc;
-}
-__device__ __forceinline__ float group_fat_threshold(const CloudDev &c) {
-    return group_fat_threshold(c.rc2, c.keybox ? c.keybox[2] : 0.0, c.n);
-}
-
-// Median of the first k values of the warp (the other lanes pass +inf):
-// bitonic sort across the lanes, then element (k-1)/2.
-__device__ __forceinline__ float warp_median(float v, int k) {
+// Sorts the warp's values ascending across the lanes (bitonic network):
+// lane k ends with the k-th smallest.
+__device__ __forceinline__ float warp_sort(float v) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int w = 2; w <= 32; w <<= 1) {
@@ -362,7 +350,7 @@ __device__ __forceinline__ float warp_median(float v, int k) {
             v = (low == up) ? fminf(v, o) : fmaxf(v, o);
         }
     }
-    return __shfl_sync(0xffffffffu, v, (k - 1) >> 1);
+    return v;
 }
 
 __device__ __forceinline__ void warp_box(float &x0, float &y0, float &x1, float &y1) {
@@ -375,22 +363,34 @@ __device__ __forceinline__ void warp_box(float &x0, float &y0, float &x1, float 
     }
 }
 
+// The largest distance from the median of the nf finite values of the warp
+// (the others +inf) that is not an outlier: max(floor, 3 IQR); *med gets
+// the median.
+__device__ __forceinline__ float warp_spread(float v, int nf, float floor_, float *med) {
+    const float s = warp_sort(v);
+    const int top = nf - 1;
+    *med = __shfl_sync(0xffffffffu, s, top >> 1);
+    const float q1 = __shfl_sync(0xffffffffu, s, top >> 2);
+    const float q3 = __shfl_sync(0xffffffffu, s, (3 * top) >> 2);
+    return fmaxf(floor_, 3.0f * (q3 - q1));
+}
+
 // Box and outlier mask of group g: every lane of the warp calls it, (x, y)
-// its member's FP32 position (hi parts), valid = the lane holds a member.
-// A group with no member in its box gets the empty box (+inf, +inf, -inf,
-// -inf).
-__device__ __forceinline__ void write_group_box(float4 *gbox, uint32_t *gmask, int g, float thr, float x,
+// its member's FP32 position (hi parts), valid = the lane holds a member,
+// rc the cutoff radius.  A group with no member in its box gets the empty
+// box (+inf, +inf, -inf, -inf).
+__device__ __forceinline__ void write_group_box(float4 *gbox, uint32_t *gmask, int g, float rc, float x,
                                                 float y, bool valid) {
     const bool fin = valid && isfinite(x) && isfinite(y);
     float x0 = fin ? x : INFINITY, y0 = fin ? y : INFINITY, x1 = fin ? x : -INFINITY, y1 = fin ? y : -INFINITY;
     warp_box(x0, y0, x1, y1);
     uint32_t mask = __ballot_sync(0xffffffffu, valid && !fin);
-    if (fmaxf(x1 - x0, y1 - y0) > thr) {  // warp-uniform: every lane holds the reduced box
+    if (fmaxf(x1 - x0, y1 - y0) > 16.0f * rc) {  // warp-uniform: every lane holds the reduced box
         const int nf = __popc(__ballot_sync(0xffffffffu, fin));
-        const float mx = warp_median(fin ? x : INFINITY, nf);
-        const float my = warp_median(fin ? y : INFINITY, nf);
-        const float h = 0.5f * thr;
-        const bool out = fin && (fabsf(x - mx) > h || fabsf(y - my) > h);
+        float mx, my;
+        const float hx = warp_spread(fin ? x : INFINITY, nf, 8.0f * rc, &mx);
+        const float hy = warp_spread(fin ? y : INFINITY, nf, 8.0f * rc, &my);
+        const bool out = fin && (fabsf(x - mx) > hx || fabsf(y - my) > hy);
         mask |= __ballot_sync(0xffffffffu, out);
         const bool core = fin && !out;
         x0 = core ? x : INFINITY;
@@ -404,6 +404,9 @@ __device__ __forceinline__ void write_group_box(float4 *gbox, uint32_t *gmask, i
         gmask[g] = mask;
     }
 }
+
+// Cutoff radius of a cloud (the outlier rule of write_group_box).
+__device__ __forceinline__ float cutoff_radius(const CloudDev &c) { return sqrtf((float)c.rc2); }
 
 // Reference cutoff decision for one pair, bit for bit:
 // r = sqrt(dx*dx + dy*dy) (no fused multiply-add, SSE4.2 has none),

@@ -56,7 +56,7 @@ static __global__ void group_bounds(CloudDev c, int b) {
         x = A.x;
         y = A.y;
     }
-    write_group_box(c.gbox[b], c.gmask[b], g, group_fat_threshold(c), x, y, i < c.n);
+    write_group_box(c.gbox[b], c.gmask[b], g, cutoff_radius(c), x, y, i < c.n);
 }
 
 // ---------------------------------------------------------------------------

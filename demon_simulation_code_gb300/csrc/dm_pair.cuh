@@ -784,7 +784,7 @@ static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
             y = A.y;
         }
         // the grid covers whole 64-particle blocks of n, all below n_pad
-        write_group_box(P.c.gbox[bw], P.c.gmask[bw], i >> 5, group_fat_threshold(P.c), x, y, i < P.c.n);
+        write_group_box(P.c.gbox[bw], P.c.gmask[bw], i >> 5, cutoff_radius(P.c), x, y, i < P.c.n);
     }
     stage_step_advance(P);
 }

@@ -600,7 +600,7 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
         c.q[s] = 0.0;
         c.m[s] = 1.0;
     }
-    write_group_box(c.gbox[0], c.gmask[0], s >> 5, group_fat_threshold(c), px, py, s < c.n);
+    write_group_box(c.gbox[0], c.gmask[0], s >> 5, cutoff_radius(c), px, py, s < c.n);
 }
 
 // An upload in the caller's order (staging arrays 0..3: x, y, vx, vy) put
@@ -623,7 +623,7 @@ static __global__ void upload_internal_order(CloudDev c, SortScratch z) {
         px = A.x;
         py = A.y;
     }
-    write_group_box(c.gbox[0], c.gmask[0], s >> 5, group_fat_threshold(c), px, py, s < c.n);
+    write_group_box(c.gbox[0], c.gmask[0], s >> 5, cutoff_radius(c), px, py, s < c.n);
 }
 
 static __global__ void set_identity(int *orig, int n) {
