@@ -829,8 +829,7 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->sort_blocks = (n + kSortPerBlock - 1) / kSortPerBlock;
     const size_t nh = align256((size_t)kSortBuckets * c->sort_blocks * sizeof(uint32_t));
     const size_t ngb = align256((size_t)(c->n_pad / 32) * sizeof(float4));
-    const size_t ngm = align256((size_t)(c->n_pad / 32) * sizeof(uint32_t));
-    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ngb * 2 + ngm * 2 + ni * 6 + nh + 1024 + 512 +
+    const size_t total = nd * (6 + 2 + 8 + 4 + 2 + 6) + nf4 * 4 + ngb * 2 + ni * 6 + nh + 1024 + 512 +
                          align256(sizeof(double) * kMomentBlocks * kMomentFields);
     cudaError_t e = cudaMalloc(&c->block, total);
     if (e != cudaSuccess) {
@@ -852,7 +851,6 @@ int dm_cloud_create(dm_ctx *ctx, int n, const double *x, const double *y, const 
     c->d_fy = takeD();
     for (int b = 0; b < 2; b++) { c->d.pa[b] = takeF4(); c->d.pb[b] = takeF4(); }
     for (int b = 0; b < 2; b++) { c->d.gbox[b] = (float4 *)p; p += ngb; }
-    for (int b = 0; b < 2; b++) { c->d.gmask[b] = (uint32_t *)p; p += ngm; }
     c->d.eval_pairs = (unsigned long long *)p; p += 256;
     c->d.step_ctr = (unsigned long long *)p; p += 256;
     c->d.time = (double *)(c->d.step_ctr + 4);  // same 256-byte slot, bytes 32-47
@@ -1624,9 +1622,6 @@ int dm_batch_create(dm_ctx *ctx, int nclouds, const int *n, const double *x, con
     for (int b = 0; b < 2 && e == cudaSuccess; b++) {
         e = cudaMalloc((void **)&d.gbox[b], (size_t)B->ngroups * sizeof(float4));
         if (e == cudaSuccess) B->extra.push_back(d.gbox[b]);
-        if (e == cudaSuccess) e = cudaMalloc((void **)&d.gmask[b], (size_t)B->ngroups * sizeof(uint32_t));
-        if (e == cudaSuccess) B->extra.push_back(d.gmask[b]);
-        if (e == cudaSuccess) e = cudaMemsetAsync(d.gmask[b], 0, (size_t)B->ngroups * sizeof(uint32_t), s);
     }
     if (e == cudaSuccess) e = cudaMalloc((void **)&B->dgseg, gseg.size() * sizeof(int));
     if (e == cudaSuccess) B->extra.push_back(B->dgseg);

@@ -37,8 +37,7 @@ __device__ __forceinline__ void batch_view(StageParams &V, const StageParams &P0
     for (int k = 0; k < 4; k++) { c.a1[k] += o; c.a23[k] += o; }
     for (int b = 0; b < 2; b++) {
         c.px[b] += o; c.py[b] += o; c.pa[b] += o; c.pb[b] += o;
-        c.gbox[b] += d.goff;  // group boxes and outlier masks numbered within the cloud
-        c.gmask[b] += d.goff;
+        c.gbox[b] += d.goff;  // group boxes numbered within the cloud
     }
     c.orig += o;  // values stay global caller indices (thermal counter, outputs)
     c.n = d.n;
@@ -87,25 +86,30 @@ __global__ void __launch_bounds__(NW * 32, (24 / NW > 0 ? 24 / NW : 1))
     stage_step_advance(P0);
 }
 
-// Box and outlier mask of every cloud's 32-particle groups in stage buffer
-// b (write_group_box; one warp per group; gseg[w] is group w's cloud; a
-// cloud's last group may be partial).
+// Box of every cloud's 32-particle groups in stage buffer b (one warp per
+// group; gseg[w] is group w's cloud; a cloud's last group may be partial).
 static __global__ void batch_group_bounds(CloudDev c, const BatchCloud *__restrict__ desc,
                                           const int *__restrict__ gseg, int ngroups, int b) {
     pdl_wait();
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= ngroups) return;  // whole warp
-    const int cl = gseg[w];
-    const BatchCloud d = desc[cl];
+    const BatchCloud d = desc[gseg[w]];
     const int li = 32 * (w - d.goff) + lane;
-    float x = 0.0f, y = 0.0f;
+    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
     if (li < d.n) {
         const float4 A = c.pa[b][d.off + li];
-        x = A.x;
-        y = A.y;
+        x0 = x1 = A.x;
+        y0 = y1 = A.y;
     }
-    write_group_box(c.gbox[b], c.gmask[b], w, sqrtf((float)d.rc2), x, y, li < d.n);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if (lane == 0) c.gbox[b][w] = make_float4(x0, y0, x1, y1);
 }
 
 // --- per-cloud Morton order ------------------------------------------------

@@ -65,9 +65,7 @@ struct CloudDev {
     double *a23[4];
     double *px[2], *py[2];
     float4 *pa[2], *pb[2];
-    float4 *gbox[2];               // [n_pad/32] FP32 box (x0, y0, x1, y1) of each 32-particle group's
-                                   // members, its outliers left out (write_group_box)
-    uint32_t *gmask[2];            // [n_pad/32] each group's outlier members (bit = lane)
+    float4 *gbox[2];               // [n_pad/32] FP32 box (x0, y0, x1, y1) of each 32-particle group
     unsigned long long *eval_pairs;  // ordered pairs the culling kernels swept (cumulative)
     unsigned long long *step_ctr;  // [2], see stage_step_index()
     double *time;                  // [2] force time slots, see stage_time()
@@ -318,95 +316,6 @@ __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, i
     c.pb[b][i] = make_float4(xl, yl, -filter_threshold(xh, yh, c.rc2),
                              __double2float_rn(c.coulomb * q));
 }
-
-// ---------------------------------------------------------------------------
-// Group boxes for the culling kernels, outliers kept out of them.
-//
-// A 32-particle group is consecutive in Morton order, so its members are
-// normally close together.  But a particle can be thrown far from the cloud
-// within one RK4 substep (a close pair at a large dt), and one such member
-// stretches its group's box -- and its tile's -- across the cloud: every
-// tile then sweeps that group, and that tile every group.  So when a group's
-// box is wider than 16 cutoff radii, its members farther from the group's
-// median than max(8 cutoff radii, 3 interquartile ranges) on either axis are
-// its outliers (quartiles over the group's members): the box covers the
-// other members only, and the outliers are flagged in the group's 32-bit
-// mask, for the culling test to check their positions one by one.
-// Non-finite positions are outliers too.  Any split into box and outliers
-// is correct (the culling test covers both); the rule only decides how much
-// work is done.
-// ---------------------------------------------------------------------------
-
-// Sorts the warp's values ascending across the lanes (bitonic network):
-// lane k ends with the k-th smallest.
-__device__ __forceinline__ float warp_sort(float v) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int w = 2; w <= 32; w <<= 1) {
-#pragma unroll
-        for (int j = w >> 1; j > 0; j >>= 1) {
-            const float o = __shfl_xor_sync(0xffffffffu, v, j);
-            const bool up = (lane & w) == 0, low = (lane & j) == 0;
-            v = (low == up) ? fminf(v, o) : fmaxf(v, o);
-        }
-    }
-    return v;
-}
-
-__device__ __forceinline__ void warp_box(float &x0, float &y0, float &x1, float &y1) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
-        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
-        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
-        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
-    }
-}
-
-// The largest distance from the median of the nf finite values of the warp
-// (the others +inf) that is not an outlier: max(floor, 3 IQR); *med gets
-// the median.
-__device__ __forceinline__ float warp_spread(float v, int nf, float floor_, float *med) {
-    const float s = warp_sort(v);
-    const int top = nf - 1;
-    *med = __shfl_sync(0xffffffffu, s, top >> 1);
-    const float q1 = __shfl_sync(0xffffffffu, s, top >> 2);
-    const float q3 = __shfl_sync(0xffffffffu, s, (3 * top) >> 2);
-    return fmaxf(floor_, 3.0f * (q3 - q1));
-}
-
-// Box and outlier mask of group g: every lane of the warp calls it, (x, y)
-// its member's FP32 position (hi parts), valid = the lane holds a member,
-// rc the cutoff radius.  A group with no member in its box gets the empty
-// box (+inf, +inf, -inf, -inf).
-__device__ __forceinline__ void write_group_box(float4 *gbox, uint32_t *gmask, int g, float rc, float x,
-                                                float y, bool valid) {
-    const bool fin = valid && isfinite(x) && isfinite(y);
-    float x0 = fin ? x : INFINITY, y0 = fin ? y : INFINITY, x1 = fin ? x : -INFINITY, y1 = fin ? y : -INFINITY;
-    warp_box(x0, y0, x1, y1);
-    uint32_t mask = __ballot_sync(0xffffffffu, valid && !fin);
-    if (fmaxf(x1 - x0, y1 - y0) > 16.0f * rc) {  // warp-uniform: every lane holds the reduced box
-        const int nf = __popc(__ballot_sync(0xffffffffu, fin));
-        float mx, my;
-        const float hx = warp_spread(fin ? x : INFINITY, nf, 8.0f * rc, &mx);
-        const float hy = warp_spread(fin ? y : INFINITY, nf, 8.0f * rc, &my);
-        const bool out = fin && (fabsf(x - mx) > hx || fabsf(y - my) > hy);
-        mask |= __ballot_sync(0xffffffffu, out);
-        const bool core = fin && !out;
-        x0 = core ? x : INFINITY;
-        y0 = core ? y : INFINITY;
-        x1 = core ? x : -INFINITY;
-        y1 = core ? y : -INFINITY;
-        warp_box(x0, y0, x1, y1);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        gbox[g] = make_float4(x0, y0, x1, y1);
-        gmask[g] = mask;
-    }
-}
-
-// Cutoff radius of a cloud (the outlier rule of write_group_box).
-__device__ __forceinline__ float cutoff_radius(const CloudDev &c) { return sqrtf((float)c.rc2); }
 
 // Reference cutoff decision for one pair, bit for bit:
 // r = sqrt(dx*dx + dy*dy) (no fused multiply-add, SSE4.2 has none),

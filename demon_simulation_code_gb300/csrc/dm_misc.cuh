@@ -40,23 +40,29 @@ static __global__ void tune_compress(CloudDev c, double cx, double cy, double la
     if (i < c.n) write_stage_position(c, 1, i, cx + lam * (c.x[i] - cx), cy + lam * (c.y[i] - cy));
 }
 
-// Box and outlier mask of each 32-particle group's FP32 positions (hi
-// parts) in stage buffer b, for the culling pair kernels (write_group_box):
-// one warp per group; padding particles are left out, so an all-padding
-// group gets an empty box.
+// Bounding box of each 32-particle group's FP32 positions (hi parts) in
+// stage buffer b, for the culling pair kernels: one warp per group; padding
+// particles are left out, so an all-padding group gets an empty box.
 static __global__ void group_bounds(CloudDev c, int b) {
     pdl_wait();
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     const int i = 32 * g + lane;
     if (32 * g >= c.n_pad) return;  // whole warp
-    float x = 0.0f, y = 0.0f;
+    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
     if (i < c.n) {
         const float4 A = c.pa[b][i];
-        x = A.x;
-        y = A.y;
+        x0 = x1 = A.x;
+        y0 = y1 = A.y;
     }
-    write_group_box(c.gbox[b], c.gmask[b], g, cutoff_radius(c), x, y, i < c.n);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if (lane == 0) c.gbox[b][g] = make_float4(x0, y0, x1, y1);
 }
 
 // ---------------------------------------------------------------------------

@@ -181,11 +181,9 @@ struct Fp32cSmem {
     static constexpr size_t cold = (size_t)ILP * 32 * sizeof(float4);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
-    // culling: near and inside group lists (NT each) and their per-warp
-    // counts; the positions of the tile's outlier members
+    // culling: near and inside group lists (NT each) and their per-warp counts
     static constexpr size_t glist = 2 * ((size_t)NW * 32 * sizeof(int) + NW * sizeof(int));
-    static constexpr size_t tpts = (size_t)ILP * 32 * sizeof(float2);
-    static constexpr size_t bytes = tile + cold + acc + red + glist + tpts;
+    static constexpr size_t bytes = tile + cold + acc + red + glist;
     // s_red, in float4 units from the start of shared memory
     static constexpr size_t red_offset = (tile + cold + acc) / sizeof(float4);
 };
@@ -241,9 +239,6 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
     float4 *s_red = s_acc + NW * ILP * 32;                 // [TILE]
     int *s_glist = reinterpret_cast<int *>(s_red + TILE);  // [NT] surviving groups
     int *s_wcount = s_glist + NT;                          // [NW]
-    // [TILE] the tile's outlier members (culling)
-    float2 *s_tpt = reinterpret_cast<float2 *>(smem_raw + Fp32cSmem<NW, ILP, TC>::bytes -
-                                               Fp32cSmem<NW, ILP, TC>::tpts);
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
@@ -259,9 +254,6 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
     // i side duplicated into both halves of a packed pair: the packed FMAs
     // evaluate two consecutive j against one i
     float2 px2[ILP], py2[ILP], nu2[ILP];  // 2 xh_i, 2 yh_i, -(filter bound)
-    // culling: the outlier members of the tile's groups (write_group_box),
-    // listed in s_tpt by warp 0
-    int kt = 0;  // tile outliers (the same on every thread)
 #pragma unroll
     for (int k = 0; k < ILP; k++) {
         const int i = tile * TILE + k * 32 + lane;
@@ -280,11 +272,6 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
         nu2[k] = dup2(nu);
         if (warp == 0) s_cold[k * 32 + lane] = cold;
         my_acc[k * 32 + lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if constexpr (CULL) {
-            const uint32_t tm = (tile * TILE + k * 32 < n) ? P.c.gmask[b][tile * ILP + k] : 0u;
-            if (warp == 0 && ((tm >> lane) & 1u)) s_tpt[kt + __popc(tm & ((1u << lane) - 1u))] = make_float2(ax, ay);
-            kt += __popc(tm);
-        }
     }
     // i side of slot k (runtime k: the slow paths exist once in the code)
     auto slot_i = [&](int k, int &ii) {
@@ -545,7 +532,6 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
         // beyond the cutoff from the tile's box is skipped whole (it holds no
         // pair the reference counts).  The survivors keep their order.
         const float4 *__restrict__ gb = P.c.gbox[b];
-        const uint32_t *__restrict__ gm = P.c.gmask[b];
         const int ngroups = (n + 31) >> 5;
         float4 tb = gb[tile * ILP];
 #pragma unroll
@@ -564,29 +550,10 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
             const int g = t * S + rank;
             bool near = false, inside = false;
             if (t < my_ng) {
-                // near when the boxes are, or a group outlier is near the
-                // tile's box or outliers, or a tile outlier near the group's
-                // box: every pair within the cutoff has its i in the tile's
-                // box or outliers and its j in the group's
                 const float4 gbox = gb[g];
-                const uint32_t gmk = gm[g];
-                const bool gcore = gbox.x <= gbox.z, tcore = tb.x <= tb.z;  // non-empty boxes
-                near = gcore && tcore && boxes_near(tb, gbox, P.rc2_hi);
-                for (uint32_t m = gmk; m && !near; m &= m - 1u) {
-                    const float4 A = pa[32 * g + __ffs(m) - 1];
-                    const float4 pt = make_float4(A.x, A.y, A.x, A.y);
-                    near = tcore && boxes_near(pt, tb, P.rc2_hi);
-                    for (int k = 0; k < kt && !near; k++) {
-                        const float2 u = s_tpt[k];
-                        near = boxes_near(pt, make_float4(u.x, u.y, u.x, u.y), P.rc2_hi);
-                    }
-                }
-                for (int k = 0; k < kt && !near && gcore; k++) {
-                    const float2 u = s_tpt[k];
-                    near = boxes_near(make_float4(u.x, u.y, u.x, u.y), gbox, P.rc2_hi);
-                }
+                near = boxes_near(tb, gbox, P.rc2_hi);
                 // the tile's own groups hold the pairs j == i: filtered path
-                inside = near && gmk == 0u && kt == 0 && g / ILP != tile && boxes_inside(tb, gbox, P.rc2_lo);
+                inside = near && g / ILP != tile && boxes_inside(tb, gbox, P.rc2_lo);
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, near && !inside);
             const uint32_t bal2 = __ballot_sync(0xffffffffu, inside);
@@ -777,14 +744,20 @@ static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
     }
     if (P.box_out) {  // a warp is one 32-particle group: its box in the buffer just written
         const int bw = P.stage & 1;
-        float x = 0.0f, y = 0.0f;
+        float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
         if (i < P.c.n) {
             const float4 A = P.c.pa[bw][i];
-            x = A.x;
-            y = A.y;
+            x0 = x1 = A.x;
+            y0 = y1 = A.y;
         }
-        // the grid covers whole 64-particle blocks of n, all below n_pad
-        write_group_box(P.c.gbox[bw], P.c.gmask[bw], i >> 5, cutoff_radius(P.c), x, y, i < P.c.n);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+            y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+            x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+            y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        }
+        if ((threadIdx.x & 31) == 0 && i < P.c.n_pad) P.c.gbox[bw][i >> 5] = make_float4(x0, y0, x1, y1);
     }
     stage_step_advance(P);
 }

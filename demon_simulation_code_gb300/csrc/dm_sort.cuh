@@ -576,7 +576,7 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= c.n_pad) return;  // whole warps: n_pad is a multiple of 64
-    float px = 0.0f, py = 0.0f;
+    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
     if (s < c.n) {
         const double x = z.stage[0][s], y = z.stage[1][s];
         c.x[s] = x;
@@ -588,8 +588,8 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
         c.orig[s] = z.orig_stage[s];
         write_stage_position(c, 0, s, x, y);
         const float4 A = c.pa[0][s];
-        px = A.x;
-        py = A.y;
+        x0 = x1 = A.x;
+        y0 = y1 = A.y;
     } else {
         for (int b = 0; b < 2; b++) {
             c.px[b][s] = (double)kPadPosition;
@@ -600,7 +600,14 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
         c.q[s] = 0.0;
         c.m[s] = 1.0;
     }
-    write_group_box(c.gbox[0], c.gmask[0], s >> 5, cutoff_radius(c), px, py, s < c.n);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if ((threadIdx.x & 31) == 0) c.gbox[0][s >> 5] = make_float4(x0, y0, x1, y1);
 }
 
 // An upload in the caller's order (staging arrays 0..3: x, y, vx, vy) put
@@ -610,7 +617,7 @@ static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
 static __global__ void upload_internal_order(CloudDev c, SortScratch z) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= c.n_pad) return;  // whole warps: n_pad is a multiple of 64
-    float px = 0.0f, py = 0.0f;
+    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
     if (s < c.n) {
         const int o = c.orig[s];
         const double x = z.stage[0][o], y = z.stage[1][o];
@@ -620,10 +627,17 @@ static __global__ void upload_internal_order(CloudDev c, SortScratch z) {
         c.vy[s] = z.stage[3][o];
         write_stage_position(c, 0, s, x, y);
         const float4 A = c.pa[0][s];
-        px = A.x;
-        py = A.y;
+        x0 = x1 = A.x;
+        y0 = y1 = A.y;
     }
-    write_group_box(c.gbox[0], c.gmask[0], s >> 5, cutoff_radius(c), px, py, s < c.n);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, off));
+        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, off));
+        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, off));
+        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, off));
+    }
+    if ((threadIdx.x & 31) == 0) c.gbox[0][s >> 5] = make_float4(x0, y0, x1, y1);
 }
 
 static __global__ void set_identity(int *orig, int n) {
