@@ -337,17 +337,21 @@ __device__ __forceinline__ bool adj_border_in(const AdjCloud &d, const double *x
 }
 
 // FP32C pair sums of particle li of cloud d over the cloud's j, staged kAsJ
-// at a time.  MODE 0: out[0..1] = sum_j w_ij (dx, dy) (times C q_i: the pair
-// force).  MODE 1 (a_i, a_j the force adjoints): out[0..1] = sum w b + h d
-// (d . b), out[2] = sum w (d . b), out[3] = sum q_j e y (a_i . d)
-// (times C q_i: the position VJP, F_ij . (a_i - a_j) and, times -kappa,
-// dg/dkappa), with b = a_i - a_j.  Every thread of the block calls it.
+// at a time as chunks of 4 j (one float4 per quantity, so a chunk is read
+// with a few broadcast loads).  MODE 0: out[0..1] = sum_j w_ij (dx, dy)
+// (times C q_i: the pair force).  MODE 1 (a_i, a_j the force adjoints):
+// out[0..1] = sum w b + h d (d . b), out[2] = sum w (d . b), out[3] = sum q_j
+// e y (a_i . d) (times C q_i: the position VJP, F_ij . (a_i - a_j) and, times
+// -kappa, dg/dkappa), with b = a_i - a_j.  j == i is the pair with r^2 = 0
+// exactly (dx = dy = 0), left out by the select.  Every thread of the block
+// calls it.
 template <int MODE>
 __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, bool valid, const double *x,
                                                     const double *y, const double *q, const float *ajx,
                                                     const float *ajy, float aix, float aiy, float (&out)[4]) {
-    __shared__ float s_nxh[kAsJ], s_nyh[kAsJ], s_nxl[kAsJ], s_nyl[kAsJ], s_q[kAsJ];
-    __shared__ float s_ax[MODE == 1 ? kAsJ : 1], s_ay[MODE == 1 ? kAsJ : 1];
+    constexpr int NQ = MODE == 0 ? 5 : 7;  // -xh, -yh, -xl, -yl, q (, a_x, a_y)
+    constexpr int NC = kAsJ / 4;
+    __shared__ float4 s_c[NQ][NC];
     constexpr int NS = MODE == 0 ? 2 : 4;
     float sum[NS], cmp[NS];
 #pragma unroll
@@ -359,52 +363,61 @@ __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, b
     const float2 kap = dup2(d.kappa_f), nkl2e = dup2(d.nkl2e);
     const float2 nk2 = dup2(-d.kappa2_f), m3 = dup2(-3.0f);
     const float2 ax2 = dup2(aix), ay2 = dup2(aiy);
+    const float lo = d.rc2_lo, hi = d.rc2_hi;
+    float *s_f = reinterpret_cast<float *>(s_c);
     for (int j0 = 0; j0 < d.n; j0 += kAsJ) {
         const int cnt = min(kAsJ, d.n - j0);
-        const int cnt4 = (cnt + 3) & ~3;
+        const int nch = (cnt + 3) >> 2;
         __syncthreads();
-        for (int e = threadIdx.x; e < cnt4; e += blockDim.x) {
+        for (int e = threadIdx.x; e < 4 * nch; e += blockDim.x) {
+            float v[NQ];
             if (e < cnt) {
                 const int j = d.off + j0 + e;
                 float h, l;
                 split2(x[j], h, l);
-                s_nxh[e] = -h;
-                s_nxl[e] = -l;
+                v[0] = -h;
+                v[2] = -l;
                 split2(y[j], h, l);
-                s_nyh[e] = -h;
-                s_nyl[e] = -l;
-                s_q[e] = (float)q[j];
+                v[1] = -h;
+                v[3] = -l;
+                v[4] = (float)q[j];
                 if (MODE == 1) {
-                    s_ax[e] = ajx[j];
-                    s_ay[e] = ajy[j];
+                    v[5] = ajx[j];
+                    v[6] = ajy[j];
                 }
             } else {  // padding: far away, no charge (a finite, zero term)
-                s_nxh[e] = s_nyh[e] = -kPadPosition;
-                s_nxl[e] = s_nyl[e] = 0.0f;
-                s_q[e] = 0.0f;
-                if (MODE == 1) s_ax[e] = s_ay[e] = 0.0f;
+                v[0] = v[1] = -kPadPosition;
+                v[2] = v[3] = v[4] = 0.0f;
+                if (MODE == 1) v[5] = v[6] = 0.0f;
             }
+#pragma unroll
+            for (int k = 0; k < NQ; k++) s_f[k * kAsJ + e] = v[k];  // s_c[k][e/4].{x,y,z,w}[e%4]
         }
         __syncthreads();
         if (!valid) continue;
-        for (int e = 0; e < cnt4; e += 4) {
+        for (int c = 0; c < nch; c++) {
+            float4 Q[NQ];
+#pragma unroll
+            for (int k = 0; k < NQ; k++) Q[k] = s_c[k][c];
             float2 part[NS];
 #pragma unroll
             for (int k = 0; k < NS; k++) part[k] = dup2(0.0f);
 #pragma unroll
-            for (int h = 0; h < 4; h += 2) {
-                const int e0 = e + h;
+            for (int h = 0; h < 2; h++) {
+                const float2 nxh = h ? make_float2(Q[0].z, Q[0].w) : make_float2(Q[0].x, Q[0].y);
+                const float2 nyh = h ? make_float2(Q[1].z, Q[1].w) : make_float2(Q[1].x, Q[1].y);
+                const float2 nxl = h ? make_float2(Q[2].z, Q[2].w) : make_float2(Q[2].x, Q[2].y);
+                const float2 nyl = h ? make_float2(Q[3].z, Q[3].w) : make_float2(Q[3].x, Q[3].y);
+                const float2 qj = h ? make_float2(Q[4].z, Q[4].w) : make_float2(Q[4].x, Q[4].y);
                 float2 dx, dy, r2, yy, ex;
-                const float2 qj = make_float2(s_q[e0], s_q[e0 + 1]);
-                pair2_core(I, make_float2(s_nxh[e0], s_nxh[e0 + 1]), make_float2(s_nyh[e0], s_nyh[e0 + 1]),
-                           make_float2(s_nxl[e0], s_nxl[e0 + 1]), make_float2(s_nyl[e0], s_nyl[e0 + 1]), nkl2e,
-                           dx, dy, r2, yy, ex);
-                const int ja = j0 + e0, jb = ja + 1;
-                bool ina = r2.x < d.rc2_lo && ja != li, inb = r2.y < d.rc2_lo && jb != li;
-                if (!(r2.x < d.rc2_lo) && r2.x < d.rc2_hi && ja < d.n && ja != li)
-                    ina = adj_border_in(d, x, y, i, d.off + ja);
-                if (!(r2.y < d.rc2_lo) && r2.y < d.rc2_hi && jb < d.n && jb != li)
-                    inb = adj_border_in(d, x, y, i, d.off + jb);
+                pair2_core(I, nxh, nyh, nxl, nyl, nkl2e, dx, dy, r2, yy, ex);
+                bool ina = r2.x < lo && r2.x > 0.0f, inb = r2.y < lo && r2.y > 0.0f;
+                // pairs within 4e-6 of the cutoff in r^2: the reference's FP64 test
+                if (__any_sync(0xffffffffu, (r2.x >= lo && r2.x < hi) || (r2.y >= lo && r2.y < hi))) {
+                    const int ja = j0 + 4 * c + 2 * h;
+                    if (r2.x >= lo && r2.x < hi && ja < d.n) ina = adj_border_in(d, x, y, i, d.off + ja);
+                    if (r2.y >= lo && r2.y < hi && ja + 1 < d.n) inb = adj_border_in(d, x, y, i, d.off + ja + 1);
+                }
                 // q_j e^{-kappa r} and 1/r, both 0 outside the cutoff and for j == i
                 // (where r = 0 made them non-finite), so every term below is 0 there
                 float2 qe = mul2(qj, ex);
@@ -419,10 +432,12 @@ __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, b
                     part[0] = fma2(ww, dx, part[0]);
                     part[1] = fma2(ww, dy, part[1]);
                 } else {
+                    const float2 ajx2 = h ? make_float2(Q[5].z, Q[5].w) : make_float2(Q[5].x, Q[5].y);
+                    const float2 ajy2 = h ? make_float2(Q[6].z, Q[6].w) : make_float2(Q[6].x, Q[6].y);
                     // h / (C q_i) = -q_j e y^3 (kappa^2 + 3 y (y + kappa))
                     const float2 hv = mul2(mul2(qe, mul2(y2, yy)), fma2(mul2(yy, m3), t, nk2));
-                    const float2 bx = add2(ax2, make_float2(-s_ax[e0], -s_ax[e0 + 1]));
-                    const float2 by = add2(ay2, make_float2(-s_ay[e0], -s_ay[e0 + 1]));
+                    const float2 bx = add2(ax2, make_float2(-ajx2.x, -ajx2.y));
+                    const float2 by = add2(ay2, make_float2(-ajy2.x, -ajy2.y));
                     const float2 dd = fma2(dx, bx, mul2(dy, by));
                     const float2 aid = fma2(ax2, dx, mul2(ay2, dy));
                     const float2 hdd = mul2(hv, dd);
