@@ -352,7 +352,6 @@ __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, b
     constexpr int NQ = MODE == 0 ? 5 : 7;  // -xh, -yh, -xl, -yl, q (, a_x, a_y)
     constexpr int NC = kAsJ / 4;
     __shared__ float4 s_c[NQ][NC];
-    __shared__ float4 s_ibox[kAdjThreads / 32], s_jbox[kAdjThreads / 32];  // per-warp boxes
     constexpr int NS = MODE == 0 ? 2 : 4;
     float sum[NS], cmp[NS];
 #pragma unroll
@@ -366,25 +365,10 @@ __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, b
     const float2 ax2 = dup2(aix), ay2 = dup2(aiy);
     const float lo = d.rc2_lo, hi = d.rc2_hi;
     float *s_f = reinterpret_cast<float *>(s_c);
-    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    // the block's i box (hi parts): with a j tile's box, decides whether every
-    // pair of the two is inside the cutoff (boxes_inside)
-    {
-        float bx0 = valid ? xh : INFINITY, by0 = valid ? yh : INFINITY;
-        float bx1 = valid ? xh : -INFINITY, by1 = valid ? yh : -INFINITY;
-        for (int o = 16; o > 0; o >>= 1) {
-            bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
-            by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
-            bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
-            by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
-        }
-        if ((threadIdx.x & 31) == 0) s_ibox[warp] = make_float4(bx0, by0, bx1, by1);
-    }
     for (int j0 = 0; j0 < d.n; j0 += kAsJ) {
         const int cnt = min(kAsJ, d.n - j0);
         const int nch = (cnt + 3) >> 2;
         __syncthreads();
-        float jx0 = INFINITY, jy0 = INFINITY, jx1 = -INFINITY, jy1 = -INFINITY;
         for (int e = threadIdx.x; e < 4 * nch; e += blockDim.x) {
             float v[NQ];
             if (e < cnt) {
@@ -401,10 +385,6 @@ __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, b
                     v[5] = ajx[j];
                     v[6] = ajy[j];
                 }
-                jx0 = fminf(jx0, -v[0]);
-                jx1 = fmaxf(jx1, -v[0]);
-                jy0 = fminf(jy0, -v[1]);
-                jy1 = fmaxf(jy1, -v[1]);
             } else {  // padding: far away, no charge (a finite, zero term)
                 v[0] = v[1] = -kPadPosition;
                 v[2] = v[3] = v[4] = 0.0f;
@@ -413,24 +393,8 @@ __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, b
 #pragma unroll
             for (int k = 0; k < NQ; k++) s_f[k * kAsJ + e] = v[k];  // s_c[k][e/4].{x,y,z,w}[e%4]
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            jx0 = fminf(jx0, __shfl_xor_sync(0xffffffffu, jx0, o));
-            jy0 = fminf(jy0, __shfl_xor_sync(0xffffffffu, jy0, o));
-            jx1 = fmaxf(jx1, __shfl_xor_sync(0xffffffffu, jx1, o));
-            jy1 = fmaxf(jy1, __shfl_xor_sync(0xffffffffu, jy1, o));
-        }
-        if ((threadIdx.x & 31) == 0) s_jbox[warp] = make_float4(jx0, jy0, jx1, jy1);
         __syncthreads();
         if (!valid) continue;
-        // every pair of the block's i and this tile's j inside the cutoff:
-        // no cutoff select and no borderline test, only j == i left out
-        float4 ib = s_ibox[0], jb = s_jbox[0];
-        for (int w = 1; w < nw; w++) {
-            const float4 a = s_ibox[w], b = s_jbox[w];
-            ib = make_float4(fminf(ib.x, a.x), fminf(ib.y, a.y), fmaxf(ib.z, a.z), fmaxf(ib.w, a.w));
-            jb = make_float4(fminf(jb.x, b.x), fminf(jb.y, b.y), fmaxf(jb.z, b.z), fmaxf(jb.w, b.w));
-        }
-        const bool all_in = ib.x <= ib.z && jb.x <= jb.z && boxes_inside(ib, jb, lo);
         for (int c = 0; c < nch; c++) {
             float4 Q[NQ];
 #pragma unroll
@@ -447,13 +411,9 @@ __device__ __forceinline__ void adj_pair_sums_fp32c(const AdjCloud &d, int li, b
                 const float2 qj = h ? make_float2(Q[4].z, Q[4].w) : make_float2(Q[4].x, Q[4].y);
                 float2 dx, dy, r2, yy, ex;
                 pair2_core(I, nxh, nyh, nxl, nyl, nkl2e, dx, dy, r2, yy, ex);
-                bool ina = r2.x > 0.0f, inb = r2.y > 0.0f;
-                if (!all_in) {
-                    ina = ina && r2.x < lo;
-                    inb = inb && r2.y < lo;
-                }
+                bool ina = r2.x < lo && r2.x > 0.0f, inb = r2.y < lo && r2.y > 0.0f;
                 // pairs within 4e-6 of the cutoff in r^2: the reference's FP64 test
-                if (!all_in && __any_sync(0xffffffffu, (r2.x >= lo && r2.x < hi) || (r2.y >= lo && r2.y < hi))) {
+                if (__any_sync(0xffffffffu, (r2.x >= lo && r2.x < hi) || (r2.y >= lo && r2.y < hi))) {
                     const int ja = j0 + 4 * c + 2 * h;
                     if (r2.x >= lo && r2.x < hi && ja < d.n) ina = adj_border_in(d, x, y, i, d.off + ja);
                     if (r2.y >= lo && r2.y < hi && ja + 1 < d.n) inb = adj_border_in(d, x, y, i, d.off + ja + 1);
