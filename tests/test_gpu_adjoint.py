@@ -16,6 +16,8 @@ from demon_simulation_code_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
+from demon_simulation_code_gb300.adjoint import AdjointKernels  # noqa: E402
+
 C = 1.0 / (4.0 * np.pi * 8.8541878e-12)
 
 
@@ -192,6 +194,25 @@ def test_rollout_gradient_vs_finite_differences_and_torch(setup):
         assert (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() < 1e-9
 
 
+class _AdjointOnTrajectory(AdjointKernels):
+    """Forward steps (and the backward pass's recomputed steps) in one
+    precision, the step adjoints in another: separates the adjoint's own
+    error from that of the trajectory it is evaluated on."""
+
+    def __init__(self, ns, forward, adjoint, **kw):
+        super().__init__(ns, precision=forward, **kw)
+        self._fwd = {"fp64": 0, "fp32c": 1}[forward]
+        self._adj = {"fp64": 0, "fp32c": 1}[adjoint]
+
+    def rk4_step(self, *a, **kw):
+        self.precision = self._fwd
+        return super().rk4_step(*a, **kw)
+
+    def rk4_step_vjp(self, *a, **kw):
+        self.precision = self._adj
+        return super().rk4_step_vjp(*a, **kw)
+
+
 def test_adjoint64_smooth_gradients_vs_finite_differences_and_fp64():
     """The 64 x 2048-particle, 200-step workload's shape on its first four
     clouds (clouds are independent, so each cloud's gradient is the same in
@@ -223,10 +244,20 @@ def test_adjoint64_smooth_gradients_vs_finite_differences_and_fp64():
     print("x0 fd", fd.tolist(), "fp64", g64["x0"][idx].tolist(), "fp32c", g32["x0"][idx].tolist())
     assert ((g64["x0"][idx] - fd).abs() / fd.abs()).max().item() < 1e-4
     assert ((g32["x0"][idx] - fd).abs() / scale).max().item() < 1e-4
-    # over all 8192 initial positions, norm-wise: the FP32C rollout's own
-    # trajectory carries FP32 force rounding, which close encounters amplify
-    # in the position gradient (measured 4e-3 at this start point; FP64 is
-    # the mode that meets 1e-4 everywhere)
+    # over all 8192 initial positions, norm-wise.  On the same (FP64)
+    # trajectory the FP32C step adjoint meets 1e-4 with room (measured
+    # 2.7e-7); the FP32C gradient differs from the FP64 one by what its own
+    # FP32C trajectory does to the loss (measured 5.1e-4; an FP64 adjoint on
+    # the FP32C trajectory differs by the same), so that gate is looser.
     rel = ((g32["x0"] - g64["x0"]).norm() / g64["x0"].norm()).item()
     print("x0 fp32c vs fp64 norm-wise", rel)
-    assert rel < 1e-2
+    assert rel < 2e-3
+    mixed = TrajectoryFit(sub, precision="fp64")
+    mixed.K = _AdjointOnTrajectory(mixed.ns, flags=sub.clouds[0].flags, gamma=sub.clouds[0].gamma,
+                                   forward="fp64", adjoint="fp32c")
+    _, gm = mixed.loss_and_grad()
+    rel_same = ((gm["x0"] - g64["x0"]).norm() / g64["x0"].norm()).item()
+    print("x0 fp32c step adjoint on the fp64 trajectory vs fp64 norm-wise", rel_same)
+    assert rel_same < 1e-5
+    for name in ("kappa", "q", "kc"):
+        assert ((gm[name] - g64[name]).abs() / g64[name].abs().max()).max().item() < 1e-5, name
