@@ -53,6 +53,7 @@ struct dm_ctx {
     double prof_pairs = 0.0;
     long long prof_launches = 0;
     int *h_err = nullptr;  // pinned word for the device error flags (read with each download)
+    int sort_ctas = 0;     // blocks of the one-cluster sort (0: not chosen yet)
 
     int fail(int code, const char *fmt, ...) {
         char buf[512];
@@ -93,7 +94,7 @@ struct dm_cloud {
     bool boxes_valid[2] = {false, false};  // group boxes (culling) match stage buffer b
     int split[2] = {0, 0};  // cluster size per precision (0 = not chosen yet)
     int tuned_variant[2] = {-1, -1};  // per precision: index into kVariants
-    float4 *partial = nullptr;         // [partial_cap][n_pad] non-cluster partial sums
+    float2 *partial = nullptr;         // [partial_cap][2][n_pad] non-cluster partial sums (per rank, axis)
     int partial_cap = 0;
     SortScratch sort{};
     int sort_blocks = 0;
@@ -255,8 +256,52 @@ int ensure_kernel_attrs(dm_ctx *ctx) {
             DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         DM_CUDA(ctx, cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
     }
-    DM_CUDA(ctx, cudaFuncSetAttribute(sort_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortClusterSmem));
+    DM_CUDA(ctx, cudaFuncSetAttribute(sort_cluster<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sort_cluster_smem<8>()));
+    DM_CUDA(ctx, cudaFuncSetAttribute(sort_cluster<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    DM_CUDA(ctx, cudaFuncSetAttribute(sort_cluster<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sort_cluster_smem<16>()));
     done[dev] = true;
+    return DM_OK;
+}
+
+template <int CTAS>
+cudaLaunchConfig_t sort_cluster_cfg(cudaStream_t s, cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CTAS);
+    cfg.blockDim = dim3(kSortClusterThreads);
+    cfg.dynamicSmemBytes = sort_cluster_smem<CTAS>();
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    attr[1].id = cudaLaunchAttributeClusterDimension;
+    attr[1].val.clusterDim.x = CTAS;
+    attr[1].val.clusterDim.y = 1;
+    attr[1].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
+    return cfg;
+}
+
+// Blocks of the one-cluster sort on this device: 16 (half the elements per
+// SM of 8) when a 16-block cluster of it can be scheduled, else 8;
+// DM_SORT_CLUSTER_CTAS=8 keeps 8.
+int choose_sort_ctas(dm_ctx *ctx) {
+    if (ctx->sort_ctas) return DM_OK;
+    int rc = ensure_kernel_attrs(ctx);
+    if (rc) return rc;
+    const char *e = getenv("DM_SORT_CLUSTER_CTAS");
+    int ctas = (e && atoi(e) == 8) ? 8 : 16;
+    if (ctas == 16) {
+        cudaLaunchAttribute attr[2];
+        cudaLaunchConfig_t cfg = sort_cluster_cfg<16>(ctx->stream, attr);
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, sort_cluster<16>, &cfg) != cudaSuccess || nc < 1) {
+            cudaGetLastError();
+            ctas = 8;
+        }
+    }
+    ctx->sort_ctas = ctas;
     return DM_OK;
 }
 
@@ -352,7 +397,7 @@ int ensure_partial(dm_cloud *c, int S) {
     if (c->partial) cudaFree(c->partial);
     c->partial = nullptr;
     c->partial_cap = 0;
-    cudaError_t e = cudaMalloc((void **)&c->partial, (size_t)S * c->n_pad * sizeof(float4));
+    cudaError_t e = cudaMalloc((void **)&c->partial, (size_t)S * 2 * c->n_pad * sizeof(float2));
     if (e != cudaSuccess)
         return ctx->fail(DM_ERR_NOMEM, "partial-sum buffer (%d x %d): %s", S, c->n_pad, cudaGetErrorString(e));
     c->partial_cap = S;
@@ -381,7 +426,10 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
     if (!k.cluster) {
         // stage_finish also writes the group boxes of the buffer the stage writes
         P.box_out = (mode != kModeForceOnly) ? 1 : 0;
-        DM_CUDA(ctx, launch_pdl(stage_finish, dim3((c->n + 63) / 64), dim3(64), 0, ctx->stream, P));
+        if (P.f.flags & ~kBasicForces)
+            DM_CUDA(ctx, launch_pdl(stage_finish, dim3((c->n + 63) / 64), dim3(64), 0, ctx->stream, P));
+        else  // one thread per particle and axis, one block per 32-particle group
+            DM_CUDA(ctx, launch_pdl(stage_finish_axes, dim3(2 * ((c->n + 63) / 64)), dim3(64), 0, ctx->stream, P));
         ctx->launches++;
     }
     if (mode != kModeForceOnly) c->boxes_valid[stage & 1] = !k.cluster;
@@ -553,10 +601,17 @@ int reorder(dm_cloud *c) {
     SortScratch &z = c->sort;
     int cur = 0;
     if (n <= kSmallSortMax) {  // one cluster launch sorts and gathers; one more commits
-        int rc = ensure_kernel_attrs(ctx);
+        int rc = choose_sort_ctas(ctx);
         if (rc) return rc;
-        DM_CUDA(ctx, launch_pdl(sort_cluster, dim3(kSortClusterCtas), dim3(kSortClusterThreads), kSortClusterSmem,
-                                s, (const float4 *)c->d.pa[0], c->d, z));
+        cudaLaunchAttribute attr[2];
+        const float4 *pa0 = c->d.pa[0];
+        if (ctx->sort_ctas == 16) {
+            const cudaLaunchConfig_t cfg = sort_cluster_cfg<16>(s, attr);
+            DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, sort_cluster<16>, pa0, c->d, z));
+        } else {
+            const cudaLaunchConfig_t cfg = sort_cluster_cfg<8>(s, attr);
+            DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, sort_cluster<8>, pa0, c->d, z));
+        }
         DM_CUDA(ctx, launch_pdl(permute_commit_init, dim3((c->n_pad + 255) / 256), dim3(256), 0, s, c->d, z));
         c->boxes_valid[0] = true;  // written by permute_commit_init
         c->boxes_valid[1] = false;

@@ -634,7 +634,11 @@ __global__ void __launch_bounds__(NW * 32, fp32c_min_blocks<NW, ILP>())
     float4 *s_red = reinterpret_cast<float4 *>(smem_raw) + Fp32cSmem<NW, ILP, TC>::red_offset;
     if constexpr (!CL) {
         for (int e = tid; e < TILE; e += NW * 32)
-            if (tile * TILE + e < n) P.partial[(size_t)rank * n_pad + tile * TILE + e] = s_red[e];
+            if (tile * TILE + e < n) {
+                const float4 v = s_red[e];
+                P.partial[(size_t)(2 * rank) * n_pad + tile * TILE + e] = make_float2(v.x, v.z);
+                P.partial[(size_t)(2 * rank + 1) * n_pad + tile * TILE + e] = make_float2(v.y, v.w);
+            }
     } else {
         // finalise particles [rank*fchunk, (rank+1)*fchunk) of the tile in
         // whole warps: an FP64 warp instruction costs the same with 1 or 32
@@ -661,85 +665,54 @@ __global__ void __launch_bounds__(NW * 32, fp32c_min_blocks<NW, ILP>())
     }
 }
 
-// Completes a stage after a non-cluster pair launch: per particle, the
-// split partial sums in rank order (FP64), then the stage epilogue.  One
-// particle per thread: the FP64 work runs in full warps on every SM.
+// Sum over the j split's ranks, in rank order, of one axis's partials
+// (s, c) of particle i (each stands for s - c): the s exactly as an
+// unevaluated float pair (TwoSum), the small c plainly, FP64 once -- FP64
+// runs at ~1/64 of the FP32 rate here and an FP64 sum over the ranks
+// dominated the finish.  Times C q_i (left out of the sweeps), in FP64.
+__device__ __forceinline__ double finish_rank_sum(const StageParams &P, int i, int axis) {
+    TwoFloatSum sa;
+    float ca = 0.0f;
+    const float2 *p = P.partial + (size_t)axis * P.c.n_pad + i;
+    const size_t stride = 2 * (size_t)P.c.n_pad;
+    int r = 0;
+    for (; r + 16 <= P.split; r += 16) {  // 16 loads in flight, summed in rank order
+        float2 v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) v[u] = p[(size_t)(r + u) * stride];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            sa.add(v[u].x);
+            ca += v[u].y;
+        }
+    }
+    for (; r + 8 <= P.split; r += 8) {  // 8 loads in flight, summed in rank order
+        float2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = p[(size_t)(r + u) * stride];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            sa.add(v[u].x);
+            ca += v[u].y;
+        }
+    }
+    for (; r < P.split; r++) {
+        const float2 v = p[(size_t)r * stride];
+        sa.add(v.x);
+        ca += v.y;
+    }
+    return __dmul_rn(pair_scale(P, i), (double)sa.hi + ((double)sa.lo - (double)ca));
+}
+
+// Completes a stage after a non-cluster pair launch when forces outside
+// kBasicForces are on (they couple the axes): one particle per thread, the
+// rank sums of both axes, then the stage epilogue.
 static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P.c.n) {
-        // One warp per 32 particles is little parallelism for the chain of
-        // dependent loads below (the split partials, then the epilogue's
-        // state): the epilogue's operands are prefetched into L1 first, so
-        // their round trip overlaps the partials'.
-        {
-            const CloudDev &c = P.c;
-            const int b = (P.mode == kModeForceOnly) ? P.fo_buf : (P.stage - 1) & 1;
-            const bool first = P.mode == kModeForceOnly || P.stage == 1;
-            prefetch_l1(c.px[b] + i);
-            prefetch_l1(c.py[b] + i);
-            prefetch_l1((first ? c.vx : c.vxc) + i);
-            prefetch_l1((first ? c.vy : c.vyc) + i);
-            prefetch_l1(c.q + i);
-            prefetch_l1(c.m + i);
-            prefetch_l1(c.orig + i);
-            if (P.mode != kModeForceOnly) {
-                prefetch_l1(c.x + i);
-                prefetch_l1(c.y + i);
-                if (!first) {
-                    prefetch_l1(c.vx + i);
-                    prefetch_l1(c.vy + i);
-                }
-                if (P.stage >= 3)
-                    for (int k = 0; k < 4; k++) prefetch_l1(c.a23[k] + i);
-                if (P.stage == 4)
-                    for (int k = 0; k < 4; k++) prefetch_l1(c.a1[k] + i);
-            }
-        }
-        // each partial (s, c) stands for s - c; the s are summed exactly as
-        // an unevaluated float pair (TwoSum), the small c plainly, in rank
-        // order, and FP64 is used once: FP64 runs at ~1/64 of the FP32 rate
-        // here and an FP64 sum over the ranks dominated this kernel
-        TwoFloatSum sx, sy;
-        float cx = 0.0f, cy = 0.0f;
-        const float4 *p = P.partial + i;
-        const size_t stride = (size_t)P.c.n_pad;
-        int r = 0;
-        for (; r + 16 <= P.split; r += 16) {  // 16 loads in flight, summed in rank order
-            float4 v[16];
-#pragma unroll
-            for (int u = 0; u < 16; u++) v[u] = p[(size_t)(r + u) * stride];
-#pragma unroll
-            for (int u = 0; u < 16; u++) {
-                sx.add(v[u].x);
-                sy.add(v[u].y);
-                cx += v[u].z;
-                cy += v[u].w;
-            }
-        }
-        for (; r + 8 <= P.split; r += 8) {  // 8 loads in flight, summed in rank order
-            float4 v[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) v[u] = p[(size_t)(r + u) * stride];
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                sx.add(v[u].x);
-                sy.add(v[u].y);
-                cx += v[u].z;
-                cy += v[u].w;
-            }
-        }
-        for (; r < P.split; r++) {
-            const float4 v = p[(size_t)r * stride];
-            sx.add(v.x);
-            sy.add(v.y);
-            cx += v.z;
-            cy += v.w;
-        }
-        // the sums leave out C q_i (pair_scale), applied here in FP64
-        const double cq = pair_scale(P, i);
-        const double fx = __dmul_rn(cq, (double)sx.hi + ((double)sx.lo - (double)cx));
-        const double fy = __dmul_rn(cq, (double)sy.hi + ((double)sy.lo - (double)cy));
+        const double fx = finish_rank_sum(P, i, 0);
+        const double fy = finish_rank_sum(P, i, 1);
         stage_epilogue(P, i, fx, fy, stage_thermal(P, i));
     }
     if (P.box_out) {  // a warp is one 32-particle group: its box in the buffer just written
@@ -758,6 +731,133 @@ static __global__ void __launch_bounds__(64) stage_finish(const StageParams P) {
             y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
         }
         if ((threadIdx.x & 31) == 0 && i < P.c.n_pad) P.c.gbox[bw][i >> 5] = make_float4(x0, y0, x1, y1);
+    }
+    stage_step_advance(P);
+}
+
+// The same completion with one thread per particle and axis, for the
+// forces in kBasicForces: block = one 32-particle group, warp 0 the x and
+// warp 1 the y components.  Each axis runs exactly the operations
+// stage_epilogue runs for it, in the same order, so the results are the
+// same bits; the finish is a latency-bound chain (rank partials, FP64 at
+// GB300's FP64 rate) and this gives it twice the warps.  The two warps
+// meet once, in shared memory, for what needs both axes: the next stage's
+// packed positions, filter bound and group box.
+static __global__ void __launch_bounds__(64) stage_finish_axes(const StageParams P) {
+    pdl_wait();
+    __shared__ float s_hi[2][32], s_lo[2][32];
+    const int lane = threadIdx.x & 31, ax = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + lane;
+    const CloudDev &c = P.c;
+    const bool live = i < c.n;
+    const bool fo = P.mode == kModeForceOnly;
+    const int s = fo ? 1 : P.stage;
+    const int b = fo ? P.fo_buf : (s - 1) & 1;
+    double na = 0.0;  // this axis's coordinate at the next stage
+    if (live) {
+        const double *pos = ax ? c.py[b] : c.px[b];
+        const double *vel = (s == 1) ? (ax ? c.vy : c.vx) : (ax ? c.vyc : c.vxc);
+        double *X = ax ? c.y : c.x;
+        double *V = ax ? c.vy : c.vx;
+        // the operands' round trip overlaps the partials' (see stage_finish)
+        prefetch_l1(pos + i);
+        prefetch_l1(vel + i);
+        prefetch_l1(c.q + i);
+        prefetch_l1(c.m + i);
+        prefetch_l1(c.orig + i);
+        if (!fo) {
+            prefetch_l1(X + i);
+            prefetch_l1(V + i);
+            if (s >= 3) {
+                prefetch_l1(c.a23[2 * ax] + i);
+                prefetch_l1(c.a23[2 * ax + 1] + i);
+            }
+            if (s == 4) {
+                prefetch_l1(c.a1[2 * ax] + i);
+                prefetch_l1(c.a1[2 * ax + 1] + i);
+            }
+        }
+        const double fpa = finish_rank_sum(P, i, ax);
+        const double xs = pos[i], vs = vel[i], q = c.q[i], m = c.m[i];
+        const long long fl = P.f.flags;
+        double F = 0.0;
+        if (fl & kConfinement) F = __dadd_rn(F, __dmul_rn(__dmul_rn(q, P.f.confine), xs));
+        if (fl & kDrag) F = __dadd_rn(F, __dmul_rn(__dmul_rn(m, -P.f.gamma), vs));
+        if (fl & kRectConfinement)
+            F = __dadd_rn(F, __dmul_rn(__dmul_rn(q, ax ? P.f.confine_y : P.f.confine_x), xs));
+        if (fl & kShieldedCoulomb) F = __dadd_rn(F, fpa);
+        if (fl & kThermal) {
+            const double2 t = stage_thermal(P, i);
+            F = __dadd_rn(F, ax ? t.y : t.x);
+        }
+        if (fo) {
+            (ax ? P.fy_out : P.fx_out)[c.orig[i]] = F;
+        } else {
+            const double dt = stage_dt(P);
+            const double k = __ddiv_rn(__dmul_rn(dt, F), m);
+            const double l = __dmul_rn(dt, vs);
+            const double x = X[i], v = V[i];
+            const bool last = (s == P.order);
+            double nv = 0.0;
+            if (last && s == 2) {  // Runge_Kutta2: x += l2, V += k2
+                na = __dadd_rn(x, l);
+                V[i] = __dadd_rn(v, k);
+                X[i] = na;
+            } else if (s == 1 || s == 2) {
+                double *const *acc = (s == 1) ? c.a1 : c.a23;
+                acc[2 * ax][i] = k;
+                acc[2 * ax + 1][i] = l;
+                na = __dadd_rn(__dmul_rn(0.5, l), x);
+                nv = __dadd_rn(__dmul_rn(0.5, k), v);
+            } else if (s == 3) {
+                c.a23[2 * ax][i] = __dadd_rn(c.a23[2 * ax][i], k);
+                c.a23[2 * ax + 1][i] = __dadd_rn(c.a23[2 * ax + 1][i], l);
+                na = __dadd_rn(x, l);
+                nv = __dadd_rn(v, k);
+            } else {
+                const double dv =
+                    __ddiv_rn(__dadd_rn(c.a1[2 * ax][i], __dadd_rn(__dmul_rn(c.a23[2 * ax][i], 2.0), k)), 6.0);
+                const double d =
+                    __ddiv_rn(__dadd_rn(c.a1[2 * ax + 1][i], __dadd_rn(__dmul_rn(c.a23[2 * ax + 1][i], 2.0), l)), 6.0);
+                na = __dadd_rn(x, d);
+                V[i] = __dadd_rn(v, dv);
+                X[i] = na;
+            }
+            (ax ? c.py : c.px)[b ^ 1][i] = na;
+            if (!last) (ax ? c.vyc : c.vxc)[i] = nv;
+            if (!isfinite(na)) atomicOr(c.err, 1);
+        }
+    }
+    if (fo) return;  // uniform over the launch
+    float h = 0.0f, lo = 0.0f;
+    if (live) split2(na, h, lo);
+    s_hi[ax][lane] = h;
+    s_lo[ax][lane] = lo;
+    __syncthreads();
+    const int bw = b ^ 1;
+    const float xh = s_hi[0][lane], yh = s_hi[1][lane];
+    if (live) {  // write_stage_position's packed words, one float4 per warp
+        const double q = c.q[i];
+        if (ax == 0)
+            c.pa[bw][i] = make_float4(xh, yh, fmaf(yh, yh, xh * xh), __double2float_rn(q));
+        else
+            c.pb[bw][i] = make_float4(s_lo[0][lane], s_lo[1][lane], -filter_threshold(xh, yh, c.rc2),
+                                      __double2float_rn(c.coulomb * q));
+    }
+    if (P.box_out && ax == 0) {  // the group's box in the buffer just written
+        float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+        if (live) {
+            x0 = x1 = xh;
+            y0 = y1 = yh;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+            y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+            x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+            y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        }
+        if (lane == 0 && i < c.n_pad) c.gbox[bw][blockIdx.x] = make_float4(x0, y0, x1, y1);
     }
     stage_step_advance(P);
 }

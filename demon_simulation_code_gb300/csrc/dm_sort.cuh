@@ -269,8 +269,8 @@ static __global__ void __launch_bounds__(kSortThreads) radix_scatter(
 
 // ---------------------------------------------------------------------------
 // One-launch sort for clouds of up to kSmallSortMax particles: a cluster of
-// kSortClusterCtas blocks, block r owning sorted positions [r*P, (r+1)*P),
-// P = kSmallSortMax / kSortClusterCtas.  Key box, keys, the three 8-bit LSD
+// CTAS blocks, block r owning sorted positions [r*P, (r+1)*P),
+// P = kSmallSortMax / CTAS.  Key box, keys, the three 8-bit LSD
 // passes and the gather of the cloud's arrays in the new order run in one
 // launch: per pass each block counts its digits per warp, the blocks'
 // digit totals meet through distributed shared memory, and every element is
@@ -279,7 +279,7 @@ static __global__ void __launch_bounds__(kSortThreads) radix_scatter(
 // (~0.1 ms at n = 16384); a single block was no better (one SM's issue rate).
 //
 // Element order: block r, warp w, round k, lane l is element
-// r*P + w*32*kSortClusterRounds + k*32 + l.  Digits are ranked in that order
+// r*P + w*32*R + k*32 + l (R = P / threads).  Digits are ranked in that order
 // (lanes with equal digits found by match_digit8) and bases are laid out
 // digit-major over (digit, block, warp), so the sort is stable and depends
 // only on the positions.  The key
@@ -289,15 +289,23 @@ static __global__ void __launch_bounds__(kSortThreads) radix_scatter(
 // ---------------------------------------------------------------------------
 constexpr int kSmallSortMax = 16384;
 constexpr int kErrSortPermutation = 8;  // error bit: the cluster sort's ranks were inconsistent
-constexpr int kSortClusterCtas = 8;  // portable cluster size
 constexpr int kSortClusterThreads = 512;
 constexpr int kSortClusterWarps = kSortClusterThreads / 32;
-constexpr int kSortClusterPer = kSmallSortMax / kSortClusterCtas;        // 2048 elements per block
-constexpr int kSortClusterRounds = kSortClusterPer / kSortClusterThreads;  // 4 per thread
 
+// CTAS blocks of PER elements, ROUNDS per thread: 8 (a portable cluster) or
+// 16 (non-portable; half the elements per SM)
+template <int CTAS>
+struct SortClusterShape {
+    static constexpr int per = kSmallSortMax / CTAS;
+    static constexpr int rounds = per / kSortClusterThreads;
+    static_assert(rounds * kSortClusterThreads == per, "whole rounds per thread");
+};
+
+template <int CTAS>
 struct SortClusterSmem {
-    uint32_t keys[2][kSortClusterPer];
-    uint16_t slot[2][kSortClusterPer];
+    static constexpr int kPer = SortClusterShape<CTAS>::per;
+    uint32_t keys[2][kPer];
+    uint16_t slot[2][kPer];
     uint32_t wcnt[kSortClusterWarps][kSortBuckets];  // per-warp digit counts, then offsets within the block
     uint32_t ctot[kSortBuckets];      // this block's digit totals (read by the whole cluster)
     uint32_t dbase[kSortBuckets];     // first sorted position of (digit, this block)
@@ -306,7 +314,8 @@ struct SortClusterSmem {
     float mom[kMomentFields];  // this block's moments (read by the whole cluster)
     float box[3];
 };
-constexpr size_t kSortClusterSmem = sizeof(SortClusterSmem);
+template <int CTAS>
+constexpr size_t sort_cluster_smem() { return sizeof(SortClusterSmem<CTAS>); }
 
 __device__ __forceinline__ void moments_f32_add(float *v, float4 a, float ox, float oy) {
     if (!(isfinite(a.x) && isfinite(a.y))) return;
@@ -334,11 +343,16 @@ __device__ __forceinline__ void moments_f32_merge(float *v, const float *o) {
 // at every step boundary).  perm (optional): new slot -> old slot.  The
 // cloud's x, y, vx, vy, q, m and orig are gathered in the new order into the
 // staging arrays of z (permute_commit_init copies them back).
-static __global__ void __cluster_dims__(kSortClusterCtas, 1, 1) __launch_bounds__(kSortClusterThreads, 1)
+// Launched as one cluster of CTAS blocks.
+template <int CTAS>
+static __global__ void __launch_bounds__(kSortClusterThreads, 1)
     sort_cluster(const float4 *__restrict__ pa0, CloudDev c, SortScratch z) {
+    constexpr int kSortClusterCtas = CTAS;
+    constexpr int kSortClusterPer = SortClusterShape<CTAS>::per;
+    constexpr int kSortClusterRounds = SortClusterShape<CTAS>::rounds;
     pdl_wait();
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    SortClusterSmem &S = *reinterpret_cast<SortClusterSmem *>(smem_raw);
+    SortClusterSmem<CTAS> &S = *reinterpret_cast<SortClusterSmem<CTAS> *>(smem_raw);
     cg::cluster_group cl = cg::this_cluster();
     const int r = (int)cl.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -352,8 +366,8 @@ static __global__ void __cluster_dims__(kSortClusterCtas, 1, 1) __launch_bounds_
         const int e = e0 + k * kSortClusterThreads + tid;
         pos[k] = (e < n) ? pa0[e] : make_float4(NAN, NAN, 0.0f, 0.0f);
     }
-    // moments of this block's slice, then of the cloud: lanes 0..7 of warp 0
-    // fetch the eight blocks' moments and merge them in a fixed butterfly
+    // moments of this block's slice, then of the cloud: lanes 0..CTAS-1 of warp 0
+    // fetch the cluster's blocks' moments and merge them in a fixed butterfly
     // (commutative steps), so every block derives the same key box
     const float4 p0 = pa0[0];
     const float ox = isfinite(p0.x) ? p0.x : 0.0f, oy = isfinite(p0.y) ? p0.y : 0.0f;
