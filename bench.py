@@ -597,10 +597,14 @@ def run_gb300(args, world, rank, local):
         wall = max_over_ranks(time.perf_counter() - t_a)
         el = max_over_ranks(a.elapsed_time(b) / 1e3)
         kernels = (local.K.ctx.launch_count() - al0) / args.adjoint_grads
-        # pair sweeps per gradient: 4 force sweeps per step forward, 4 per
-        # recomputed step and 4 VJP sweeps per step backward
-        sweeps = 12 * local.steps
+        # pair sweeps per gradient: 4 force sweeps per step forward and 4 VJP
+        # sweeps per step backward, plus 4 per recomputed step when the stage
+        # inputs are not kept
+        kept = bool(getattr(local.K, "kept_stages", False))
+        sweeps = (8 if kept else 12) * local.steps
         adjoint = {"workload": wa.name, "clouds": len(wa.clouds), "n": wa.clouds[0].n, "steps": local.steps,
+                   "stage_inputs": "kept from the forward pass" if kept else
+                                   f"recomputed from checkpoints every {local.every} steps",
                    "checkpoint_every": local.every, "precision": "fp32c",
                    "seconds_per_gradient": el / args.adjoint_grads,
                    "wall_seconds_per_gradient": wall / args.adjoint_grads,

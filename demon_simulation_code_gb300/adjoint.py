@@ -6,11 +6,15 @@ libdemon_gb300.so on the tensors' device memory: one fused launch per RK4
 stage forward (pair force, per-particle forces and stage algebra,
 ``dm_adjoint_rk4_step``) and one per stage backward (force VJP and the
 adjoint recurrences, ``dm_adjoint_rk4_step_vjp``), FP64 or FP32 pair terms
-with Kahan sums.  The forward pass keeps the state every
-``checkpoint_every`` steps; the backward pass recomputes each segment from
-its checkpoint, keeping the four stage inputs of every step of the segment,
-and walks the segment in reverse from them -- four force sweeps and four
-VJP sweeps per step on the way back, four force sweeps forward.
+with Kahan sums.  When gradients are wanted, the forward pass keeps the four
+stage inputs of every step (16 doubles per particle and step: 3.4 GB for
+64 x 2048 particles over 200 steps) as long as they fit the memory budget
+(``keep_stages``), and the backward pass walks the steps in reverse from
+them: four force sweeps per step forward, four VJP sweeps back.  Otherwise
+the forward pass keeps the state every ``checkpoint_every`` steps and the
+backward pass recomputes each segment from its checkpoint, keeping the
+segment's stage inputs -- four more force sweeps per step.  Both give the
+same bits (the forward step is deterministic).
 
 RK4 step (the reference's Runge_Kutta4.cpp:23-137, written for s = (x, y,
 vx, vy) and f(s) = (vx, vy, Fx/m, Fy/m)):
@@ -114,7 +118,11 @@ class AdjointKernels:
         return out  # gx, gy, gvx, gvy, gq_i, gkappa_i, gkc_i
 
     def per_cloud(self, v):
-        return torch.zeros(self.nclouds, dtype=v.dtype, device=v.device).index_add_(0, self.seg, v)
+        """Per-cloud sums of a per-particle tensor, in a fixed order (an
+        atomic scatter-add would round differently from call to call)."""
+        if len(set(self.ns)) == 1:
+            return v.view(self.nclouds, self.ns[0]).sum(dim=1)
+        return torch.stack([seg.sum() for seg in torch.split(v, self.ns)])
 
     def rk4_step(self, s, q, m, dt, stages=None):
         """One fused RK4 step of the state s = (x, y, vx, vy), in place;
@@ -146,13 +154,21 @@ class Rollout(torch.autograd.Function):
         K.set_params(kappa.detach().cpu().numpy(), kc.detach().cpu().numpy())
         q = qc.detach()[K.seg].contiguous()
         s = tuple(t.detach().clone().contiguous() for t in (x0, y0, vx0, vy0))
-        ckpts = []
-        for t in range(nsteps):
-            if t % every == 0:
-                ckpts.append(tuple(v.clone() for v in s))
-            K.rk4_step(s, q, m, dt)
+        ckpts, store = [], None
+        if any(ctx.needs_input_grad) and _keep_all_stages(meta["keep"], nsteps, s[0]):
+            store = torch.empty((nsteps, 16, s[0].numel()), dtype=torch.float64, device=s[0].device)
+            ckpts.append(tuple(v.clone() for v in s))
+            for t in range(nsteps):
+                K.rk4_step(s, q, m, dt, stages=store[t])
+        else:
+            for t in range(nsteps):
+                if t % every == 0:
+                    ckpts.append(tuple(v.clone() for v in s))
+                K.rk4_step(s, q, m, dt)
+        K.kept_stages = store is not None  # how the last differentiable rollout ran
         ctx.meta = meta
         ctx.ckpts = ckpts
+        ctx.store = store
         ctx.save_for_backward(kappa, qc, kc)
         return s
 
@@ -168,6 +184,11 @@ class Rollout(torch.autograd.Function):
         gq = torch.zeros_like(q)
         gk = torch.zeros_like(q)
         gc = torch.zeros_like(q)
+        if ctx.store is not None:  # every step's stage inputs kept by the forward pass
+            for t in range(nsteps - 1, -1, -1):
+                K.rk4_step_vjp(ctx.store[t], q, m, dt, lam, gq, gk, gc)
+            ctx.store = None
+            return (lam[0], lam[1], lam[2], lam[3], K.per_cloud(gk), K.per_cloud(gq), K.per_cloud(gc), None)
         store = torch.empty((min(every, nsteps), 16, ref.numel()), dtype=torch.float64, device=ref.device)
         for ci in range(len(ctx.ckpts) - 1, -1, -1):
             t0 = ci * every
@@ -180,6 +201,32 @@ class Rollout(torch.autograd.Function):
         return (lam[0], lam[1], lam[2], lam[3], K.per_cloud(gk), K.per_cloud(gq), K.per_cloud(gc), None)
 
 
-def rollout(K, x0, y0, vx0, vy0, kappa, qc, kc, m, dt, steps, checkpoint_every=20):
-    meta = {"kernels": K, "m": m, "dt": float(dt), "steps": int(steps), "every": int(checkpoint_every)}
+# Default memory budget for kept stage inputs: this many bytes, and at most a
+# quarter of the device memory free at the time.
+STAGE_BUDGET_BYTES = 16 << 30
+
+
+def stage_bytes(nsteps: int, total: int) -> int:
+    """Bytes of every step's four stage inputs (x, y, vx, vy each)."""
+    return int(nsteps) * 16 * int(total) * 8
+
+
+def _keep_all_stages(keep, nsteps, like) -> bool:
+    if keep is True or keep is False:
+        return keep
+    if keep != "auto":
+        raise ValueError("keep_stages must be True, False or 'auto'")
+    need = stage_bytes(nsteps, like.numel())
+    free, _ = torch.cuda.mem_get_info(like.device)
+    return need <= min(STAGE_BUDGET_BYTES, free // 4)
+
+
+def rollout(K, x0, y0, vx0, vy0, kappa, qc, kc, m, dt, steps, checkpoint_every=20, keep_stages="auto"):
+    """(x_T, y_T, vx_T, vy_T) after `steps` RK4 steps, differentiable with
+    respect to the start state and the per-cloud (kappa, q, k_c).
+    keep_stages: True keeps every step's stage inputs for the backward pass,
+    False recomputes them from checkpoints every `checkpoint_every` steps,
+    "auto" keeps them when they fit the memory budget.  Same gradients."""
+    meta = {"kernels": K, "m": m, "dt": float(dt), "steps": int(steps), "every": int(checkpoint_every),
+            "keep": keep_stages}
     return Rollout.apply(x0, y0, vx0, vy0, kappa, qc, kc, meta)

@@ -36,7 +36,7 @@ class TrajectoryFit:
     `norm` particles, by default this fit's own particle count)."""
 
     def __init__(self, workload, perturb: float | None = None, seed: int = 4, device=None,
-                 precision: str = "fp64", cloud_ids=None, norm: int | None = None):
+                 precision: str = "fp64", cloud_ids=None, norm: int | None = None, keep_stages="auto"):
         ids = list(range(len(workload.clouds))) if cloud_ids is None else [int(i) for i in cloud_ids]
         clouds = [workload.clouds[i] for i in ids]
         self.cloud_ids = ids
@@ -45,6 +45,7 @@ class TrajectoryFit:
         self.dt = float(workload.dt)
         self.steps = int(workload.steps)
         self.every = int(workload.extra.get("checkpoint_every", 20))
+        self.keep_stages = keep_stages
         perturb = float(workload.extra.get("perturb", 0.2) if perturb is None else perturb)
         dev = torch.device("cuda", torch.cuda.current_device() if device is None else int(device))
 
@@ -85,7 +86,7 @@ class TrajectoryFit:
 
     def _rollout(self, x0, kappa, q, kc, K=None):
         return rollout(self.K if K is None else K, x0, self.y0, self.vx0, self.vy0, kappa, q, kc, self.m,
-                       self.dt, self.steps, self.every)
+                       self.dt, self.steps, self.every, self.keep_stages)
 
     def per_cloud_loss(self, kappa, q, kc, x0=None, K=None):
         """[nclouds] tensor of L_c (their sum is the loss)."""

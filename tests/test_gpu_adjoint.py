@@ -194,6 +194,27 @@ def test_rollout_gradient_vs_finite_differences_and_torch(setup):
         assert (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item() < 1e-9
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_kept_stage_inputs_give_the_checkpointed_gradients(setup, prec):
+    """The backward pass from stage inputs kept by the forward pass and the
+    one that recomputes them from checkpoints give the same bits."""
+    from demon_simulation_code_gb300.adjoint import rollout
+
+    K64, ns, (x, y, vx, vy), m, kappa, kc, qc, K32 = setup
+    K = K64 if prec == "fp64" else K32
+    out = []
+    for keep in (True, False):
+        leaves = [t.clone().requires_grad_(True) for t in (x, vy, kappa, qc, kc)]
+        xT, yT, vxT, _ = rollout(K, leaves[0], y, vx, leaves[1], leaves[2], leaves[3], leaves[4], m, 1e-5,
+                                 23, 7, keep_stages=keep)
+        assert K.kept_stages is keep
+        L = ((xT - x - 1e-5) ** 2 + (yT - y) ** 2).mean() + 1e-3 * (vxT ** 2).mean()
+        L.backward()
+        out.append([t.grad.clone() for t in leaves] + [L.detach()])
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
+
+
 class _AdjointOnTrajectory(AdjointKernels):
     """Forward steps (and the backward pass's recomputed steps) in one
     precision, the step adjoints in another: separates the adjoint's own
