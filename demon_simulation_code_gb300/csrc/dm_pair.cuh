@@ -175,9 +175,10 @@ struct PairTuning {
 // ---------------------------------------------------------------------------
 template <int NW, int ILP, int TC>
 struct Fp32cSmem {
-    // j tile: TC 4-j chunks as structure of arrays (-xh, -yh, |p|^2) for the
-    // filter + (-xl, -yl, q, j) per j
-    static constexpr size_t tile = (size_t)TC * (3 * sizeof(float4) + 4 * sizeof(float4));
+    // j tile: TC 4-j chunks, each field of the 4 j in one 16-byte word
+    // (-xh, -yh, |p|^2, -xl, -yl, q, j): two consecutive j of a field load
+    // straight into the register pair a packed instruction takes
+    static constexpr size_t tile = (size_t)TC * 7 * sizeof(float4);
     static constexpr size_t cold = (size_t)ILP * 32 * sizeof(float4);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
@@ -233,8 +234,11 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
     float4 *s_x4 = reinterpret_cast<float4 *>(smem_raw);  // [TC] -xh of 4 j
     float4 *s_y4 = s_x4 + TC;                              // [TC] -yh
     float4 *s_b4 = s_y4 + TC;                              // [TC] xh^2 + yh^2
-    float4 *s_pj = s_b4 + TC;                              // [4*TC] (-xl, -yl, q, j)
-    float4 *s_cold = s_pj + 4 * TC;                        // [ILP][32] (xl, yl, -, i)
+    float4 *s_xl4 = s_b4 + TC;                             // [TC] -xl
+    float4 *s_yl4 = s_xl4 + TC;                            // [TC] -yl
+    float4 *s_q4 = s_yl4 + TC;                             // [TC] q
+    int4 *s_j4 = reinterpret_cast<int4 *>(s_q4 + TC);      // [TC] j (-1: padding)
+    float4 *s_cold = reinterpret_cast<float4 *>(s_j4 + TC);  // [ILP][32] (xl, yl, -, i)
     float4 *s_acc = s_cold + ILP * 32;                     // [NW][ILP][32]
     float4 *s_red = s_acc + NW * ILP * 32;                 // [TILE]
     int *s_glist = reinterpret_cast<int *>(s_red + TILE);  // [NT] surviving groups
@@ -295,6 +299,10 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
     for (int k = 0; k < ILP; k++) hits[k] = 0u;
     const float *s_xf = reinterpret_cast<const float *>(s_x4);
     const float *s_yf = reinterpret_cast<const float *>(s_y4);
+    const float *s_xlf = reinterpret_cast<const float *>(s_xl4);
+    const float *s_ylf = reinterpret_cast<const float *>(s_yl4);
+    const float *s_qf = reinterpret_cast<const float *>(s_q4);
+    const int *s_jf = reinterpret_cast<const int *>(s_j4);
     auto flush_hits = [&](int cbase) {
 #pragma unroll 1
         for (int k = 0; k < ILP; k++) {
@@ -316,22 +324,21 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
                 m &= m - 1u;
                 const int j0 = jbase + (e0 >> 2) * (4 * NW) + (e0 & 3);  // index into the tile's j
                 const int j1 = jbase + (e1 >> 2) * (4 * NW) + (e1 & 3);
-                const float4 B0 = s_pj[j0], B1 = s_pj[j1];
                 float2 dx, dy, r2, w;
                 pair2_terms(I, make_float2(s_xf[j0], s_xf[j1]), make_float2(s_yf[j0], s_yf[j1]),
-                            make_float2(B0.x, B1.x), make_float2(B0.y, B1.y), make_float2(B0.z, B1.z * q1), kap,
-                            nkl2e, dx, dy, r2, w);
-                const int g0 = __float_as_int(B0.w), g1 = __float_as_int(B1.w);
+                            make_float2(s_xlf[j0], s_xlf[j1]), make_float2(s_ylf[j0], s_ylf[j1]),
+                            make_float2(s_qf[j0], s_qf[j1] * q1), kap, nkl2e, dx, dy, r2, w);
+                const int g0 = s_jf[j0], g1 = s_jf[j1];
                 // certainly inside: r2 < rc2_lo; borderline pairs decided exactly
                 w.x = (r2.x < rc2_lo && g0 != ii) ? w.x : 0.0f;
                 w.y = (r2.y < rc2_lo && g1 != ii && q1 != 0.0f) ? w.y : 0.0f;
                 if (!(r2.x < rc2_lo) && r2.x < rc2_hi) {
                     float bx, by;
-                    w.x = border_pair(P, b, I, ii, s_xf[j0], s_yf[j0], B0.x, B0.y, B0.z, g0, bx, by);
+                    w.x = border_pair(P, b, I, ii, s_xf[j0], s_yf[j0], s_xlf[j0], s_ylf[j0], s_qf[j0], g0, bx, by);
                 }
                 if (q1 != 0.0f && !(r2.y < rc2_lo) && r2.y < rc2_hi) {
                     float bx, by;
-                    w.y = border_pair(P, b, I, ii, s_xf[j1], s_yf[j1], B1.x, B1.y, B1.z, g1, bx, by);
+                    w.y = border_pair(P, b, I, ii, s_xf[j1], s_yf[j1], s_xlf[j1], s_ylf[j1], s_qf[j1], g1, bx, by);
                 }
                 const float2 fx = mul2(w, dx), fy = mul2(w, dy);
                 kahan_add(acc.x, acc.z, fx.x + fx.y);
@@ -347,22 +354,28 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
     // the same 4 j, the cutoff taken by a select (pairs within 4e-6 of it in
     // r^2 decided exactly, j == i excluded); the chunk's terms summed plainly
     // and added to the slot's compensated sums.
+    const int tile_j0 = tile * TILE;  // the tile's own particles: the only chunks that can hold j == i
     auto direct_chunk = [&](int c, int k) {
         int ii;
         const PairI I = slot_i(k, ii);
-        const float4 X = s_x4[c], Y = s_y4[c];
-        const float4 B0 = s_pj[4 * c], B1 = s_pj[4 * c + 1], B2 = s_pj[4 * c + 2], B3 = s_pj[4 * c + 3];
+        const float4 X = s_x4[c], Y = s_y4[c], XL = s_xl4[c], YL = s_yl4[c], Q = s_q4[c];
         float2 dx, dy, r2, w, dx2, dy2, r22, w2;
-        pair2_terms(I, make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(B0.x, B1.x),
-                    make_float2(B0.y, B1.y), make_float2(B0.z, B1.z), kap, nkl2e, dx, dy, r2, w);
-        pair2_terms(I, make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(B2.x, B3.x),
-                    make_float2(B2.y, B3.y), make_float2(B2.z, B3.z), kap, nkl2e, dx2, dy2, r22, w2);
-        const int g0 = __float_as_int(B0.w), g1 = __float_as_int(B1.w);
-        const int g2 = __float_as_int(B2.w), g3 = __float_as_int(B3.w);
-        w.x = (r2.x < rc2_lo && g0 != ii) ? w.x : 0.0f;
-        w.y = (r2.y < rc2_lo && g1 != ii) ? w.y : 0.0f;
-        w2.x = (r22.x < rc2_lo && g2 != ii) ? w2.x : 0.0f;
-        w2.y = (r22.y < rc2_lo && g3 != ii) ? w2.y : 0.0f;
+        pair2_terms(I, make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(XL.x, XL.y),
+                    make_float2(YL.x, YL.y), make_float2(Q.x, Q.y), kap, nkl2e, dx, dy, r2, w);
+        pair2_terms(I, make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(XL.z, XL.w),
+                    make_float2(YL.z, YL.w), make_float2(Q.z, Q.w), kap, nkl2e, dx2, dy2, r22, w2);
+        if ((unsigned)(s_jf[4 * c] - tile_j0) < (unsigned)TILE) {  // warp-uniform: this tile's own chunk
+            const int4 J = s_j4[c];
+            w.x = (r2.x < rc2_lo && J.x != ii) ? w.x : 0.0f;
+            w.y = (r2.y < rc2_lo && J.y != ii) ? w.y : 0.0f;
+            w2.x = (r22.x < rc2_lo && J.z != ii) ? w2.x : 0.0f;
+            w2.y = (r22.y < rc2_lo && J.w != ii) ? w2.y : 0.0f;
+        } else {
+            w.x = (r2.x < rc2_lo) ? w.x : 0.0f;
+            w.y = (r2.y < rc2_lo) ? w.y : 0.0f;
+            w2.x = (r22.x < rc2_lo) ? w2.x : 0.0f;
+            w2.y = (r22.y < rc2_lo) ? w2.y : 0.0f;
+        }
         const bool bd = (!(r2.x < rc2_lo) && r2.x < rc2_hi) || (!(r2.y < rc2_lo) && r2.y < rc2_hi) ||
                         (!(r22.x < rc2_lo) && r22.x < rc2_hi) || (!(r22.y < rc2_lo) && r22.y < rc2_hi);
         float2 fx = fma2(w2, dx2, mul2(w, dx));
@@ -373,10 +386,9 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
                 const float rr = (u == 0) ? r2.x : (u == 1) ? r2.y : (u == 2) ? r22.x : r22.y;
                 if (rr < rc2_lo || !(rr < rc2_hi)) continue;
                 const int jj = 4 * c + u;
-                const float4 Bj = s_pj[jj];
                 float bx, by;
-                const float wb = border_pair(P, b, I, ii, s_xf[jj], s_yf[jj], Bj.x, Bj.y, Bj.z,
-                                             __float_as_int(Bj.w), bx, by);
+                const float wb = border_pair(P, b, I, ii, s_xf[jj], s_yf[jj], s_xlf[jj], s_ylf[jj], s_qf[jj],
+                                             s_jf[jj], bx, by);
                 fx.x = fmaf(wb, bx, fx.x);
                 fy.x = fmaf(wb, by, fy.x);
             }
@@ -398,6 +410,9 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
         for (int e = tid; e < tcn; e += NT) {
             const int jb = 4 * chunk_of(q0 + e);  // first j of the chunk
             float xs[4], ys[4], bs[4];
+            float *xl = reinterpret_cast<float *>(s_xl4 + e), *yl = reinterpret_cast<float *>(s_yl4 + e);
+            float *qs = reinterpret_cast<float *>(s_q4 + e);
+            int *js = reinterpret_cast<int *>(s_j4 + e);
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 if (jb + u < n) {
@@ -406,12 +421,16 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
                     xs[u] = -A.x;
                     ys[u] = -A.y;
                     bs[u] = A.z;
-                    s_pj[4 * e + u] = make_float4(-B.x, -B.y, A.w, __int_as_float(jb + u));
+                    xl[u] = -B.x;
+                    yl[u] = -B.y;
+                    qs[u] = A.w;
+                    js[u] = jb + u;
                 } else {  // padding: never passes the filter; a finite, zero term
                     xs[u] = -kPadPosition;
                     ys[u] = -kPadPosition;
                     bs[u] = INFINITY;
-                    s_pj[4 * e + u] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+                    xl[u] = yl[u] = qs[u] = 0.0f;
+                    js[u] = -1;
                 }
             }
             s_x4[e] = make_float4(xs[0], xs[1], xs[2], xs[3]);
@@ -436,17 +455,16 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
             }
             int ng = 0;
             for (int c = warp; c < tcn; c += NW) {
-                const float4 X = s_x4[c], Y = s_y4[c];
-                const float4 B0 = s_pj[4 * c], B1 = s_pj[4 * c + 1], B2 = s_pj[4 * c + 2], B3 = s_pj[4 * c + 3];
+                const float4 X = s_x4[c], Y = s_y4[c], XL = s_xl4[c], YL = s_yl4[c], Q = s_q4[c];
 #pragma unroll
                 for (int k = 0; k < ILP; k++) {
                     float2 dx, dy, r2, w;
-                    pair2_terms(I[k], make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(B0.x, B1.x),
-                                make_float2(B0.y, B1.y), make_float2(B0.z, B1.z), kap, nkl2e, dx, dy, r2, w);
+                    pair2_terms(I[k], make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(XL.x, XL.y),
+                                make_float2(YL.x, YL.y), make_float2(Q.x, Q.y), kap, nkl2e, dx, dy, r2, w);
                     fx[k] = fma2(w, dx, fx[k]);
                     fy[k] = fma2(w, dy, fy[k]);
-                    pair2_terms(I[k], make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(B2.x, B3.x),
-                                make_float2(B2.y, B3.y), make_float2(B2.z, B3.z), kap, nkl2e, dx, dy, r2, w);
+                    pair2_terms(I[k], make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(XL.z, XL.w),
+                                make_float2(YL.z, YL.w), make_float2(Q.z, Q.w), kap, nkl2e, dx, dy, r2, w);
                     fx[k] = fma2(w, dx, fx[k]);
                     fy[k] = fma2(w, dy, fy[k]);
                 }
