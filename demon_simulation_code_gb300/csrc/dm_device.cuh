@@ -10,7 +10,7 @@
 //                    epilogue writes the next stage's positions into b^1:
 //                      px[b], py[b]  FP64 (CacheOperator's xCache/yCache)
 //                      pa[b] = (xh, yh, xh^2+yh^2, (float)q)  float4
-//                      pb[b] = (xl, yl, -threshold, C*q)      float4
+//                      pb[b] = (xl, yl, -threshold, 0)        float4
 //                    (threshold = the FP32 pair filter's bound, see
 //                    filter_threshold; computed once per particle here
 //                    instead of in every CTA that reads the particle)
@@ -282,15 +282,19 @@ __device__ __forceinline__ void split2(double x, float &hi, float &lo) {
 // margin, evaluated in FP32 on the hi parts.  The margin 2^-17 (|p_i| + rc)^2
 // is ~10x the worst FP32 rounding of that expanded form plus the hi/lo split
 // error for any pair within rc of i, so no pair the reference keeps is
-// filtered out.  Rounded up.  |p_i| + rc is formed from FP32 square roots
-// with every operation rounded up (an upper bound, so the margin only grows):
-// two FP64 square roots per particle per stage cost more than the rest of
-// this function at GB300's FP64 rate.
+// filtered out.  Evaluated in FP32 with every operation rounded in the
+// direction that keeps the result an upper bound of the exact value of
+// rc^2 - |p_i|^2 + 2^-17 (|p_i| + rc)^2 (|p_i|^2 rounded down where it is
+// subtracted, up where it feeds the margin), so the bound can only be
+// looser, by a few FP32 ulps of |p_i|^2 -- ~1% of the margin.  GB300 runs
+// FP64 at ~1/64 of the FP32 rate: one conversion is the only FP64 operation.
 __device__ __forceinline__ float filter_threshold(float xh, float yh, double rc2) {
-    const double a2 = (double)xh * xh + (double)yh * yh;
-    const float pf = __fadd_ru(__fsqrt_ru(__double2float_ru(a2)), __fsqrt_ru(__double2float_ru(rc2)));
-    const double pr = (double)pf;
-    return __double2float_ru(rc2 - a2 + 7.62939453125e-6 * pr * pr);
+    const float rcf = __double2float_ru(rc2);                  // >= rc^2
+    const float a2_dn = __fmaf_rd(xh, xh, __fmul_rd(yh, yh));  // <= |p_i|^2
+    const float a2_up = __fmaf_ru(xh, xh, __fmul_ru(yh, yh));  // >= |p_i|^2
+    const float pf = __fadd_ru(__fsqrt_ru(a2_up), __fsqrt_ru(rcf));  // >= |p_i| + rc
+    const float margin = __fmul_ru(__fmul_ru(pf, pf), 7.62939453125e-6f);
+    return __fadd_ru(__fsub_ru(rcf, a2_dn), margin);
 }
 
 // Programmatic dependent launch: a kernel launched with the programmatic-
@@ -317,8 +321,7 @@ __device__ __forceinline__ void write_stage_position(const CloudDev &c, int b, i
     split2(ys, yh, yl);
     const double q = c.q[i];
     c.pa[b][i] = make_float4(xh, yh, fmaf(yh, yh, xh * xh), __double2float_rn(q));
-    c.pb[b][i] = make_float4(xl, yl, -filter_threshold(xh, yh, c.rc2),
-                             __double2float_rn(c.coulomb * q));
+    c.pb[b][i] = make_float4(xl, yl, -filter_threshold(xh, yh, c.rc2), 0.0f);
 }
 
 // Reference cutoff decision for one pair, bit for bit:
