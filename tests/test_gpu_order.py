@@ -72,3 +72,42 @@ def test_batch_per_cloud_sort_is_a_permutation(gpu_ctx, oracle_lib):
         for a, r in zip(g, ref):
             assert np.array_equal(a, r)
     b.close()
+
+
+@pytest.mark.parametrize("n", [1, 2049, 16384])
+def test_eight_block_cluster_sort_is_a_permutation(monkeypatch, oracle_lib, n):
+    """The portable 8-block cluster sort (DM_SORT_CLUSTER_CTAS=8, read by a
+    context at its first re-sort) keeps the trajectory exact too."""
+    from demon_simulation_code_gb300 import Context
+
+    monkeypatch.setenv("DM_SORT_CLUSTER_CTAS", "8")
+    ctx = Context(0)
+    c0 = free_cloud(n, 500 + n)
+    c = DeviceCloud.from_cloud(ctx, c0)
+    c.step(3, DT, "fp64")
+    got = c.download()
+    p = oracle.make_params(**c0.params())
+    ref = oracle_lib.rk4_fixed(c0.x, c0.y, c0.vx, c0.vy, c0.q, c0.m, p, DT, 3)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    c.close()
+
+
+def test_two_axis_finish_gives_the_per_particle_finish_bits(gpu_ctx):
+    """Clouds with only the axis-separable forces complete each stage with
+    one thread per particle and axis; adding a zero gravitational force
+    routes the same arithmetic through the one-thread-per-particle finish.
+    The two must agree bit for bit."""
+    base = W.disk16k().clouds[0]
+    runs = []
+    for extra_flags in (0, W.GRAVITATIONAL):
+        c0 = base.copy()
+        c0.flags = base.flags | extra_flags
+        c0.extra = dict(base.extra, gravity=0.0)
+        c = DeviceCloud.from_cloud(gpu_ctx, c0)
+        c.set_kernel("fp32c<4,2,128,false,cull>", 16)
+        c.step(3, 1e-4, "fp32c")
+        runs.append(c.download())
+        c.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
