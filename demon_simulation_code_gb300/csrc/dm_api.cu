@@ -158,6 +158,21 @@ int direct_min_hits() {
     return v;
 }
 
+// StageParams::near_direct_f2: groups whose farthest separation from the
+// tile is within F = 1.6 r_c are evaluated without the filter (measured on
+// disk16k: the collapsed-state launch 154.8 -> 146.0 us, the densest step
+// -7%, calm steps +1%; 1.3-2.5 within 1% of each other).
+// DM_NEAR_DIRECT_F overrides F (0 turns the class off; at most 4).
+float near_direct_f2() {
+    static const float v = [] {
+        const char *e = getenv("DM_NEAR_DIRECT_F");
+        double f = e ? atof(e) : 1.6;
+        if (!(f >= 0.0 && f <= 4.0)) f = 0.0;
+        return (float)(f * f);
+    }();
+    return v;
+}
+
 // kappa*log2(e) as a float pair (hi + lo to ~2^-48 relative).
 void kappa_log2e(double kappa, float &hi, float &lo) {
     const double k = kappa * 1.4426950408889634;
@@ -188,6 +203,7 @@ StageParams make_stage_params(dm_cloud *c, int stage, int mode, double dt, const
     P.kappa_f = (float)kappa;
     P.nkl2e = (float)(-kappa * 1.4426950408889634);
     P.direct_min = direct_min_hits();
+    P.near_direct_f2 = near_direct_f2();
     return P;
 }
 
@@ -1426,6 +1442,7 @@ int batch_launch_stage(dm_batch *B, int stage, int mode, double dt, int fo_buf =
     P.fx_out = B->d_fx;
     P.fy_out = B->d_fy;
     P.direct_min = direct_min_hits();
+    P.near_direct_f2 = near_direct_f2();
     const int slot = (mode == kModeForceOnly) ? 0 : stage - 1;
     if (k.cull) {  // group boxes of the buffer this stage reads
         const int br = (mode == kModeForceOnly) ? fo_buf : (stage - 1) & 1;

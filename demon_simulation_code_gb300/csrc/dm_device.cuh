@@ -122,6 +122,10 @@ struct StageParams {
     // this many of the 128 (lane, j) pairs of a slot is evaluated directly
     // (all lanes, cutoff by a select) instead of through per-lane hit bits
     int direct_min;
+    // culling: a near group whose farthest separation from the tile is
+    // within sqrt(near_direct_f2) r_c skips the filter (every chunk
+    // evaluated directly); 0: no such class
+    float near_direct_f2;
     // j split without clusters: rank r of tile t is block t*split + r and
     // writes its partial sums (s, c) of particle i to the float2 planes
     // partial[(2r + axis)*n_pad + i]; stage_finish sums them

@@ -182,8 +182,9 @@ struct Fp32cSmem {
     static constexpr size_t cold = (size_t)ILP * 32 * sizeof(float4);
     static constexpr size_t acc = (size_t)NW * ILP * 32 * sizeof(float4);
     static constexpr size_t red = (size_t)ILP * 32 * sizeof(float4);
-    // culling: near and inside group lists (NT each) and their per-warp counts
-    static constexpr size_t glist = 2 * ((size_t)NW * 32 * sizeof(int) + NW * sizeof(int));
+    // culling: near, inside and mostly-inside group lists (NT each) and
+    // their per-warp counts
+    static constexpr size_t glist = 3 * ((size_t)NW * 32 * sizeof(int) + NW * sizeof(int));
     static constexpr size_t bytes = tile + cold + acc + red + glist;
     // s_red, in float4 units from the start of shared memory
     static constexpr size_t red_offset = (tile + cold + acc) / sizeof(float4);
@@ -402,8 +403,12 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
     // Sweeps the `count` chunks (4 consecutive j) of this CTA's list through
     // shared-memory tiles; chunk_of(q) is the cloud chunk index of entry q.
     // Within a tile, chunk c goes to warp c % NW.
-    auto sweep = [&](int count, auto chunk_of, auto dense_tag) {
-    constexpr bool DENSE = decltype(dense_tag)::value;
+    // MODE 0: the packed filter, then direct chunks or hit bits; 1: groups
+    // entirely inside the cutoff; 2: groups mostly inside it, every chunk
+    // evaluated directly with the cutoff taken by a select (no filter)
+    auto sweep = [&](int count, auto chunk_of, auto mode_tag) {
+    constexpr int MODE = decltype(mode_tag)::value;
+    constexpr bool DENSE = MODE == 1;
     for (int q0 = 0; q0 < count; q0 += TC) {
         const int tcn = min(TC, count - q0);
         __syncthreads();
@@ -484,6 +489,11 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
                 kahan_add(acc[k].y, acc[k].w, fy[k].x + fy[k].y);
                 my_acc[k * 32 + lane] = acc[k];
             }
+        } else if constexpr (MODE == 2) {
+            for (int c = warp; c < tcn; c += NW) {
+#pragma unroll 1
+                for (int k = 0; k < ILP; k++) direct_chunk(c, k);
+            }
         } else {
         // one flush site: the loop runs one step past the tile's last chunk
         int nb = 0, cbase = warp;  // chunks recorded in hits, chunk of bit group 0
@@ -544,7 +554,7 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
         // rank (and every warp) samples the whole cloud evenly
         const int nch_all = (n + 3) >> 2;
         const int my_nch = (nch_all - rank + S - 1) / S;  // chunks of this rank
-        sweep(my_nch, [&](int q) { return q * S + rank; }, std::false_type{});
+        sweep(my_nch, [&](int q) { return q * S + rank; }, std::integral_constant<int, 0>{});
     } else {
         // 32-particle groups dealt round-robin to ranks; a group whose box is
         // beyond the cutoff from the tile's box is skipped whole (it holds no
@@ -561,40 +571,54 @@ __device__ __forceinline__ void fp32c_sweep(const StageParams &P, int tile, int 
         }
         const int my_ng = (ngroups - rank + S - 1) / S;
         unsigned long long swept = 0ull;
-        int *s_glist2 = s_wcount + NW;  // [NT] groups entirely inside the cutoff
+        int *s_glist2 = s_wcount + NW;   // [NT] groups entirely inside the cutoff
         int *s_wcount2 = s_glist2 + NT;  // [NW]
+        int *s_glist3 = s_wcount2 + NW;  // [NT] groups mostly inside it
+        int *s_wcount3 = s_glist3 + NT;  // [NW]
+        const float rc2_mostly = P.rc2_lo * P.near_direct_f2;  // 0: no such class
         for (int t0 = 0; t0 < my_ng; t0 += NT) {
             const int t = t0 + tid;
             const int g = t * S + rank;
-            bool near = false, inside = false;
+            bool near = false, inside = false, mostly = false;
             if (t < my_ng) {
                 const float4 gbox = gb[g];
                 near = boxes_near(tb, gbox, P.rc2_hi);
-                // the tile's own groups hold the pairs j == i: filtered path
+                // the tile's own groups hold the pairs j == i: not "inside"
                 inside = near && g / ILP != tile && boxes_inside(tb, gbox, P.rc2_lo);
+                // farthest separation within sqrt(near_direct_f2) r_c: most
+                // pairs pass the filter, so it is skipped
+                mostly = near && !inside && rc2_mostly > 0.0f && boxes_inside(tb, gbox, rc2_mostly);
             }
-            const uint32_t bal = __ballot_sync(0xffffffffu, near && !inside);
+            const uint32_t bal = __ballot_sync(0xffffffffu, near && !inside && !mostly);
             const uint32_t bal2 = __ballot_sync(0xffffffffu, inside);
+            const uint32_t bal3 = __ballot_sync(0xffffffffu, mostly);
             if (lane == 0) {
                 s_wcount[warp] = __popc(bal);
                 s_wcount2[warp] = __popc(bal2);
+                s_wcount3[warp] = __popc(bal3);
             }
             __syncthreads();
-            int off = 0, total = 0, off2 = 0, total2 = 0;
+            int off = 0, total = 0, off2 = 0, total2 = 0, off3 = 0, total3 = 0;
 #pragma unroll
             for (int w = 0; w < NW; w++) {
-                const int cw = s_wcount[w], cw2 = s_wcount2[w];
+                const int cw = s_wcount[w], cw2 = s_wcount2[w], cw3 = s_wcount3[w];
                 off += (w < warp) ? cw : 0;
                 off2 += (w < warp) ? cw2 : 0;
+                off3 += (w < warp) ? cw3 : 0;
                 total += cw;
                 total2 += cw2;
+                total3 += cw3;
             }
             const uint32_t below = (1u << lane) - 1u;
-            if (near && !inside) s_glist[off + __popc(bal & below)] = g;
+            if (near && !inside && !mostly) s_glist[off + __popc(bal & below)] = g;
             if (inside) s_glist2[off2 + __popc(bal2 & below)] = g;
-            sweep(8 * total, [&](int q) { return 8 * s_glist[q >> 3] + (q & 7); }, std::false_type{});
-            sweep(8 * total2, [&](int q) { return 8 * s_glist2[q >> 3] + (q & 7); }, std::true_type{});
-            swept += (unsigned long long)(total + total2);
+            if (mostly) s_glist3[off3 + __popc(bal3 & below)] = g;
+            sweep(8 * total, [&](int q) { return 8 * s_glist[q >> 3] + (q & 7); }, std::integral_constant<int, 0>{});
+            sweep(8 * total2, [&](int q) { return 8 * s_glist2[q >> 3] + (q & 7); },
+                  std::integral_constant<int, 1>{});
+            sweep(8 * total3, [&](int q) { return 8 * s_glist3[q >> 3] + (q & 7); },
+                  std::integral_constant<int, 2>{});
+            swept += (unsigned long long)(total + total2 + total3);
             __syncthreads();  // the lists and counts are reused by the next batch
         }
         if (tid == 0 && swept) atomicAdd(P.c.eval_pairs, swept * 32ull * (unsigned long long)TILE);
