@@ -636,7 +636,7 @@ def run_gb300(args, world, rank, local):
             else:
                 cpu1 = rec
 
-    # roofline of the dominant kernel (fused pair + stage, FP32 pipe bound)
+    # roofline of the dominant kernel (the pair launch; FP32 pipe bound)
     peak = ctx.probe_peak("fp32")
     avg_launch_s = pair_ms / 1e3 / max(launches, 1)
     achieved = FLOPS_PER_PAIR * n * (n - 1) / avg_launch_s / 1e12
@@ -675,8 +675,9 @@ def run_gb300(args, world, rank, local):
                          "traffic": traffic,
                          "flops_per_pair": FLOPS_PER_PAIR,
                          "avg_launch_us": avg_launch_s * 1e6,
-                         "launch_timing": "CUDA events around each pair launch, on the bit-identical "
-                                          "replay of the window (L2 flushed before each step)",
+                         "launch_timing": "CUDA events around each pair kernel launch alone (the stage "
+                                          "finish launch outside them), on the bit-identical replay of "
+                                          "the window (L2 flushed before each step)",
                          # box culling skips pair groups out of reach: the work the
                          # kernel actually swept, and the pipe fraction on that work
                          "swept_pair_fraction": swept_frac,

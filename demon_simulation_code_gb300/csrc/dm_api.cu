@@ -437,8 +437,28 @@ int launch_variant(dm_cloud *c, int vi, int S, int stage, int mode, double dt, c
         ctx->launches++;
         c->boxes_valid[br] = true;
     }
+    // profiling (dm_ctx_profile_enable): CUDA events around the pair launch
+    // alone (a cluster variant's launch includes its epilogue)
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ctx->prof) {
+        if (ctx->prof_used == ctx->prof_events.size()) {
+            cudaEvent_t a, b;
+            DM_CUDA(ctx, cudaEventCreate(&a));
+            DM_CUDA(ctx, cudaEventCreate(&b));
+            ctx->prof_events.push_back({a, b});
+        }
+        e0 = ctx->prof_events[ctx->prof_used].first;
+        e1 = ctx->prof_events[ctx->prof_used].second;
+        ctx->prof_used++;
+        DM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+    }
     DM_CUDA(ctx, k.launch(&cfg, P));
     ctx->launches++;
+    if (ctx->prof) {
+        DM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        ctx->prof_launches++;
+        ctx->prof_pairs += (double)c->n * (double)(c->n - 1);
+    }
     if (!k.cluster) {
         // stage_finish also writes the group boxes of the buffer the stage writes
         P.box_out = (mode != kModeForceOnly) ? 1 : 0;
@@ -468,27 +488,7 @@ int launch_stage(dm_cloud *c, int precision, int stage, int mode, double dt, con
     }
     const int vi = c->tuned_variant[pi];
     const int S = c->split[pi];
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (ctx->prof) {
-        if (ctx->prof_used == ctx->prof_events.size()) {
-            cudaEvent_t a, b;
-            DM_CUDA(ctx, cudaEventCreate(&a));
-            DM_CUDA(ctx, cudaEventCreate(&b));
-            ctx->prof_events.push_back({a, b});
-        }
-        e0 = ctx->prof_events[ctx->prof_used].first;
-        e1 = ctx->prof_events[ctx->prof_used].second;
-        ctx->prof_used++;
-        DM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
-    }
-    rc = launch_variant(c, vi, S, stage, mode, dt, dt_dev);
-    if (rc) return rc;
-    if (ctx->prof) {
-        DM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
-        ctx->prof_launches++;
-        ctx->prof_pairs += (double)c->n * (double)(c->n - 1);
-    }
-    return DM_OK;
+    return launch_variant(c, vi, S, stage, mode, dt, dt_dev);
 }
 
 // Autotuner: times every variant of this precision over a set of splits on
