@@ -616,7 +616,7 @@ int reorder(dm_cloud *c) {
     const int grid = (n + 255) / 256;
     SortScratch &z = c->sort;
     int cur = 0;
-    if (n <= kSmallSortMax) {  // one cluster launch sorts and gathers; one more commits
+    if (n <= kSmallSortMax) {  // one cluster launch sorts and rewrites the cloud in place
         int rc = choose_sort_ctas(ctx);
         if (rc) return rc;
         cudaLaunchAttribute attr[2];
@@ -628,11 +628,10 @@ int reorder(dm_cloud *c) {
             const cudaLaunchConfig_t cfg = sort_cluster_cfg<8>(s, attr);
             DM_CUDA(ctx, cudaLaunchKernelEx(&cfg, sort_cluster<8>, pa0, c->d, z));
         }
-        DM_CUDA(ctx, launch_pdl(permute_commit_init, dim3((c->n_pad + 255) / 256), dim3(256), 0, s, c->d, z));
-        c->boxes_valid[0] = true;  // written by permute_commit_init
+        c->boxes_valid[0] = true;  // written by sort_cluster
         c->boxes_valid[1] = false;
         DM_CUDA(ctx, cudaGetLastError());
-        ctx->launches += 2;
+        ctx->launches += 1;
         c->order_dirty = false;
         return DM_OK;
     } else {

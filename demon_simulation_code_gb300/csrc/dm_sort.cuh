@@ -340,9 +340,8 @@ __device__ __forceinline__ void moments_f32_merge(float *v, const float *o) {
 }
 
 // pa0: the FP32 hi parts of the current positions (stage buffer 0 holds them
-// at every step boundary).  perm (optional): new slot -> old slot.  The
-// cloud's x, y, vx, vy, q, m and orig are gathered in the new order into the
-// staging arrays of z (permute_commit_init copies them back).
+// at every step boundary).  The cloud's x, y, vx, vy, q, m and orig end up in
+// the new order, with stage buffer 0 and the group boxes rewritten.
 // Launched as one cluster of CTAS blocks.
 template <int CTAS>
 static __global__ void __launch_bounds__(kSortClusterThreads, 1)
@@ -520,8 +519,8 @@ static __global__ void __launch_bounds__(kSortClusterThreads, 1)
         cur ^= 1;
     }
 
-    // gather: new slot s takes old slot S.slot[cur][s - e0]; every load is
-    // issued before any store (the arrays do not alias)
+    // gather: new slot s takes old slot S.slot[cur][s - e0]; plain loads (the
+    // arrays are overwritten in place below), all issued before any store
     int src[kSortClusterRounds];
 #pragma unroll
     for (int k = 0; k < kSortClusterRounds; k++) {
@@ -533,24 +532,56 @@ static __global__ void __launch_bounds__(kSortClusterThreads, 1)
         }
         src[k] = o;
     }
-    const double *__restrict__ in[6] = {c.x, c.y, c.vx, c.vy, c.q, c.m};
+    const double *in[6] = {c.x, c.y, c.vx, c.vy, c.q, c.m};
     double val[6][kSortClusterRounds];
     int ov[kSortClusterRounds];
 #pragma unroll
     for (int k = 0; k < kSortClusterRounds; k++) {
         const bool ok = e0 + k * kSortClusterThreads + tid < n;
 #pragma unroll
-        for (int a = 0; a < 6; a++) val[a][k] = ok ? __ldg(in[a] + src[k]) : 0.0;
-        ov[k] = ok ? __ldg(c.orig + src[k]) : 0;
+        for (int a = 0; a < 6; a++) val[a][k] = ok ? in[a][src[k]] : 0.0;
+        ov[k] = ok ? c.orig[src[k]] : 0;
     }
+    // Every block of the cluster holds its sources in registers, and the
+    // cluster barrier orders those loads before any block's stores.  The
+    // cluster covers every slot of the cloud, so the cloud's arrays are
+    // rewritten in place in the new order, with stage buffer 0 (the first
+    // stage's inputs), the padding slots and the 32-particle group boxes.
+    cl.sync();
 #pragma unroll
     for (int k = 0; k < kSortClusterRounds; k++) {
-        const int s = e0 + k * kSortClusterThreads + tid;
+        const int s = e0 + k * kSortClusterThreads + tid;  // a warp holds 32 consecutive slots
+        float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
         if (s < n) {
-#pragma unroll
-            for (int a = 0; a < 6; a++) z.stage[a][s] = val[a][k];
-            z.orig_stage[s] = ov[k];
+            const double x = val[0][k], y = val[1][k];
+            c.x[s] = x;
+            c.y[s] = y;
+            c.vx[s] = val[2][k];
+            c.vy[s] = val[3][k];
+            c.q[s] = val[4][k];
+            c.m[s] = val[5][k];
+            c.orig[s] = ov[k];
+            write_stage_position(c, 0, s, x, y);
+            x0 = x1 = __double2float_rn(x);  // the hi parts write_stage_position stored
+            y0 = y1 = __double2float_rn(y);
+        } else if (s < c.n_pad) {
+            for (int b = 0; b < 2; b++) {
+                c.px[b][s] = (double)kPadPosition;
+                c.py[b][s] = (double)kPadPosition;
+                c.pa[b][s] = make_float4(kPadPosition, kPadPosition, kPadPosition * kPadPosition, 0.0f);
+                c.pb[b][s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            c.q[s] = 0.0;
+            c.m[s] = 1.0;
         }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+            y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+            x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+            y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+        }
+        if (lane == 0 && s < c.n_pad) c.gbox[0][s >> 5] = make_float4(x0, y0, x1, y1);
     }
 }
 
@@ -581,47 +612,6 @@ static __global__ void permute_commit(CloudDev c, SortScratch z) {
     c.q[s] = z.stage[4][s];
     c.m[s] = z.stage[5][s];
     c.orig[s] = z.orig_stage[s];
-}
-
-// permute_commit and init_positions in one launch: copy the gathered arrays
-// back, write stage buffer 0 from the new positions and the boxes of its
-// 32-particle groups (each warp is one group; as group_bounds computes them).
-static __global__ void permute_commit_init(CloudDev c, SortScratch z) {
-    pdl_wait();
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= c.n_pad) return;  // whole warps: n_pad is a multiple of 64
-    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
-    if (s < c.n) {
-        const double x = z.stage[0][s], y = z.stage[1][s];
-        c.x[s] = x;
-        c.y[s] = y;
-        c.vx[s] = z.stage[2][s];
-        c.vy[s] = z.stage[3][s];
-        c.q[s] = z.stage[4][s];
-        c.m[s] = z.stage[5][s];
-        c.orig[s] = z.orig_stage[s];
-        write_stage_position(c, 0, s, x, y);
-        const float4 A = c.pa[0][s];
-        x0 = x1 = A.x;
-        y0 = y1 = A.y;
-    } else {
-        for (int b = 0; b < 2; b++) {
-            c.px[b][s] = (double)kPadPosition;
-            c.py[b][s] = (double)kPadPosition;
-            c.pa[b][s] = make_float4(kPadPosition, kPadPosition, kPadPosition * kPadPosition, 0.0f);
-            c.pb[b][s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        }
-        c.q[s] = 0.0;
-        c.m[s] = 1.0;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
-        y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
-        x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
-        y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
-    }
-    if ((threadIdx.x & 31) == 0) c.gbox[0][s >> 5] = make_float4(x0, y0, x1, y1);
 }
 
 // An upload in the caller's order (staging arrays 0..3: x, y, vx, vy) put
