@@ -544,9 +544,42 @@ def run_gb300(args, world, rank, local):
         wb = W.batch256()
         # N > 1: whole clouds per rank, balanced by sum N^2 (no exchange)
         parts = assign_clouds([c.n for c in wb.clouds], world)
-        bt = DeviceBatch(ctx, [wb.clouds[c] for c in parts[rank]])
+        mine = [wb.clouds[c] for c in parts[rank]]
+        bt = DeviceBatch(ctx, mine)
         bt.step(4, wb.dt)
         torch.cuda.synchronize()
+        # like for like: the batched FP32C kernel and the plain FP64 kernel
+        # (one cloud at a time, the model split) over the same 4 steps from
+        # the same state (the batch's state after its warm-up steps)
+        bstate = [bt.split(a) for a in bt.download()]
+        start = []
+        for k, c0 in enumerate(mine):
+            c = c0.copy()
+            c.x, c.y, c.vx, c.vy = (bstate[a][k].copy() for a in range(4))
+            start.append(c)
+        pairs_like = 4.0 * 4 * sum(c.n * (c.n - 1) for c in mine)
+        b2 = DeviceBatch(ctx, start)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        b2.step(4, wb.dt)
+        b.record(stream)
+        torch.cuda.synchronize()
+        like32 = pairs_like / (a.elapsed_time(b) / 1e3)
+        b2.close()
+        ctx.set_autotune(False)
+        singles = [DeviceCloud.from_cloud(ctx, c) for c in start]
+        torch.cuda.synchronize()
+        a.record(stream)
+        for cl in singles:
+            cl.step(4, wb.dt, "fp64")
+        b.record(stream)
+        torch.cuda.synchronize()
+        like64 = pairs_like / (a.elapsed_time(b) / 1e3)
+        for cl in singles:
+            cl.close()
+        ctx.set_autotune(True)
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         barrier()
@@ -562,6 +595,8 @@ def run_gb300(args, world, rank, local):
         batch = {"workload": wb.name, "value": 4.0 * wb.pairs_per_eval * args.batch_steps / el,
                  "unit": UNIT, "steps": args.batch_steps, "ms_per_step": el / args.batch_steps * 1e3,
                  "variant": name, "work_items": nitems, "persistent_grid": grid,
+                 "like_for_like_4_steps": {"fp32c_batched": like32, "fp64_one_cloud_at_a_time": like64,
+                                           "fp32c_over_fp64": like32 / like64},
                  "graph_captured": args.batch_steps >= 16,
                  "swept_pair_fraction": (bswept / (4.0 * sum(wb.clouds[c].n * (wb.clouds[c].n - 1)
                                                               for c in parts[rank]) * args.batch_steps)
