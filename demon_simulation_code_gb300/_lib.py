@@ -107,8 +107,10 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_void_p)]),
     "dm_cloud_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dm_cloud_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
-    "dm_cloud_upload": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
-    "dm_cloud_download": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
+    # the per-step state transfers take plain addresses (addr): building a
+    # typed pointer per array costs more than the rest of the call's host work
+    "dm_cloud_upload": (ctypes.c_int, [ctypes.c_void_p] * 5),
+    "dm_cloud_download": (ctypes.c_int, [ctypes.c_void_p] * 5),
     "dm_cloud_set_charge_mass": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     "dm_cloud_set_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ForceParams)]),
     "dm_cloud_eval_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
@@ -204,3 +206,10 @@ def ptr(a: np.ndarray):
     if a.dtype != np.float64 or not a.flags.c_contiguous:
         raise TypeError("expected a C-contiguous float64 array")
     return a.ctypes.data_as(_dp)
+
+
+def addr(a: np.ndarray) -> int:
+    """The address of a C-contiguous float64 array (for c_void_p arguments)."""
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data

@@ -13,7 +13,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import DM_FP32C, DM_FP64, check, ptr
+from ._lib import DM_FP32C, DM_FP64, addr, check, ptr
 
 PRECISIONS = {"fp64": DM_FP64, "fp32c": DM_FP32C, DM_FP64: DM_FP64, DM_FP32C: DM_FP32C}
 
@@ -124,7 +124,7 @@ class DeviceCloud:
 
     def upload(self, x, y, vx, vy):
         a = [np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, vx, vy)]
-        self._chk(self.lib.dm_cloud_upload(self.h, *(ptr(v) for v in a)))
+        self._chk(self.lib.dm_cloud_upload(self.h, *(addr(v) for v in a)))
 
     def download(self, out=None):
         """x, y, vx, vy in the caller's order; `out`: four contiguous float64
@@ -137,7 +137,7 @@ class DeviceCloud:
             if len(out) != 4 or any(not (isinstance(v, np.ndarray) and v.dtype == np.float64 and
                                          v.flags.c_contiguous and v.size == self.n) for v in out):
                 raise ValueError("download(out=...): four contiguous float64 arrays of length n")
-        self._chk(self.lib.dm_cloud_download(self.h, *(ptr(v) for v in out)))
+        self._chk(self.lib.dm_cloud_download(self.h, *(addr(v) for v in out)))
         return tuple(out)
 
     def set_charge_mass(self, q=None, m=None):

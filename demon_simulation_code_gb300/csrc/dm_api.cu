@@ -722,6 +722,20 @@ int run_steps(dm_cloud *c, int nsteps, double dt, int precision) {
     return enqueue_steps(c, nsteps - reps * kGraphSteps, dt, precision);
 }
 
+// The device's own address of a caller's host buffer when the device may
+// dereference it (page-locked host memory: cudaHostAlloc, cudaMallocHost,
+// cudaHostRegister, torch's pin_memory), else nullptr: then the buffer is
+// copied by DMA.  On GB300 such buffers are read and written over
+// NVLink-C2C by the copy kernel, one launch for all four arrays.
+const void *device_view(const void *p) {
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -992,10 +1006,19 @@ int dm_cloud_upload(dm_cloud *c, const double *x, const double *y, const double 
     // caller order -> staging -> the cloud's current internal order (charges,
     // masses and the order stay; stage buffer 0 and its boxes are rewritten)
     double **st = c->sort.stage;
-    DM_CUDA(ctx, cudaMemcpyAsync(st[0], x, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    DM_CUDA(ctx, cudaMemcpyAsync(st[1], y, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    DM_CUDA(ctx, cudaMemcpyAsync(st[2], vx, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    DM_CUDA(ctx, cudaMemcpyAsync(st[3], vy, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    const void *dv[4] = {device_view(x), device_view(y), device_view(vx), device_view(vy)};
+    if (dv[0] && dv[1] && dv[2] && dv[3]) {
+        copy4<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->n, (const double *)dv[0], (const double *)dv[1],
+                                                           (const double *)dv[2], (const double *)dv[3], st[0],
+                                                           st[1], st[2], st[3], nullptr, nullptr);
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches += 1;
+    } else {
+        DM_CUDA(ctx, cudaMemcpyAsync(st[0], x, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        DM_CUDA(ctx, cudaMemcpyAsync(st[1], y, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        DM_CUDA(ctx, cudaMemcpyAsync(st[2], vx, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        DM_CUDA(ctx, cudaMemcpyAsync(st[3], vy, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
     upload_internal_order<<<(c->n_pad + 255) / 256, 256, 0, ctx->stream>>>(c->d, c->sort);
     c->boxes_valid[0] = true;
     c->boxes_valid[1] = false;
@@ -1015,13 +1038,23 @@ int dm_cloud_download(dm_cloud *c, double *x, double *y, double *vx, double *vy)
         c->d.orig, c->n, c->d.x, c->d.y, c->d.vx, c->d.vy, st[0], st[1], st[2], st[3]);
     DM_CUDA(ctx, cudaGetLastError());
     ctx->launches++;
-    if (x) DM_CUDA(ctx, cudaMemcpyAsync(x, st[0], bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, st[1], bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, st[2], bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    if (vy) DM_CUDA(ctx, cudaMemcpyAsync(vy, st[3], bytes, cudaMemcpyDeviceToHost, ctx->stream));
     // the error flags come back with the state: one synchronisation
     if (!ctx->h_err) DM_CUDA(ctx, cudaMallocHost((void **)&ctx->h_err, sizeof(int)));
-    DM_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    const void *dv[4] = {device_view(x), device_view(y), device_view(vx), device_view(vy)};
+    int *err_dv = (int *)device_view(ctx->h_err);
+    if (dv[0] && dv[1] && dv[2] && dv[3] && err_dv) {
+        copy4<<<(c->n + 255) / 256, 256, 0, ctx->stream>>>(c->n, st[0], st[1], st[2], st[3], (double *)dv[0],
+                                                           (double *)dv[1], (double *)dv[2], (double *)dv[3],
+                                                           c->d.err, err_dv);
+        DM_CUDA(ctx, cudaGetLastError());
+        ctx->launches++;
+    } else {
+        if (x) DM_CUDA(ctx, cudaMemcpyAsync(x, st[0], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (y) DM_CUDA(ctx, cudaMemcpyAsync(y, st[1], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (vx) DM_CUDA(ctx, cudaMemcpyAsync(vx, st[2], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (vy) DM_CUDA(ctx, cudaMemcpyAsync(vy, st[3], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        DM_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    }
     DM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return device_error_status(ctx, c, *ctx->h_err);
 }

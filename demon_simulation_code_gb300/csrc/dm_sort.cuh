@@ -662,6 +662,22 @@ static __global__ void scatter_to_caller(const int *__restrict__ orig, int n, co
     if (a3) o3[o] = a3[s];
 }
 
+// Four arrays of n doubles copied element for element (coalesced on both
+// sides): caller buffers in page-locked host memory read or written by the
+// device itself over the host link, in place of four DMA copies.  err_src /
+// err_dst (optional): the device error word copied along with them.
+static __global__ void copy4(int n, const double *__restrict__ i0, const double *__restrict__ i1,
+                             const double *__restrict__ i2, const double *__restrict__ i3, double *o0,
+                             double *o1, double *o2, double *o3, const int *err_src, int *err_dst) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (err_dst && s == 0) *err_dst = *err_src;
+    if (s >= n) return;
+    o0[s] = i0[s];
+    o1[s] = i1[s];
+    o2[s] = i2[s];
+    o3[s] = i3[s];
+}
+
 // out[s] = in[orig[s]] for up to two arrays (caller -> internal order).
 static __global__ void gather_from_caller(const int *__restrict__ orig, int n, const double *i0,
                                           const double *i1, double *o0, double *o1) {

@@ -177,7 +177,10 @@ int dm_cloud_destroy(dm_cloud *cloud);
 int dm_cloud_size(const dm_cloud *cloud, int *n);
 
 /* Host -> device state (positions, velocities); charges/masses unchanged.
- * Replaces writing Cloud::x/y/Vx/Vy directly (Cloud.h:22). */
+ * Replaces writing Cloud::x/y/Vx/Vy directly (Cloud.h:22).  Page-locked
+ * buffers (any for which cudaPointerGetAttributes gives a device address)
+ * are read by one device copy kernel; other memory is copied by DMA.  The
+ * same holds for dm_cloud_download's outputs. */
 int dm_cloud_upload(dm_cloud *cloud, const double *x, const double *y,
                     const double *vx, const double *vy);
 

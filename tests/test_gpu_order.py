@@ -111,3 +111,39 @@ def test_two_axis_finish_gives_the_per_particle_finish_bits(gpu_ctx):
         c.close()
     for a, b in zip(*runs):
         assert np.array_equal(a, b)
+
+
+def test_page_locked_buffers_are_copied_by_the_device_with_the_same_bits(gpu_ctx):
+    """Page-locked caller buffers are read and written by a copy kernel (one
+    launch per direction, no DMA copies); the state and trajectory must be
+    the same bits as through pageable buffers."""
+    torch = pytest.importorskip("torch")
+    n = 5000
+    c0 = W.disk_cloud(n, 2e-2, 7)
+    rng = np.random.default_rng(9)
+    new = [rng.normal(0.0, 1e-2 if k < 2 else 1e-3, size=n) for k in range(4)]
+    pinned = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+    out = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+    for p, v in zip(pinned, new):
+        p[:] = v
+    a = DeviceCloud.from_cloud(gpu_ctx, c0)
+    b = DeviceCloud.from_cloud(gpu_ctx, c0)
+    a.step(2, DT, "fp32c")
+    b.step(2, DT, "fp32c")
+    l0 = gpu_ctx.launch_count()
+    a.upload(*pinned)
+    assert gpu_ctx.launch_count() - l0 == 2  # the copy kernel and the reorder into internal order
+    b.upload(*new)
+    back = a.download(out=out)
+    for x, y in zip(back, new):
+        assert np.array_equal(x, y)
+    a.step(3, DT, "fp32c")
+    b.step(3, DT, "fp32c")
+    l0 = gpu_ctx.launch_count()
+    ga = a.download(out=out)
+    assert gpu_ctx.launch_count() - l0 == 2  # the scatter to caller order and the copy kernel
+    gb = b.download()
+    for x, y in zip(ga, gb):
+        assert np.array_equal(x, y)
+    a.close()
+    b.close()
