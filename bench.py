@@ -553,8 +553,8 @@ def run_gb300(args, world, rank, local):
         # the same state (the batch's state after its warm-up steps)
         bstate = [bt.split(a) for a in bt.download()]
         start = []
-        for k, c0 in enumerate(mine):
-            c = c0.copy()
+        for k, cb in enumerate(mine):
+            c = cb.copy()
             c.x, c.y, c.vx, c.vy = (bstate[a][k].copy() for a in range(4))
             start.append(c)
         pairs_like = 4.0 * 4 * sum(c.n * (c.n - 1) for c in mine)
