@@ -208,26 +208,47 @@ static __global__ void __launch_bounds__(kSortThreads) radix_hist(const uint32_t
     if (threadIdx.x < kSortBuckets) hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of len entries in one block of 1024 threads.
+// Exclusive scan of len entries in one block of 1024 threads.  Warp w owns
+// the w-th of 32 consecutive segments and reads it 32 entries at a time
+// (lane l takes entry 32 r + l of the segment, so every load is one
+// coalesced row): first the segment's total, then, after a scan of the 32
+// totals, the segment again, row by row, each row scanned by shuffles on top
+// of the carried prefix.  (A thread per contiguous run of entries made every
+// warp load touch 32 cache lines: 110 us for the 65,536 entries of a
+// 262,144-particle sort.)
 static __global__ void __launch_bounds__(1024) radix_scan(uint32_t *hist, int len) {
-    __shared__ uint32_t part[1024];
-    const int per = (len + 1023) / 1024;
-    const int lo = threadIdx.x * per, hi = min(len, lo + per);
+    __shared__ uint32_t wsum[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int seg = (len + 31) / 32;
+    const int lo = min(len, warp * seg), hi = min(len, lo + seg);
     uint32_t s = 0;
-    for (int e = lo; e < hi; e++) s += hist[e];
-    part[threadIdx.x] = s;
+    for (int e = lo + lane; e < hi; e += 32) s += hist[e];
+    s = __reduce_add_sync(0xffffffffu, s);
+    if (lane == 0) wsum[warp] = s;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const uint32_t v = (threadIdx.x >= off) ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+    if (warp == 0) {  // exclusive prefix of the 32 segment totals
+        const uint32_t v = wsum[lane];
+        uint32_t inc = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += t;
+        }
+        wsum[lane] = inc - v;
     }
-    uint32_t run = part[threadIdx.x] - s;  // exclusive prefix of this segment
-    for (int e = lo; e < hi; e++) {
-        const uint32_t v = hist[e];
-        hist[e] = run;
-        run += v;
+    __syncthreads();
+    uint32_t carry = wsum[warp];
+    for (int r = lo; r < hi; r += 32) {
+        const int e = r + lane;
+        const uint32_t v = (e < hi) ? hist[e] : 0u;
+        uint32_t inc = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += t;
+        }
+        if (e < hi) hist[e] = carry + inc - v;
+        carry += __shfl_sync(0xffffffffu, inc, 31);
     }
 }
 
